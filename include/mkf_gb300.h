@@ -1,0 +1,168 @@
+/*
+ * mkf_gb300.h -- C ABI of the GB300 (sm_103a) filtering hot path of the
+ * mkfbodytracker_pdaf upper-body tracker.
+ *
+ * One shared library (libmkf_gb300.so) exports every function below.  All
+ * signatures use plain pointers, sizes and POD structs; device pointers are
+ * named d_*, host pointers have no prefix.  Every call that touches the GPU
+ * takes a stream (a cudaStream_t passed as mkf_stream_t; NULL = legacy default
+ * stream).  Every function returns an MKF_* status; no exception or C++ type
+ * crosses the ABI.  A handle is single-stream and not thread-safe; distinct
+ * handles are independent (the reference's filters are likewise driven from
+ * one ROS spin thread, pfPoseTracker.cpp:11).
+ *
+ * Randomness: the reference draws from cv::RNG(getTickCount()) per resample
+ * (pf2DRao.cpp:179), cv::theRNG in randn (pf2DRao.cpp:96) and rand()
+ * (pf2D.cpp:228,255), so its runs are not reproducible.  Here every draw is
+ * Philox4x32-10 keyed by (seed, track) and counted by (frame, item, stream),
+ * or an explicit uniform passed by the caller, so CPU and GPU see the same
+ * draws.  Layout of one particle-frame's draws: ceil(d/4) Philox blocks at
+ * streams 0..; words 2p,2p+1 give Box-Muller pair p (top 24 bits); the
+ * component uniform is the low bytes of words 0..2.  Resampling uniform of
+ * frame f: word 0 of block (f, 0xFFFFFFFF, 0x100).  Prior draws use frame
+ * 0xFFFFFFFF.
+ */
+#ifndef MKF_GB300_H
+#define MKF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* mkf_stream_t;   /* == cudaStream_t */
+
+enum {
+  MKF_OK = 0,
+  MKF_ERR_ARG = 1,       /* bad argument / size out of range */
+  MKF_ERR_CUDA = 2,      /* a CUDA runtime call failed (message in mkf_last_error) */
+  MKF_ERR_NONPD = 3,     /* innovation covariance not positive definite */
+  MKF_ERR_NAN = 4,       /* NaN/Inf produced */
+  MKF_ERR_TIMEOUT = 5,   /* a bounded device wait gave up */
+  MKF_ERR_NOMEM = 6,     /* allocation failed */
+  MKF_ERR_STATE = 7      /* call out of order (e.g. update before reset) */
+};
+
+/* per-track / per-filter status bits (returned in status arrays) */
+enum {
+  MKF_ST_FALLBACK = 1,   /* a resampling step took the max-weight-0 fallback
+                            (pf2DRao.cpp:184-192) */
+  MKF_ST_NAN = 2,        /* a NaN/Inf log-likelihood was seen */
+  MKF_ST_NONPD = 4,      /* an innovation covariance was not positive definite */
+  MKF_ST_TRUNC = 8       /* a detection list longer than MKF_MAX_DET was truncated */
+};
+
+#define MKF_MAX_D 24       /* state dimension (PCA dims) */
+#define MKF_MAX_K 32       /* mixture components */
+#define MKF_MAX_J 4        /* measured joints */
+#define MKF_MAX_DET 16     /* detections per joint list */
+#define MKF_MAX_M 8        /* RBPF measurement rows */
+
+const char* mkf_version(void);
+/* message of the last failing call on this thread ("" if none) */
+const char* mkf_last_error(void);
+
+/* ------------------------------------------------------------------ K1 draws */
+/* Host Philox4x32-10 block: key = {lo32(seed), hi32(seed) ^ track},
+ * ctr = {frame, item, stream, 0}. */
+int mkf_philox_block(uint64_t seed, uint32_t track, uint32_t frame, uint32_t item,
+                     uint32_t stream, uint32_t out[4]);
+/* The exact per-particle draws the particle kernels use for items 0..n-1 of
+ * one frame: d_eps (n*d normals, row per particle), d_ucomp (n component
+ * uniforms).  Replaces randn (pf2DRao.cpp:96) / pf2D.cpp:151-153. */
+int mkf_draw_particles(uint64_t seed, uint32_t track, uint32_t frame, int n, int d,
+                       float* d_eps, float* d_ucomp, mkf_stream_t stream);
+
+/* ------------------------------------------------------- A6 systematic resample */
+/* ParticleFilter::resample(weights, N) (pf2DRao.cpp:175-210).  Weights are
+ * quantised to 64-bit integers with 40 bits below the largest (exact power-of-
+ * two scaling, truncation) and resampled exactly: idx[i] = first j with
+ * Q_j >= (i + U/2^32) Q_{L-1} / N (ties to the lower index, as the wheel's
+ * strict '>').  All-zero/NaN weights take the reference's uniform-random
+ * fallback (pf2DRao.cpp:184-192) with idx_i = floor(u_i L),
+ * u_i = Philox(key {U, 0x5EED}, ctr {i,0,0,0}).  d_fallback (optional, one int)
+ * receives 1 if the fallback was taken.  L, N <= 2^23. */
+int mkf_resample_f64(const double* d_w, int L, int N, uint32_t U, int* d_idx,
+                     int* d_fallback, mkf_stream_t stream);
+int mkf_resample_f32(const float* d_w, int L, int N, uint32_t U, int* d_idx,
+                     int* d_fallback, mkf_stream_t stream);
+
+/* ------------------------------------------- A1/A13 mixture-of-MRRW motion model */
+/* Stacked per-model arrays (leading dimension n_models), all host pointers.
+ * Config form of my_gmm::loadGaussian (my_gmm.cpp:45-75): F_k = diag(a_k),
+ * B_k = (I - A_k) mu_k, Q_k = Lq_k Lq_k^T, prior N(mu_k, S0_k S0_k^T), mixture
+ * weights pi.  Measurement: joint j pixel = pinhole(Bm_j x + mm_j). */
+typedef struct mkf_bpf_models {
+  int n_models, d, K, J;
+  const float* a;     /* n*K*d */
+  const float* mu;    /* n*K*d */
+  const float* Lq;    /* n*K*d(d+1)/2, packed lower row-major */
+  const float* S0c;   /* n*K*d(d+1)/2 */
+  const float* pi;    /* n*K (cumulated in float32, sequentially, by the library) */
+  const float* Bm;    /* n*J*3*d */
+  const float* mm;    /* n*J*3 */
+  float fx, fy, cx, cy;
+} mkf_bpf_models;
+
+typedef struct mkf_bpf_track {
+  int32_t n_particles;   /* 1 .. 2^22 (batched: 1 .. 8192) */
+  int32_t n_frames;
+  int64_t frame_base;    /* first global frame index of this track */
+  uint64_t seed;
+  uint32_t track_id;     /* Philox key component */
+  int32_t model_index;
+  float kappa;           /* clutter density, detections per px^2 (> 0) */
+  float p_detect;        /* in (0, 1) */
+  float sigma_px;        /* detection noise std, px */
+} mkf_bpf_track;
+
+/* ---- plain per-track bootstrap PF (pf2D ParticleFilter API, pf2D.h:25-51,
+ * with the mixture motion model): construct / reset / update / estimate. */
+typedef struct mkf_bpf* mkf_bpf_t;
+int mkf_bpf_create(const mkf_bpf_models* models, const mkf_bpf_track* track, mkf_bpf_t* out);
+/* prior draw x ~ N(mu_k, Sigma_k), k ~ pi (my_gmm::resetTracker, my_gmm.cpp:30-42) */
+int mkf_bpf_reset(mkf_bpf_t h, mkf_stream_t stream);
+/* one frame (pf2D.cpp:148-210 order: predict from the resampled set, weight,
+ * estimate, resample).  d_det_off: J+1 offsets into d_det (x,y pairs).
+ * Writes the frame's weighted-mean state (d), log-likelihood increment and ESS
+ * to the optional device pointers. */
+int mkf_bpf_update(mkf_bpf_t h, uint32_t frame, const int* d_det_off, const float* d_det,
+                   float* d_est, float* d_loglik, float* d_ess, mkf_stream_t stream);
+/* debug copies of the last update into caller device buffers (any may be NULL):
+ * particles after propagation (SoA d x N), log-weights (N), normalised-to-max
+ * weights (N; only filled while debug is enabled) and the ancestors drawn (N) */
+int mkf_bpf_set_debug(mkf_bpf_t h, int enable);
+int mkf_bpf_read_debug(mkf_bpf_t h, float* d_x, float* d_logw, float* d_w, int* d_anc,
+                       mkf_stream_t stream);
+int mkf_bpf_status(mkf_bpf_t h, int* status);
+int mkf_bpf_destroy(mkf_bpf_t h);
+
+/* ---- batched uneven tracks: one persistent kernel over all tracks */
+typedef struct mkf_bpf_batch* mkf_bpf_batch_t;
+/* tracks: n_tracks descriptors; n_frames_total = sum of n_frames (global frame
+ * index space); detections are per (global frame g, joint j) lists
+ * det[det_off[g*J+j] .. det_off[g*J+j+1]). */
+int mkf_bpf_batch_create(const mkf_bpf_models* models, int n_tracks, const mkf_bpf_track* tracks,
+                         int64_t n_frames_total, mkf_bpf_batch_t* out);
+/* tuning: threads per CTA (64..512, multiple of 32) and CTAs per SM (0 = max) */
+int mkf_bpf_batch_set_tuning(mkf_bpf_batch_t h, int block_threads, int ctas_per_sm);
+/* device-resident run: outputs est (G*d), loglik (G), ess (G), status (n_tracks) */
+int mkf_bpf_batch_run(mkf_bpf_batch_t h, const int* d_det_off, const float* d_det,
+                      float* d_est, float* d_loglik, float* d_ess, int* d_status,
+                      mkf_stream_t stream);
+/* host-buffer run: copies detections in, runs, copies outputs out, synchronises.
+ * n_det = number of (x,y) pairs in det. */
+int mkf_bpf_batch_run_host(mkf_bpf_batch_t h, const int* det_off, const float* det, int64_t n_det,
+                           float* est, float* loglik, float* ess, int* status,
+                           mkf_stream_t stream);
+/* debug capture of one track's per-frame weights and ancestors (n_frames*N
+ * each, device pointers; NULL disables) */
+int mkf_bpf_batch_set_debug(mkf_bpf_batch_t h, int track, float* d_w, int* d_anc);
+int mkf_bpf_batch_destroy(mkf_bpf_batch_t h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

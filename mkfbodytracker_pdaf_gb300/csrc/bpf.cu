@@ -1,0 +1,1050 @@
+// bpf.cu -- bootstrap particle filter over the mixture-of-MRRW motion model.
+//
+// Reference structure: pf2D ParticleFilter::update/predict/resample
+// (pf2D.cpp:148-210, 90-102, 225-268) with the motion of my_gmm/KF_model
+// (my_gmm.cpp:53-58: x' = g x + (1-g) mu, Q = (1-g^2) Sigma, generalised to
+// A_k = diag(a_k), Q_k = Lq_k Lq_k^T), and the PDA clutter likelihood whose
+// reference analogue is the Pa/clutter-floor mixture at pfPose.cpp:261.
+//
+// Two launch shapes share the per-particle device code:
+//  * batched: one persistent kernel; each CTA owns one track at a time and
+//    runs all its frames with the weights, scan and ancestors in shared
+//    memory (particle states in a per-CTA global slot, L2-resident);
+//  * streaming: one track with up to 2^22 particles, three grid-wide kernels
+//    per frame (propagate+score+partials, quantised block sums, search).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "mkf_common.cuh"
+
+namespace mkf {
+
+constexpr float kZMin = 0.05f;
+constexpr float kTwoPi = 6.283185307179586f;
+
+// ------------------------------------------------------------------ model
+struct DevModels {
+  int n, d, K, J;
+  bool diag;          // every Lq_k diagonal
+  float *a, *mb, *mu, *Lq, *Ld, *S0c, *cumpi, *Bm, *mm;   // device
+  float fx, fy, cx, cy;
+};
+
+static void free_models(DevModels& m) {
+  float* ps[] = {m.a, m.mb, m.mu, m.Lq, m.Ld, m.S0c, m.cumpi, m.Bm, m.mm};
+  for (float* p : ps) if (p) cudaFree(p);
+  memset(&m, 0, sizeof(m));
+}
+
+static int upload(float** dst, const std::vector<float>& src) {
+  MKF_CUDA(cudaMalloc(dst, std::max<size_t>(1, src.size()) * sizeof(float)));
+  MKF_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return MKF_OK;
+}
+
+static int build_models(const mkf_bpf_models* M, DevModels& out) {
+  MKF_ARG(M && M->n_models > 0, "models: n_models must be > 0");
+  MKF_ARG(M->d == 12 || M->d == 24, "models: d must be 12 or 24");
+  MKF_ARG(M->K >= 1 && M->K <= MKF_MAX_K, "models: K out of range");
+  MKF_ARG(M->J >= 1 && M->J <= MKF_MAX_J, "models: J out of range");
+  MKF_ARG(M->a && M->mu && M->Lq && M->S0c && M->pi && M->Bm && M->mm, "models: null array");
+  const int n = M->n_models, d = M->d, K = M->K, J = M->J, DD = d * (d + 1) / 2;
+  const size_t nKd = (size_t)n * K * d;
+  std::vector<float> mb(nKd), Ld(nKd), cum((size_t)n * K);
+  bool diag = true;
+  for (size_t i = 0; i < nKd; ++i)
+    mb[i] = (float)((1.0 - (double)M->a[i]) * (double)M->mu[i]);
+  for (int p = 0; p < n; ++p)
+    for (int k = 0; k < K; ++k) {
+      const float* L = M->Lq + ((size_t)p * K + k) * DD;
+      for (int r = 0; r < d; ++r) {
+        for (int c = 0; c < r; ++c) if (L[r * (r + 1) / 2 + c] != 0.0f) diag = false;
+        Ld[((size_t)p * K + k) * d + r] = L[r * (r + 1) / 2 + r];
+      }
+    }
+  for (int p = 0; p < n; ++p) {   // sequential float32 cumulation (the oracle reads this array)
+    float acc = 0.0f;
+    for (int c = 0; c < K; ++c) { acc += M->pi[(size_t)p * K + c]; cum[(size_t)p * K + c] = acc; }
+  }
+  memset(&out, 0, sizeof(out));
+  out.n = n; out.d = d; out.K = K; out.J = J; out.diag = diag;
+  out.fx = M->fx; out.fy = M->fy; out.cx = M->cx; out.cy = M->cy;
+  auto vec = [](const float* p, size_t cnt) { return std::vector<float>(p, p + cnt); };
+  int st;
+  if ((st = upload(&out.a, vec(M->a, nKd)))) return st;
+  if ((st = upload(&out.mb, mb))) return st;
+  if ((st = upload(&out.mu, vec(M->mu, nKd)))) return st;
+  if ((st = upload(&out.Lq, vec(M->Lq, (size_t)n * K * DD)))) return st;
+  if ((st = upload(&out.Ld, Ld))) return st;
+  if ((st = upload(&out.S0c, vec(M->S0c, (size_t)n * K * DD)))) return st;
+  if ((st = upload(&out.cumpi, cum))) return st;
+  if ((st = upload(&out.Bm, vec(M->Bm, (size_t)n * J * 3 * d)))) return st;
+  if ((st = upload(&out.mm, vec(M->mm, (size_t)n * J * 3)))) return st;
+  return MKF_OK;
+}
+
+// ------------------------------------------------------------------ per-particle math
+// parameters of one model as seen by one particle (pointers into shared or global)
+struct PView {
+  const float *a, *mb, *mu, *Lq, *Ld, *S0c, *cumpi, *Bm, *mm;
+  int K, J;
+  float fx, fy, cx, cy;
+};
+
+__device__ __forceinline__ int pick_component(const float* cumpi, int K, float u) {
+  int k = 0;
+  while (k < K - 1 && !(u < cumpi[k])) ++k;
+  return k;
+}
+
+template <int D>
+__device__ __forceinline__ void prior_sample(const PView& p, const float* eps, float uc, float* x) {
+  constexpr int DD = D * (D + 1) / 2;
+  int k = pick_component(p.cumpi, p.K, uc);
+  const float* L = p.S0c + k * DD;
+#pragma unroll
+  for (int r = 0; r < D; ++r) {
+    float s = p.mu[k * D + r];
+#pragma unroll
+    for (int c = 0; c <= r; ++c) s = fmaf(L[r * (r + 1) / 2 + c], eps[c], s);
+    x[r] = s;
+  }
+}
+
+template <int D, bool DIAG>
+__device__ __forceinline__ void propagate(const PView& p, const float* eps, float uc, float* x) {
+  constexpr int DD = D * (D + 1) / 2;
+  int k = pick_component(p.cumpi, p.K, uc);
+  const float* a = p.a + k * D;
+  const float* mb = p.mb + k * D;
+  if (DIAG) {
+    const float* l = p.Ld + k * D;
+#pragma unroll
+    for (int r = 0; r < D; ++r) x[r] = fmaf(l[r], eps[r], fmaf(a[r], x[r], mb[r]));
+  } else {
+    const float* L = p.Lq + k * DD;
+    float xn[D];
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      float s = fmaf(a[r], x[r], mb[r]);
+#pragma unroll
+      for (int c = 0; c <= r; ++c) s = fmaf(L[r * (r + 1) / 2 + c], eps[c], s);
+      xn[r] = s;
+    }
+#pragma unroll
+    for (int r = 0; r < D; ++r) x[r] = xn[r];
+  }
+}
+
+// log[(1-P_D) kappa + P_D sum_i N(z_i; pi(x), sigma^2 I)] summed over measured joints
+template <int D>
+__device__ __forceinline__ float loglik(const PView& p, const float* x, const int* cnt,
+                                        const float2* det, float kappa, float pd, float sigma) {
+  const float inv2s2 = 0.5f / (sigma * sigma);
+  const float norm = pd / (kTwoPi * sigma * sigma);
+  const float floor_ = (1.0f - pd) * kappa;
+  float ll = 0.0f;
+  for (int j = 0; j < p.J; ++j) {
+    const float* B = p.Bm + j * 3 * D;
+    float q0 = p.mm[j * 3 + 0], q1 = p.mm[j * 3 + 1], q2 = p.mm[j * 3 + 2];
+#pragma unroll
+    for (int c = 0; c < D; ++c) {
+      q0 = fmaf(B[c], x[c], q0);
+      q1 = fmaf(B[D + c], x[c], q1);
+      q2 = fmaf(B[2 * D + c], x[c], q2);
+    }
+    if (!(q2 > kZMin)) { ll += __logf(kappa); continue; }
+    float iz = 1.0f / q2;
+    float u = fmaf(p.fx * q0, iz, p.cx), v = fmaf(p.fy * q1, iz, p.cy);
+    float acc = 0.0f;
+    const float2* dj = det + j * MKF_MAX_DET;
+    for (int i = 0; i < cnt[j]; ++i) {
+      float dx = dj[i].x - u, dy = dj[i].y - v;
+      acc += __expf(-(dx * dx + dy * dy) * inv2s2);
+    }
+    ll += __logf(fmaf(norm, acc, floor_));
+  }
+  return ll;
+}
+
+// ------------------------------------------------------------------ batched persistent kernel
+struct BatchArgs {
+  int n_tracks, K, J, Nmax;
+  const int4* meta;                 // n_particles, n_frames, model_index, track_id
+  const long long* fbase;
+  const unsigned long long* seed;
+  const float4* obs;                // kappa, p_detect, sigma, 0
+  const int* order;
+  int* counter;
+  DevModels m;
+  const int* det_off;
+  const float2* det;
+  float* est;
+  float* loglik;
+  float* ess;
+  int* status;
+  float* scratch;                   // gridDim.x * 2 * D * Nmax
+  int dbg_track;
+  float* dbg_w;
+  int* dbg_anc;
+};
+
+template <int D>
+__host__ __device__ constexpr int params_floats(int K, int J, bool diag) {
+  return 2 * K * D + (diag ? K * D : K * D * (D + 1) / 2) + K + J * 3 * D + J * 3;
+}
+
+template <int D, bool DIAG>
+__global__ void __launch_bounds__(512) bpf_batched_kernel(BatchArgs A) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int TB = blockDim.x, tid = threadIdx.x;
+  constexpr int NV = D + 3;
+  uint64_t* sQ = reinterpret_cast<uint64_t*>(smem);                      // 8 Nmax
+  int* sA = reinterpret_cast<int*>(smem + 8 * (size_t)A.Nmax);           // 4 Nmax
+  float* sP = reinterpret_cast<float*>(smem + 12 * (size_t)A.Nmax);      // params
+  const int K = A.K, J = A.J;
+  float* s_a = sP;
+  float* s_mb = s_a + K * D;
+  float* s_L = s_mb + K * D;
+  float* s_cum = s_L + (DIAG ? K * D : K * D * (D + 1) / 2);
+  float* s_Bm = s_cum + K;
+  float* s_mm = s_Bm + J * 3 * D;
+  float2* s_det = reinterpret_cast<float2*>(sP + ((params_floats<D>(K, J, DIAG) + 1) & ~1));
+  int* s_cnt = reinterpret_cast<int*>(s_det + MKF_MAX_J * MKF_MAX_DET);
+  float* s_red = reinterpret_cast<float*>(s_cnt + 8);                    // 32*NV floats
+  uint64_t* s_red64 = reinterpret_cast<uint64_t*>(s_red + 32 * NV + 2);  // 33 u64 (aligned below)
+  s_red64 = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(s_red64) + 7) & ~uintptr_t(7));
+  __shared__ int s_item;
+  __shared__ int s_flag;
+
+  float* xa0 = A.scratch + (size_t)blockIdx.x * 2 * D * A.Nmax;
+  float* xb0 = xa0 + (size_t)D * A.Nmax;
+  const int Nmax = A.Nmax;
+
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(A.counter, 1);
+    __syncthreads();
+    const int item = s_item;
+    __syncthreads();
+    if (item >= A.n_tracks) break;
+    const int b = A.order[item];
+    const int4 mt = A.meta[b];
+    const int N = mt.x, T = mt.y, mi = mt.z;
+    const uint32_t trk = (uint32_t)mt.w;
+    const long long g0 = A.fbase[b];
+    const unsigned long long seed = A.seed[b];
+    const float4 ob = A.obs[b];
+    // stage this track's model in shared memory
+    {
+      const float* ga = A.m.a + (size_t)mi * K * D;
+      const float* gmb = A.m.mb + (size_t)mi * K * D;
+      const float* gL = DIAG ? A.m.Ld + (size_t)mi * K * D : A.m.Lq + (size_t)mi * K * D * (D + 1) / 2;
+      const float* gc = A.m.cumpi + (size_t)mi * K;
+      const float* gB = A.m.Bm + (size_t)mi * J * 3 * D;
+      const float* gm = A.m.mm + (size_t)mi * J * 3;
+      for (int i = tid; i < K * D; i += TB) { s_a[i] = ga[i]; s_mb[i] = gmb[i]; }
+      for (int i = tid; i < (DIAG ? K * D : K * D * (D + 1) / 2); i += TB) s_L[i] = gL[i];
+      for (int i = tid; i < K; i += TB) s_cum[i] = gc[i];
+      for (int i = tid; i < J * 3 * D; i += TB) s_Bm[i] = gB[i];
+      for (int i = tid; i < J * 3; i += TB) s_mm[i] = gm[i];
+      if (tid == 0) s_flag = 0;
+    }
+    __syncthreads();
+    PView pv;
+    pv.a = s_a; pv.mb = s_mb; pv.Lq = s_L; pv.Ld = s_L; pv.cumpi = s_cum; pv.Bm = s_Bm; pv.mm = s_mm;
+    pv.mu = A.m.mu + (size_t)mi * K * D;
+    pv.S0c = A.m.S0c + (size_t)mi * K * D * (D + 1) / 2;
+    pv.K = K; pv.J = J; pv.fx = A.m.fx; pv.fy = A.m.fy; pv.cx = A.m.cx; pv.cy = A.m.cy;
+    const bool dbg = (A.dbg_w != nullptr) && (b == A.dbg_track);
+
+    float* xa = xa0;
+    float* xb = xb0;
+    // prior draw (frame index 0xFFFFFFFF), identity ancestry
+    for (int i = tid; i < N; i += TB) {
+      float eps[D], x[D];
+      float uc = particle_draws<D>(seed, trk, kFramePrior, (uint32_t)i, eps);
+      prior_sample<D>(pv, eps, uc, x);
+#pragma unroll
+      for (int r = 0; r < D; ++r) xa[(size_t)r * Nmax + i] = x[r];
+      sA[i] = i;
+    }
+    __syncthreads();
+
+    for (int t = 0; t < T; ++t) {
+      const long long g = g0 + t;
+      // this frame's detection lists
+      if (tid < J) {
+        int lo = A.det_off[g * J + tid], hi = A.det_off[g * J + tid + 1];
+        int n = hi - lo;
+        if (n > MKF_MAX_DET) { n = MKF_MAX_DET; atomicOr(&s_flag, MKF_ST_TRUNC); }
+        s_cnt[tid] = n < 0 ? 0 : n;
+      }
+      __syncthreads();
+      for (int q = tid; q < J * MKF_MAX_DET; q += TB) {
+        int j = q / MKF_MAX_DET, i = q - j * MKF_MAX_DET;
+        if (i < s_cnt[j]) s_det[j * MKF_MAX_DET + i] = A.det[A.det_off[g * J + j] + i];
+      }
+      __syncthreads();
+
+      // ---- propagate from the resampled set and score
+      float lmax = -INFINITY;
+      for (int i = tid; i < N; i += TB) {
+        const int an = sA[i];
+        float x[D], eps[D];
+#pragma unroll
+        for (int r = 0; r < D; ++r) x[r] = xa[(size_t)r * Nmax + an];
+        float uc = particle_draws<D>(seed, trk, (uint32_t)t, (uint32_t)i, eps);
+        propagate<D, DIAG>(pv, eps, uc, x);
+#pragma unroll
+        for (int r = 0; r < D; ++r) xb[(size_t)r * Nmax + i] = x[r];
+        float ll = loglik<D>(pv, x, s_cnt, s_det, ob.x, ob.y, ob.z);
+        sA[i] = __float_as_int(ll);
+        lmax = fmaxf(lmax, ll);
+      }
+      const float M = block_max(lmax, s_red);
+      const bool fb = !(M > -INFINITY) || !(M < INFINITY);
+
+      // ---- normalised weights, weighted-mean estimate, ESS
+      float acc[NV];
+#pragma unroll
+      for (int c = 0; c < NV; ++c) acc[c] = 0.0f;   // s, s2, wmax, v[D]
+      for (int i = tid; i < N; i += TB) {
+        float ll = __int_as_float(sA[i]);
+        float w = fb ? 0.0f : (ll == M ? 1.0f : __expf(ll - M));
+        if (!(w >= 0.0f)) w = 0.0f;
+        sA[i] = __float_as_int(w);
+        if (dbg) A.dbg_w[(size_t)t * N + i] = w;
+        acc[0] += w;
+        acc[1] = fmaf(w, w, acc[1]);
+        acc[2] = fmaxf(acc[2], w);
+#pragma unroll
+        for (int r = 0; r < D; ++r) acc[3 + r] = fmaf(w, xb[(size_t)r * Nmax + i], acc[3 + r]);
+      }
+      {
+        const int lane = tid & 31, w = tid >> 5, nw = (TB + 31) >> 5;
+#pragma unroll
+        for (int c = 0; c < NV; ++c) acc[c] = (c == 2) ? warp_max(acc[c]) : warp_sum(acc[c]);
+        __syncthreads();
+        if (lane == 0)
+#pragma unroll
+          for (int c = 0; c < NV; ++c) s_red[w * NV + c] = acc[c];
+        __syncthreads();
+        if (tid < NV) {   // thread c alone reads column c, then stores its total in slot c
+          float r = 0.0f;
+          for (int q = 0; q < nw; ++q) r = (tid == 2) ? fmaxf(r, s_red[q * NV + tid]) : r + s_red[q * NV + tid];
+          s_red[tid] = r;
+        }
+        __syncthreads();
+      }
+      const float S = s_red[0], S2 = s_red[1], Wmax = s_red[2];
+      if (tid < D) A.est[(size_t)g * D + tid] = s_red[3 + tid] / S;
+      if (tid == 0) {
+        A.loglik[g] = M + __logf(S) - __logf((float)N);
+        A.ess[g] = S * S / S2;
+        if (fb) s_flag |= MKF_ST_FALLBACK | MKF_ST_NAN;
+      }
+      int e = 0;
+      frexpf(Wmax, &e);
+      __syncthreads();
+
+      // ---- quantise + exact prefix sums (contiguous chunk per thread)
+      const int E = (N + TB - 1) / TB;
+      const int j0 = min(N, tid * E), j1 = min(N, j0 + E);
+      uint64_t cs = 0;
+      for (int j = j0; j < j1; ++j) cs += quantize_f32(__int_as_float(sA[j]), e);
+      uint64_t Qt;
+      uint64_t pre = block_excl_scan_u64(cs, s_red64, &Qt);
+      for (int j = j0; j < j1; ++j) {
+        pre += quantize_f32(__int_as_float(sA[j]), e);
+        sQ[j] = pre;
+      }
+      __syncthreads();
+
+      // ---- systematic ancestors by exact search
+      const uint32_t U = resample_uniform(seed, trk, (uint32_t)t);
+      const bool fb2 = fb || Qt == 0;
+      for (int i = tid; i < N; i += TB) {
+        int an = fb2 ? resample_fallback_index(U, i, N) : resample_search(sQ, N, N, resample_rhs(i, U, Qt));
+        sA[i] = an;
+        if (dbg) A.dbg_anc[(size_t)t * N + i] = an;
+      }
+      __syncthreads();
+      float* tmp = xa; xa = xb; xb = tmp;
+    }
+    if (tid == 0) A.status[b] = s_flag;
+    __syncthreads();
+  }
+}
+
+static size_t batched_smem_bytes(int D, int Nmax, int K, int J, bool diag) {
+  size_t pf = (D == 12) ? params_floats<12>(K, J, diag) : params_floats<24>(K, J, diag);
+  size_t bytes = 12 * (size_t)Nmax + 4 * ((pf + 1) & ~size_t(1)) + 8 * MKF_MAX_J * MKF_MAX_DET + 32 +
+                 4 * (32 * (D + 3) + 2) + 8 * 34 + 16;
+  return (bytes + 15) & ~size_t(15);
+}
+
+// ------------------------------------------------------------------ streaming kernels (one track)
+struct FrameScalars {
+  float M;
+  int fb;
+  unsigned long long Qt;
+  unsigned int ticket_a, ticket_b;
+  int status;
+  int pad;
+};
+
+struct StreamArgs {
+  int N, tile_a, tile_b;
+  uint64_t seed;
+  uint32_t track, frame, U;
+  float kappa, pd, sigma;
+  PView pv;
+  const int* det_off;
+  const float2* det;
+  const int* anc;
+  const float* xa;
+  float* xb;
+  float* logw;
+  float* partial;         // nb_a * (D+3): m, s, s2, v[D]
+  unsigned long long* bsum;  // nb_b
+  FrameScalars* fs;
+  float* est;
+  float* out_loglik;
+  float* out_ess;
+  float* dbg_w;
+  int* anc_out;
+  bool prior;
+};
+
+// online merge of (m, s, s2, v) accumulators
+template <int D>
+__device__ __forceinline__ void merge_acc(float& m, float& s, float& s2, float* v, float m2, float t,
+                                          float t2, const float* v2) {
+  if (!(m2 > -INFINITY)) return;
+  if (!(m > -INFINITY)) {
+    m = m2; s = t; s2 = t2;
+#pragma unroll
+    for (int r = 0; r < D; ++r) v[r] = v2[r];
+    return;
+  }
+  float M = fmaxf(m, m2);
+  float f1 = __expf(m - M), f2 = __expf(m2 - M);
+  s = s * f1 + t * f2;
+  s2 = s2 * f1 * f1 + t2 * f2 * f2;
+#pragma unroll
+  for (int r = 0; r < D; ++r) v[r] = v[r] * f1 + v2[r] * f2;
+  m = M;
+}
+
+template <int D>
+__device__ void block_merge(float& m, float& s, float& s2, float* v, float* red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  constexpr int NV = D + 3;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    float m2 = __shfl_xor_sync(0xffffffffu, m, o);
+    float t = __shfl_xor_sync(0xffffffffu, s, o);
+    float t2 = __shfl_xor_sync(0xffffffffu, s2, o);
+    float v2[D];
+#pragma unroll
+    for (int r = 0; r < D; ++r) v2[r] = __shfl_xor_sync(0xffffffffu, v[r], o);
+    // symmetric merge so all lanes agree
+    float mm = m, ss = s, ss2 = s2, vv[D];
+#pragma unroll
+    for (int r = 0; r < D; ++r) vv[r] = v[r];
+    if (lane & o) {   // put the lower lane's value first for a fixed order
+      m = m2; s = t; s2 = t2;
+#pragma unroll
+      for (int r = 0; r < D; ++r) v[r] = v2[r];
+      merge_acc<D>(m, s, s2, v, mm, ss, ss2, vv);
+    } else {
+      merge_acc<D>(m, s, s2, v, m2, t, t2, v2);
+    }
+  }
+  __syncthreads();
+  if (lane == 0) {
+    red[w * NV + 0] = m; red[w * NV + 1] = s; red[w * NV + 2] = s2;
+#pragma unroll
+    for (int r = 0; r < D; ++r) red[w * NV + 3 + r] = v[r];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    m = red[0]; s = red[1]; s2 = red[2];
+#pragma unroll
+    for (int r = 0; r < D; ++r) v[r] = red[3 + r];
+    for (int q = 1; q < nw; ++q) merge_acc<D>(m, s, s2, v, red[q * NV], red[q * NV + 1], red[q * NV + 2], red + q * NV + 3);
+  }
+}
+
+template <int D, bool DIAG>
+__global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
+  __shared__ float2 s_det[MKF_MAX_J * MKF_MAX_DET];
+  __shared__ int s_cnt[MKF_MAX_J];
+  __shared__ float s_red[32 * (D + 3)];
+  __shared__ bool s_last;
+  const int tid = threadIdx.x, TB = blockDim.x;
+  const int J = A.pv.J;
+  if (!A.prior) {
+    if (tid < J) {
+      int n = A.det_off[tid + 1] - A.det_off[tid];
+      if (n > MKF_MAX_DET) { n = MKF_MAX_DET; if (blockIdx.x == 0) atomicOr(&A.fs->status, MKF_ST_TRUNC); }
+      s_cnt[tid] = n < 0 ? 0 : n;
+    }
+    __syncthreads();
+    for (int q = tid; q < J * MKF_MAX_DET; q += TB) {
+      int j = q / MKF_MAX_DET, i = q - j * MKF_MAX_DET;
+      if (i < s_cnt[j]) s_det[j * MKF_MAX_DET + i] = A.det[A.det_off[j] + i];
+    }
+    __syncthreads();
+  }
+  float m = -INFINITY, s = 0.0f, s2 = 0.0f, v[D];
+#pragma unroll
+  for (int r = 0; r < D; ++r) v[r] = 0.0f;
+  const int base = blockIdx.x * A.tile_a;
+  const int end = min(A.N, base + A.tile_a);
+  for (int i = base + tid; i < end; i += TB) {
+    float x[D], eps[D];
+    if (A.prior) {
+      float uc = particle_draws<D>(A.seed, A.track, kFramePrior, (uint32_t)i, eps);
+      prior_sample<D>(A.pv, eps, uc, x);
+#pragma unroll
+      for (int r = 0; r < D; ++r) A.xb[(size_t)r * A.N + i] = x[r];
+      continue;
+    }
+    const int an = A.anc[i];
+#pragma unroll
+    for (int r = 0; r < D; ++r) x[r] = A.xa[(size_t)r * A.N + an];
+    float uc = particle_draws<D>(A.seed, A.track, A.frame, (uint32_t)i, eps);
+    propagate<D, DIAG>(A.pv, eps, uc, x);
+#pragma unroll
+    for (int r = 0; r < D; ++r) A.xb[(size_t)r * A.N + i] = x[r];
+    float ll = loglik<D>(A.pv, x, s_cnt, s_det, A.kappa, A.pd, A.sigma);
+    A.logw[i] = ll;
+    // online accumulation
+    if (ll > m) {
+      float f = (m > -INFINITY) ? __expf(m - ll) : 0.0f;
+      s = s * f + 1.0f;
+      s2 = s2 * f * f + 1.0f;
+#pragma unroll
+      for (int r = 0; r < D; ++r) v[r] = fmaf(v[r], f, x[r]);
+      m = ll;
+    } else if (ll > -INFINITY) {
+      float w = __expf(ll - m);
+      s += w;
+      s2 = fmaf(w, w, s2);
+#pragma unroll
+      for (int r = 0; r < D; ++r) v[r] = fmaf(w, x[r], v[r]);
+    }
+  }
+  if (A.prior) return;
+  block_merge<D>(m, s, s2, v, s_red);
+  constexpr int NV = D + 3;
+  if (tid == 0) {
+    float* p = A.partial + (size_t)blockIdx.x * NV;
+    p[0] = m; p[1] = s; p[2] = s2;
+#pragma unroll
+    for (int r = 0; r < D; ++r) p[3 + r] = v[r];
+    __threadfence();
+    unsigned t = atomicAdd(&A.fs->ticket_a, 1u);
+    s_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  // last block: combine every block's partial in a fixed order
+  m = -INFINITY; s = 0.0f; s2 = 0.0f;
+#pragma unroll
+  for (int r = 0; r < D; ++r) v[r] = 0.0f;
+  for (int q = tid; q < (int)gridDim.x; q += TB) {
+    const volatile float* p = A.partial + (size_t)q * NV;
+    float v2[D];
+#pragma unroll
+    for (int r = 0; r < D; ++r) v2[r] = p[3 + r];
+    merge_acc<D>(m, s, s2, v, p[0], p[1], p[2], v2);
+  }
+  block_merge<D>(m, s, s2, v, s_red);
+  if (tid == 0) {
+    bool fb = !(m > -INFINITY) || !(m < INFINITY);
+    A.fs->M = m;
+    A.fs->fb = fb ? 1 : 0;
+    if (fb) A.fs->status |= MKF_ST_FALLBACK | MKF_ST_NAN;
+    A.fs->ticket_a = 0u;
+    if (A.est)
+      for (int r = 0; r < D; ++r) A.est[r] = v[r] / s;
+    if (A.out_loglik) *A.out_loglik = m + logf(s) - logf((float)A.N);
+    if (A.out_ess) *A.out_ess = s * s / s2;
+  }
+}
+
+__device__ __forceinline__ float stream_weight(float ll, float M, int fb) {
+  float w = fb ? 0.0f : (ll == M ? 1.0f : __expf(ll - M));
+  return (w >= 0.0f) ? w : 0.0f;
+}
+
+// block sums of quantised weights; the last block scans them (exclusive)
+__global__ void __launch_bounds__(256) bpf_stream_b(StreamArgs A) {
+  __shared__ uint64_t s_red64[34];
+  __shared__ bool s_last;
+  const int tid = threadIdx.x, TB = blockDim.x;
+  const float M = A.fs->M;
+  const int fb = A.fs->fb;
+  const int base = blockIdx.x * A.tile_b, end = min(A.N, base + A.tile_b);
+  const int E = (A.tile_b + TB - 1) / TB;
+  const int j0 = min(end, base + tid * E), j1 = min(end, j0 + E);
+  uint64_t cs = 0;
+  for (int j = j0; j < j1; ++j) {
+    float w = stream_weight(A.logw[j], M, fb);
+    if (A.dbg_w) A.dbg_w[j] = w;
+    cs += quantize_f32(w, 1);
+  }
+  uint64_t tot;
+  block_excl_scan_u64(cs, s_red64, &tot);
+  if (tid == 0) {
+    A.bsum[blockIdx.x] = tot;
+    __threadfence();
+    unsigned t = atomicAdd(&A.fs->ticket_b, 1u);
+    s_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  // exclusive scan over all block sums (chunk per thread), in place
+  const int nb = gridDim.x;
+  const int E2 = (nb + TB - 1) / TB;
+  const int q0 = min(nb, tid * E2), q1 = min(nb, q0 + E2);
+  uint64_t c2 = 0;
+  for (int q = q0; q < q1; ++q) c2 += ((volatile unsigned long long*)A.bsum)[q];
+  uint64_t Qt;
+  uint64_t pre = block_excl_scan_u64(c2, s_red64, &Qt);
+  __syncthreads();
+  for (int q = q0; q < q1; ++q) {
+    uint64_t v = ((volatile unsigned long long*)A.bsum)[q];
+    A.bsum[q] = pre;
+    pre += v;
+  }
+  if (tid == 0) {
+    A.fs->Qt = Qt;
+    A.fs->ticket_b = 0u;
+    if (Qt == 0ull && !fb) { A.fs->fb = 1; A.fs->status |= MKF_ST_FALLBACK; }
+  }
+}
+
+__device__ __forceinline__ int count_targets_le(uint64_t X, int N, uint32_t U, uint64_t Qt) {
+  // number of targets i in [0,N) with (i 2^32 + U) Qt <= N X 2^32
+  const unsigned __int128 lim = ((unsigned __int128)(uint64_t)N * (unsigned __int128)X) << 32;
+  double est = (double)N * ((double)X / (double)Qt);
+  long long i = (long long)est;
+  if (i < 0) i = 0;
+  if (i > N) i = N;
+  // smallest i with R_i > lim
+  for (int it = 0; it < 64 && i < N && resample_rhs((int)i, U, Qt) <= lim; ++it) ++i;
+  for (int it = 0; it < 64 && i > 0 && resample_rhs((int)(i - 1), U, Qt) > lim; ++it) --i;
+  // guarantee correctness if the estimate was far off: binary search fallback
+  bool ok = (i == N || resample_rhs((int)i, U, Qt) > lim) && (i == 0 || resample_rhs((int)(i - 1), U, Qt) <= lim);
+  if (!ok) {
+    long long lo = 0, hi = N;
+    while (lo < hi) {
+      long long mid = (lo + hi) >> 1;
+      if (resample_rhs((int)mid, U, Qt) <= lim) lo = mid + 1; else hi = mid;
+    }
+    i = lo;
+  }
+  return (int)i;
+}
+
+__global__ void __launch_bounds__(256) bpf_stream_c(StreamArgs A, int tile_c) {
+  extern __shared__ __align__(16) unsigned char smem_c[];
+  uint64_t* sQ = reinterpret_cast<uint64_t*>(smem_c);
+  __shared__ uint64_t s_red64[34];
+  __shared__ int s_lo, s_hi;
+  const int tid = threadIdx.x, TB = blockDim.x;
+  const float M = A.fs->M;
+  const int fb = A.fs->fb;
+  const uint64_t Qt = A.fs->Qt;
+  const int base = blockIdx.x * tile_c, end = min(A.N, base + tile_c), n = end - base;
+  if (fb) {
+    for (int i = base + tid; i < end; i += TB) A.anc_out[i] = resample_fallback_index(A.U, i, A.N);
+    return;
+  }
+  const int E = (tile_c + TB - 1) / TB;
+  const int j0 = min(end, base + tid * E), j1 = min(end, j0 + E);
+  uint64_t cs = 0;
+  for (int j = j0; j < j1; ++j) cs += quantize_f32(stream_weight(A.logw[j], M, fb), 1);
+  uint64_t tot;
+  uint64_t pre = block_excl_scan_u64(cs, s_red64, &tot) + A.bsum[blockIdx.x];
+  for (int j = j0; j < j1; ++j) {
+    pre += quantize_f32(stream_weight(A.logw[j], M, fb), 1);
+    sQ[j - base] = pre;
+  }
+  if (tid == 0) {
+    uint64_t Xprev = A.bsum[blockIdx.x];
+    s_lo = (blockIdx.x == 0) ? 0 : count_targets_le(Xprev, A.N, A.U, Qt);
+    s_hi = (blockIdx.x == gridDim.x - 1) ? A.N : count_targets_le(Xprev + tot, A.N, A.U, Qt);
+  }
+  __syncthreads();
+  for (int i = s_lo + tid; i < s_hi; i += TB)
+    A.anc_out[i] = base + resample_search(sQ, n, A.N, resample_rhs(i, A.U, Qt));
+}
+
+// ------------------------------------------------------------------ handles
+struct BpfHandle {
+  DevModels m;
+  mkf_bpf_track tr;
+  int N, d;
+  float *xa, *xb, *logw, *w, *partial;
+  int* anc;
+  unsigned long long* bsum;
+  FrameScalars* fs;
+  int nb_a, nb_b, tile_a, tile_b;
+  bool ready;
+  bool debug;
+};
+
+constexpr int kStreamTB = 256;
+constexpr int kTileA = 2048;
+constexpr int kTileB = 4096;
+
+}  // namespace mkf
+
+using namespace mkf;
+
+struct mkf_bpf { BpfHandle h; };
+struct mkf_bpf_batch {
+  DevModels m;
+  int n_tracks, Nmax, d, K, J;
+  long long G;
+  int tb, ctas_per_sm;
+  int4* meta;
+  long long* fbase;
+  unsigned long long* seed;
+  float4* obs;
+  int* order;
+  int* counter;
+  float* scratch;
+  size_t scratch_slots;
+  int dbg_track;
+  float* dbg_w;
+  int* dbg_anc;
+  // host-run staging
+  int* h_det_off_dev;
+  float* h_det_dev;
+  size_t det_cap;
+  float *d_est, *d_ll, *d_ess;
+  int* d_status;
+};
+
+static PView make_view(const DevModels& m, int mi) {
+  PView p;
+  const int d = m.d, K = m.K, J = m.J, DD = d * (d + 1) / 2;
+  p.a = m.a + (size_t)mi * K * d; p.mb = m.mb + (size_t)mi * K * d; p.mu = m.mu + (size_t)mi * K * d;
+  p.Lq = m.Lq + (size_t)mi * K * DD; p.Ld = m.Ld + (size_t)mi * K * d;
+  p.S0c = m.S0c + (size_t)mi * K * DD; p.cumpi = m.cumpi + (size_t)mi * K;
+  p.Bm = m.Bm + (size_t)mi * J * 3 * d; p.mm = m.mm + (size_t)mi * J * 3;
+  p.K = K; p.J = J; p.fx = m.fx; p.fy = m.fy; p.cx = m.cx; p.cy = m.cy;
+  return p;
+}
+
+extern "C" int mkf_bpf_create(const mkf_bpf_models* models, const mkf_bpf_track* track, mkf_bpf_t* out) {
+  MKF_ARG(models && track && out, "mkf_bpf_create: null argument");
+  MKF_ARG(track->n_particles >= 1 && track->n_particles <= (1 << 22), "mkf_bpf_create: n_particles out of range");
+  MKF_ARG(track->model_index >= 0 && track->model_index < models->n_models, "mkf_bpf_create: bad model_index");
+  MKF_ARG(track->kappa > 0.0f && track->p_detect > 0.0f && track->p_detect < 1.0f && track->sigma_px > 0.0f,
+          "mkf_bpf_create: kappa, p_detect, sigma_px out of range");
+  mkf_bpf* H = new (std::nothrow) mkf_bpf();
+  if (!H) return MKF_ERR_NOMEM;
+  BpfHandle& h = H->h;
+  memset(&h, 0, sizeof(h));
+  int st = build_models(models, h.m);
+  if (st) { free_models(h.m); delete H; return st; }
+  h.tr = *track;
+  h.N = track->n_particles;
+  h.d = models->d;
+  h.tile_a = kTileA; h.tile_b = kTileB;
+  h.nb_a = (h.N + kTileA - 1) / kTileA;
+  h.nb_b = (h.N + kTileB - 1) / kTileB;
+  const size_t N = h.N, d = h.d;
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = cudaMalloc(&h.xa, N * d * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&h.xb, N * d * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&h.logw, N * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&h.w, N * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&h.anc, N * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&h.partial, (size_t)h.nb_a * (d + 3) * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&h.bsum, (size_t)h.nb_b * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&h.fs, sizeof(FrameScalars));
+  if (e == cudaSuccess) e = cudaMemset(h.fs, 0, sizeof(FrameScalars));
+  if (e != cudaSuccess) {
+    mkf_bpf_destroy(H);
+    return cuda_fail(e, "mkf_bpf_create: allocation", __FILE__, __LINE__);
+  }
+  *out = H;
+  return MKF_OK;
+}
+
+template <int D, bool DIAG>
+static void launch_stream_a(const StreamArgs& a, int nb, cudaStream_t s) {
+  bpf_stream_a<D, DIAG><<<nb, kStreamTB, 0, s>>>(a);
+}
+
+static void stream_a(int d, bool diag, const StreamArgs& a, int nb, cudaStream_t s) {
+  if (d == 12) { if (diag) launch_stream_a<12, true>(a, nb, s); else launch_stream_a<12, false>(a, nb, s); }
+  else { if (diag) launch_stream_a<24, true>(a, nb, s); else launch_stream_a<24, false>(a, nb, s); }
+}
+
+static StreamArgs stream_args(BpfHandle& h) {
+  StreamArgs a;
+  memset(&a, 0, sizeof(a));
+  a.N = h.N; a.tile_a = h.tile_a; a.tile_b = h.tile_b;
+  a.seed = h.tr.seed; a.track = h.tr.track_id;
+  a.kappa = h.tr.kappa; a.pd = h.tr.p_detect; a.sigma = h.tr.sigma_px;
+  a.pv = make_view(h.m, h.tr.model_index);
+  a.partial = h.partial; a.bsum = h.bsum; a.fs = h.fs;
+  return a;
+}
+
+extern "C" int mkf_bpf_reset(mkf_bpf_t H, mkf_stream_t stream) {
+  MKF_ARG(H, "mkf_bpf_reset: null handle");
+  BpfHandle& h = H->h;
+  cudaStream_t s = (cudaStream_t)stream;
+  StreamArgs a = stream_args(h);
+  a.prior = true;
+  a.xb = h.xa;
+  stream_a(h.d, h.m.diag, a, h.nb_a, s);
+  MKF_CHECK_LAUNCH("mkf_bpf_reset: prior kernel");
+  // identity ancestry: sequence 0..N-1
+  std::vector<int> iota(h.N);
+  for (int i = 0; i < h.N; ++i) iota[i] = i;
+  MKF_CUDA(cudaMemcpyAsync(h.anc, iota.data(), sizeof(int) * h.N, cudaMemcpyHostToDevice, s));
+  MKF_CUDA(cudaMemsetAsync(h.fs, 0, sizeof(FrameScalars), s));
+  MKF_CUDA(cudaStreamSynchronize(s));
+  h.ready = true;
+  return MKF_OK;
+}
+
+extern "C" int mkf_bpf_update(mkf_bpf_t H, uint32_t frame, const int* d_det_off, const float* d_det,
+                              float* d_est, float* d_loglik, float* d_ess, mkf_stream_t stream) {
+  MKF_ARG(H && d_det_off, "mkf_bpf_update: null argument");
+  BpfHandle& h = H->h;
+  if (!h.ready) { set_error("mkf_bpf_update: call mkf_bpf_reset first"); return MKF_ERR_STATE; }
+  cudaStream_t s = (cudaStream_t)stream;
+  StreamArgs a = stream_args(h);
+  a.frame = frame;
+  a.U = resample_uniform(h.tr.seed, h.tr.track_id, frame);
+  a.det_off = d_det_off;
+  a.det = reinterpret_cast<const float2*>(d_det);
+  a.anc = h.anc; a.xa = h.xa; a.xb = h.xb; a.logw = h.logw;
+  a.est = d_est; a.out_loglik = d_loglik; a.out_ess = d_ess;
+  a.dbg_w = h.debug ? h.w : nullptr;
+  a.anc_out = h.anc;
+  stream_a(h.d, h.m.diag, a, h.nb_a, s);
+  MKF_CHECK_LAUNCH("mkf_bpf_update: propagate/score kernel");
+  bpf_stream_b<<<h.nb_b, kStreamTB, 0, s>>>(a);
+  MKF_CHECK_LAUNCH("mkf_bpf_update: block-sum kernel");
+  bpf_stream_c<<<h.nb_b, kStreamTB, (size_t)h.tile_b * sizeof(uint64_t), s>>>(a, h.tile_b);
+  MKF_CHECK_LAUNCH("mkf_bpf_update: search kernel");
+  std::swap(h.xa, h.xb);
+  return MKF_OK;
+}
+
+extern "C" int mkf_bpf_read_debug(mkf_bpf_t H, float* d_x, float* d_logw, float* d_w, int* d_anc,
+                                  mkf_stream_t stream) {
+  MKF_ARG(H, "mkf_bpf_read_debug: null handle");
+  BpfHandle& h = H->h;
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t N = h.N;
+  if (d_x) MKF_CUDA(cudaMemcpyAsync(d_x, h.xa, N * h.d * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  if (d_logw) MKF_CUDA(cudaMemcpyAsync(d_logw, h.logw, N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  if (d_w) MKF_CUDA(cudaMemcpyAsync(d_w, h.w, N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  if (d_anc) MKF_CUDA(cudaMemcpyAsync(d_anc, h.anc, N * sizeof(int), cudaMemcpyDeviceToDevice, s));
+  return MKF_OK;
+}
+
+extern "C" int mkf_bpf_set_debug(mkf_bpf_t H, int enable) {
+  MKF_ARG(H, "mkf_bpf_set_debug: null handle");
+  H->h.debug = enable != 0;
+  return MKF_OK;
+}
+
+extern "C" int mkf_bpf_status(mkf_bpf_t H, int* status) {
+  MKF_ARG(H && status, "mkf_bpf_status: null argument");
+  FrameScalars fs;
+  MKF_CUDA(cudaMemcpy(&fs, H->h.fs, sizeof(fs), cudaMemcpyDeviceToHost));
+  *status = fs.status;
+  return MKF_OK;
+}
+
+extern "C" int mkf_bpf_destroy(mkf_bpf_t H) {
+  if (!H) return MKF_OK;
+  BpfHandle& h = H->h;
+  void* ps[] = {h.xa, h.xb, h.logw, h.w, h.anc, h.partial, h.bsum, h.fs};
+  for (void* p : ps) if (p) cudaFree(p);
+  free_models(h.m);
+  delete H;
+  return MKF_OK;
+}
+
+// ------------------------------------------------------------------ batched C ABI
+extern "C" int mkf_bpf_batch_create(const mkf_bpf_models* models, int n_tracks, const mkf_bpf_track* tracks,
+                                    int64_t n_frames_total, mkf_bpf_batch_t* out) {
+  MKF_ARG(models && tracks && out && n_tracks > 0, "mkf_bpf_batch_create: bad argument");
+  int Nmax = 0;
+  long long sumT = 0;
+  for (int b = 0; b < n_tracks; ++b) {
+    const mkf_bpf_track& t = tracks[b];
+    MKF_ARG(t.n_particles >= 1 && t.n_particles <= 8192, "mkf_bpf_batch_create: n_particles must be in [1, 8192]");
+    MKF_ARG(t.n_frames >= 0, "mkf_bpf_batch_create: n_frames < 0");
+    MKF_ARG(t.model_index >= 0 && t.model_index < models->n_models, "mkf_bpf_batch_create: bad model_index");
+    MKF_ARG(t.frame_base >= 0 && t.frame_base + t.n_frames <= n_frames_total, "mkf_bpf_batch_create: frame range");
+    MKF_ARG(t.kappa > 0.0f && t.p_detect > 0.0f && t.p_detect < 1.0f && t.sigma_px > 0.0f,
+            "mkf_bpf_batch_create: kappa, p_detect, sigma_px out of range");
+    Nmax = std::max(Nmax, t.n_particles);
+    sumT += t.n_frames;
+  }
+  mkf_bpf_batch* B = new (std::nothrow) mkf_bpf_batch();
+  if (!B) return MKF_ERR_NOMEM;
+  memset(B, 0, sizeof(*B));
+  int st = build_models(models, B->m);
+  if (st) { free_models(B->m); delete B; return st; }
+  B->n_tracks = n_tracks; B->Nmax = (Nmax + 31) & ~31; B->d = models->d; B->K = models->K; B->J = models->J;
+  B->G = n_frames_total;
+  B->tb = 256; B->ctas_per_sm = 0;
+  B->dbg_track = -1;
+  std::vector<int4> meta(n_tracks);
+  std::vector<long long> fb(n_tracks);
+  std::vector<unsigned long long> sd(n_tracks);
+  std::vector<float4> ob(n_tracks);
+  std::vector<int> order(n_tracks);
+  for (int b = 0; b < n_tracks; ++b) {
+    const mkf_bpf_track& t = tracks[b];
+    meta[b] = make_int4(t.n_particles, t.n_frames, t.model_index, (int)t.track_id);
+    fb[b] = t.frame_base; sd[b] = t.seed;
+    ob[b] = make_float4(t.kappa, t.p_detect, t.sigma_px, 0.0f);
+    order[b] = b;
+  }
+  // longest-processing-time-first schedule over the persistent CTAs
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return (long long)tracks[x].n_particles * tracks[x].n_frames > (long long)tracks[y].n_particles * tracks[y].n_frames;
+  });
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = cudaMalloc(&B->meta, n_tracks * sizeof(int4));
+  if (e == cudaSuccess) e = cudaMalloc(&B->fbase, n_tracks * sizeof(long long));
+  if (e == cudaSuccess) e = cudaMalloc(&B->seed, n_tracks * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc(&B->obs, n_tracks * sizeof(float4));
+  if (e == cudaSuccess) e = cudaMalloc(&B->order, n_tracks * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&B->counter, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpy(B->meta, meta.data(), n_tracks * sizeof(int4), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(B->fbase, fb.data(), n_tracks * sizeof(long long), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(B->seed, sd.data(), n_tracks * sizeof(unsigned long long), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(B->obs, ob.data(), n_tracks * sizeof(float4), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(B->order, order.data(), n_tracks * sizeof(int), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    mkf_bpf_batch_destroy(B);
+    return cuda_fail(e, "mkf_bpf_batch_create: allocation", __FILE__, __LINE__);
+  }
+  (void)sumT;
+  *out = B;
+  return MKF_OK;
+}
+
+extern "C" int mkf_bpf_batch_set_tuning(mkf_bpf_batch_t B, int block_threads, int ctas_per_sm) {
+  MKF_ARG(B, "mkf_bpf_batch_set_tuning: null handle");
+  MKF_ARG(block_threads >= 64 && block_threads <= 512 && block_threads % 32 == 0,
+          "mkf_bpf_batch_set_tuning: block_threads must be a multiple of 32 in [64, 512]");
+  MKF_ARG(ctas_per_sm >= 0 && ctas_per_sm <= 32, "mkf_bpf_batch_set_tuning: ctas_per_sm out of range");
+  B->tb = block_threads;
+  B->ctas_per_sm = ctas_per_sm;
+  return MKF_OK;
+}
+
+extern "C" int mkf_bpf_batch_set_debug(mkf_bpf_batch_t B, int track, float* d_w, int* d_anc) {
+  MKF_ARG(B, "mkf_bpf_batch_set_debug: null handle");
+  B->dbg_track = track; B->dbg_w = d_w; B->dbg_anc = d_anc;
+  return MKF_OK;
+}
+
+template <int D, bool DIAG>
+static int launch_batched(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
+  auto kern = bpf_batched_kernel<D, DIAG>;
+  size_t smem = batched_smem_bytes(D, B->Nmax, B->K, B->J, DIAG);
+  MKF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 0;
+  MKF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, B->tb, smem));
+  if (occ < 1) { set_error("mkf_bpf_batch_run: block shape does not fit on an SM"); return MKF_ERR_ARG; }
+  int per_sm = B->ctas_per_sm > 0 ? std::min(B->ctas_per_sm, occ) : occ;
+  long long grid = (long long)num_sms() * per_sm;
+  grid = std::min<long long>(grid, B->n_tracks);
+  size_t need = (size_t)grid * 2 * D * B->Nmax;
+  if (need > B->scratch_slots) {
+    if (B->scratch) cudaFree(B->scratch);
+    B->scratch = nullptr;
+    B->scratch_slots = 0;
+    MKF_CUDA(cudaMalloc(&B->scratch, need * sizeof(float)));
+    B->scratch_slots = need;
+  }
+  a.scratch = B->scratch;
+  MKF_CUDA(cudaMemsetAsync(B->counter, 0, sizeof(int), s));
+  kern<<<(int)grid, B->tb, smem, s>>>(a);
+  MKF_CHECK_LAUNCH("mkf_bpf_batch_run: batched kernel");
+  return MKF_OK;
+}
+
+extern "C" int mkf_bpf_batch_run(mkf_bpf_batch_t B, const int* d_det_off, const float* d_det,
+                                 float* d_est, float* d_loglik, float* d_ess, int* d_status,
+                                 mkf_stream_t stream) {
+  MKF_ARG(B && d_det_off && d_est && d_loglik && d_ess && d_status, "mkf_bpf_batch_run: null argument");
+  BatchArgs a;
+  memset(&a, 0, sizeof(a));
+  a.n_tracks = B->n_tracks; a.K = B->K; a.J = B->J; a.Nmax = B->Nmax;
+  a.meta = B->meta; a.fbase = B->fbase; a.seed = B->seed; a.obs = B->obs;
+  a.order = B->order; a.counter = B->counter; a.m = B->m;
+  a.det_off = d_det_off; a.det = reinterpret_cast<const float2*>(d_det);
+  a.est = d_est; a.loglik = d_loglik; a.ess = d_ess; a.status = d_status;
+  a.dbg_track = B->dbg_track; a.dbg_w = B->dbg_w; a.dbg_anc = B->dbg_anc;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (B->d == 12) return B->m.diag ? launch_batched<12, true>(B, a, s) : launch_batched<12, false>(B, a, s);
+  return B->m.diag ? launch_batched<24, true>(B, a, s) : launch_batched<24, false>(B, a, s);
+}
+
+extern "C" int mkf_bpf_batch_run_host(mkf_bpf_batch_t B, const int* det_off, const float* det, int64_t n_det,
+                                      float* est, float* loglik, float* ess, int* status,
+                                      mkf_stream_t stream) {
+  MKF_ARG(B && det_off && det && est && loglik && ess && status && n_det >= 0, "mkf_bpf_batch_run_host: null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  const size_t G = (size_t)B->G, J = (size_t)B->J, d = (size_t)B->d;
+  if (!B->h_det_off_dev) {
+    MKF_CUDA(cudaMalloc(&B->h_det_off_dev, (G * J + 1) * sizeof(int)));
+    MKF_CUDA(cudaMalloc(&B->d_est, G * d * sizeof(float)));
+    MKF_CUDA(cudaMalloc(&B->d_ll, G * sizeof(float)));
+    MKF_CUDA(cudaMalloc(&B->d_ess, G * sizeof(float)));
+    MKF_CUDA(cudaMalloc(&B->d_status, B->n_tracks * sizeof(int)));
+  }
+  if ((size_t)n_det > B->det_cap || !B->h_det_dev) {
+    if (B->h_det_dev) cudaFree(B->h_det_dev);
+    B->h_det_dev = nullptr;
+    MKF_CUDA(cudaMalloc(&B->h_det_dev, std::max<size_t>(1, (size_t)n_det) * 2 * sizeof(float)));
+    B->det_cap = (size_t)n_det;
+  }
+  MKF_CUDA(cudaMemcpyAsync(B->h_det_off_dev, det_off, (G * J + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+  MKF_CUDA(cudaMemcpyAsync(B->h_det_dev, det, (size_t)n_det * 2 * sizeof(float), cudaMemcpyHostToDevice, s));
+  int st = mkf_bpf_batch_run(B, B->h_det_off_dev, B->h_det_dev, B->d_est, B->d_ll, B->d_ess, B->d_status, stream);
+  if (st) return st;
+  MKF_CUDA(cudaMemcpyAsync(est, B->d_est, G * d * sizeof(float), cudaMemcpyDeviceToHost, s));
+  MKF_CUDA(cudaMemcpyAsync(loglik, B->d_ll, G * sizeof(float), cudaMemcpyDeviceToHost, s));
+  MKF_CUDA(cudaMemcpyAsync(ess, B->d_ess, G * sizeof(float), cudaMemcpyDeviceToHost, s));
+  MKF_CUDA(cudaMemcpyAsync(status, B->d_status, B->n_tracks * sizeof(int), cudaMemcpyDeviceToHost, s));
+  MKF_CUDA(cudaStreamSynchronize(s));
+  return MKF_OK;
+}
+
+extern "C" int mkf_bpf_batch_destroy(mkf_bpf_batch_t B) {
+  if (!B) return MKF_OK;
+  void* ps[] = {B->meta, B->fbase, B->seed, B->obs, B->order, B->counter, B->scratch,
+                B->h_det_off_dev, B->h_det_dev, B->d_est, B->d_ll, B->d_ess, B->d_status};
+  for (void* p : ps) if (p) cudaFree(p);
+  free_models(B->m);
+  delete B;
+  return MKF_OK;
+}

@@ -1,0 +1,190 @@
+// mkf_common.cuh -- shared device/host pieces of the GB300 filtering hot path.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include "../../include/mkf_gb300.h"
+
+#define MKF_HD __host__ __device__ __forceinline__
+
+namespace mkf {
+
+// ---------------------------------------------------------------- errors
+void set_error(const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+#define MKF_CUDA(call)                                                   \
+  do {                                                                   \
+    cudaError_t _e = (call);                                             \
+    if (_e != cudaSuccess) return ::mkf::cuda_fail(_e, #call, __FILE__, __LINE__); \
+  } while (0)
+#define MKF_CHECK_LAUNCH(what)                                           \
+  do {                                                                   \
+    cudaError_t _e = cudaGetLastError();                                 \
+    if (_e != cudaSuccess) return ::mkf::cuda_fail(_e, what, __FILE__, __LINE__); \
+  } while (0)
+#define MKF_ARG(cond, msg)                                               \
+  do {                                                                   \
+    if (!(cond)) { ::mkf::set_error(msg); return MKF_ERR_ARG; }          \
+  } while (0)
+
+int num_sms();
+
+// ---------------------------------------------------------------- Philox4x32-10
+// Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3",
+// SC'11.  Replaces cv::RNG / randn / rand() (pf2DRao.cpp:96,179; pf2D.cpp:228,255).
+struct u32x4 { uint32_t x, y, z, w; };
+
+MKF_HD u32x4 philox4x32_10(u32x4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+#ifdef __CUDA_ARCH__
+    uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+    uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+#else
+    uint64_t p0 = (uint64_t)0xD2511F53u * c.x, p1 = (uint64_t)0xCD9E8D57u * c.z;
+    uint32_t lo0 = (uint32_t)p0, hi0 = (uint32_t)(p0 >> 32);
+    uint32_t lo1 = (uint32_t)p1, hi1 = (uint32_t)(p1 >> 32);
+#endif
+    u32x4 n;
+    n.x = hi1 ^ c.y ^ k0;
+    n.y = lo1;
+    n.z = hi0 ^ c.w ^ k1;
+    n.w = lo0;
+    c = n;
+  }
+  return c;
+}
+
+MKF_HD u32x4 draw_block(uint64_t seed, uint32_t track, uint32_t frame, uint32_t item,
+                        uint32_t stream) {
+  u32x4 c{frame, item, stream, 0u};
+  return philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32) ^ track);
+}
+
+constexpr uint32_t kFramePrior = 0xFFFFFFFFu;
+constexpr uint32_t kItemFrame = 0xFFFFFFFFu;
+constexpr uint32_t kStreamResample = 0x100u;
+
+MKF_HD uint32_t resample_uniform(uint64_t seed, uint32_t track, uint32_t frame) {
+  return draw_block(seed, track, frame, kItemFrame, kStreamResample).x;
+}
+
+#ifdef __CUDACC__
+// Box-Muller pair from two words (top 24 bits): u1 in (0,1], u2 in [0,1).
+// MUFU intrinsics: the CPU oracle consumes these values dumped by
+// mkf_draw_particles, so libm-vs-device rounding never enters parity.
+__device__ __forceinline__ void box_muller(uint32_t w0, uint32_t w1, float& z0, float& z1) {
+  float u1 = (float)((w0 >> 8) + 1u) * (1.0f / 16777216.0f);
+  float u2 = (float)(w1 >> 8) * (1.0f / 16777216.0f);
+  float r = sqrtf(-2.0f * __logf(u1));
+  float s, c;
+  __sincosf(3.14159265358979f * (2.0f * u2 - 1.0f), &s, &c);
+  z0 = r * c;
+  z1 = r * s;
+}
+
+// All draws of one particle-frame.
+template <int D>
+__device__ __forceinline__ float particle_draws(uint64_t seed, uint32_t track, uint32_t frame,
+                                                uint32_t item, float* eps) {
+  uint32_t lowb = 0;
+#pragma unroll
+  for (int b = 0; b < (D + 3) / 4; ++b) {
+    u32x4 w = draw_block(seed, track, frame, item, (uint32_t)b);
+    if (b == 0) lowb = (w.x & 0xFFu) | ((w.y & 0xFFu) << 8) | ((w.z & 0xFFu) << 16);
+    if (4 * b + 1 < D) box_muller(w.x, w.y, eps[4 * b], eps[4 * b + 1]);
+    if (4 * b + 3 < D) box_muller(w.z, w.w, eps[4 * b + 2], eps[4 * b + 3]);
+  }
+  return (float)lowb * (1.0f / 16777216.0f);
+}
+
+// ---------------------------------------------------------------- block helpers
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ uint64_t warp_incl_scan_u64(uint64_t v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint64_t t = __shfl_up_sync(0xffffffffu, v, o);
+    if (lane >= o) v += t;
+  }
+  return v;
+}
+
+// block-wide max; red must hold >= 32 floats; all threads get the result
+__device__ __forceinline__ float block_max(float v, float* red) {
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  v = warp_max(v);
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  float r = lane < nw ? red[lane] : -INFINITY;
+  r = warp_max(r);
+  return r;
+}
+
+// exclusive block scan of one uint64 per thread; red holds >= 33 uint64
+__device__ __forceinline__ uint64_t block_excl_scan_u64(uint64_t v, uint64_t* red, uint64_t* total) {
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  uint64_t inc = warp_incl_scan_u64(v, lane);
+  __syncthreads();
+  if (lane == 31) red[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    uint64_t t = lane < nw ? red[lane] : 0;
+    uint64_t ti = warp_incl_scan_u64(t, lane);
+    if (lane < nw) red[lane] = ti - t;
+    if (lane == 31) red[32] = ti;
+  }
+  __syncthreads();
+  uint64_t r = red[w] + inc - v;
+  if (total) *total = red[32];
+  return r;
+}
+
+// ---------------------------------------------------------------- exact resampler
+// Weights -> 64-bit integers with 40 bits below the max (exact power-of-two
+// scaling then truncation); systematic resampling in exact integer arithmetic.
+constexpr int kQBits = 40;
+
+__device__ __forceinline__ uint64_t quantize_f32(float w, int e) {
+  return (w > 0.0f) ? (uint64_t)__float2ull_rz(ldexpf(w, kQBits - e)) : 0ull;
+}
+__device__ __forceinline__ uint64_t quantize_f64(double w, int e) {
+  return (w > 0.0) ? (uint64_t)__double2ull_rz(ldexp(w, kQBits - e)) : 0ull;
+}
+
+// target of particle i: (i 2^32 + U) * Qt  (128-bit)
+__device__ __forceinline__ unsigned __int128 resample_rhs(int i, uint32_t U, uint64_t Qt) {
+  return (unsigned __int128)((((uint64_t)(uint32_t)i) << 32) | (uint64_t)U) * (unsigned __int128)Qt;
+}
+// first j in [0, n) with N Q[j] 2^32 >= rhs; Q nondecreasing; returns n-1 if none
+__device__ __forceinline__ int resample_search(const uint64_t* Q, int n, int N, unsigned __int128 rhs) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    unsigned __int128 lhs = ((unsigned __int128)(uint64_t)N * (unsigned __int128)Q[mid]) << 32;
+    if (lhs < rhs) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+__device__ __forceinline__ int resample_fallback_index(uint32_t U, int i, int L) {
+  u32x4 o = philox4x32_10(u32x4{(uint32_t)i, 0u, 0u, 0u}, U, 0x5EEDu);
+  return (int)(((uint64_t)o.x * (uint64_t)L) >> 32);
+}
+#endif  // __CUDACC__
+
+}  // namespace mkf

@@ -1,0 +1,186 @@
+"""Host-side mirror of the reference's filter classes over the C ABI.
+
+``BootstrapParticleFilter`` follows pf2D's ``ParticleFilter`` (pf2D.h:25-51:
+construct, predict+update per frame, getEstimator) with the mixture motion
+model of ``my_gmm`` (my_gmm.cpp:45-75); ``BatchedBootstrapPF`` runs thousands
+of such filters over uneven tracks in one persistent launch.  Device buffers
+are torch CUDA tensors (plumbing only); all arithmetic runs in
+libmkf_gb300.so.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+class Models:
+    """Stacked model arrays (mkf_bpf_models) from a synthetic/user model dict with
+    keys a, mu, Lq (packed), S0c (packed), pi, Bm, mm, cam, d, K, J."""
+
+    def __init__(self, model, index=None):
+        sel = (lambda a: a) if index is None else (lambda a: a[index:index + 1])
+        self.arrays = {k: _f32(sel(model[k])) for k in ("a", "mu", "Lq", "S0c", "pi", "Bm", "mm")}
+        n = self.arrays["a"].shape[0]
+        fx, fy, cx, cy = model["cam"]
+        ptr = {k: v.ctypes.data_as(C.c_void_p) for k, v in self.arrays.items()}
+        self.s = N.BpfModels(n, model["d"], model["K"], model["J"], ptr["a"], ptr["mu"], ptr["Lq"],
+                             ptr["S0c"], ptr["pi"], ptr["Bm"], ptr["mm"], fx, fy, cx, cy)
+        self.d = model["d"]
+        self.J = model["J"]
+
+
+def _track_struct(t, model_index=None, frame_base=None):
+    return N.BpfTrack(int(t["n_particles"]), int(t["n_frames"]),
+                      int(t["frame_base"] if frame_base is None else frame_base),
+                      int(t["seed"]), int(t["track_id"]),
+                      int(t["param_index"] if model_index is None else model_index),
+                      float(t["kappa"]), float(t["pd"]), float(t["sigma"]))
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream(torch, stream=None):
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+class BootstrapParticleFilter:
+    """One track: ParticleFilter(N) with reset / update(frame, detections) / getEstimator."""
+
+    def __init__(self, model, track, model_index=None):
+        import torch
+        self.torch = torch
+        mi = track["param_index"] if model_index is None else model_index
+        self.models = Models(model, index=mi)
+        self.track = track
+        self.d = model["d"]
+        self.N = int(track["n_particles"])
+        h = C.c_void_p()
+        N.check(N.lib().mkf_bpf_create(C.byref(self.models.s), C.byref(_track_struct(track, 0)),
+                                       C.byref(h)), "mkf_bpf_create")
+        self.h = h
+        dev = torch.device("cuda")
+        self.est = torch.zeros(self.d, dtype=torch.float32, device=dev)
+        self.loglik = torch.zeros(1, dtype=torch.float32, device=dev)
+        self.ess = torch.zeros(1, dtype=torch.float32, device=dev)
+
+    def set_debug(self, on=True):
+        N.check(N.lib().mkf_bpf_set_debug(self.h, int(on)), "mkf_bpf_set_debug")
+
+    def reset(self, stream=None):
+        N.check(N.lib().mkf_bpf_reset(self.h, _stream(self.torch, stream)), "mkf_bpf_reset")
+
+    def update(self, frame, det_off, det, est=None, loglik=None, ess=None, stream=None):
+        """det_off: int32 CUDA tensor (J+1), det: float32 CUDA tensor (M, 2)."""
+        est = self.est if est is None else est
+        loglik = self.loglik if loglik is None else loglik
+        ess = self.ess if ess is None else ess
+        N.check(N.lib().mkf_bpf_update(self.h, int(frame), _ptr(det_off), _ptr(det), _ptr(est),
+                                       _ptr(loglik), _ptr(ess), _stream(self.torch, stream)),
+                "mkf_bpf_update")
+        return est
+
+    def getEstimator(self):
+        return self.est
+
+    def debug_views(self, stream=None):
+        """(x SoA (d,N), logw (N), w (N), anc (N)) copied from the last update."""
+        torch = self.torch
+        x = torch.empty((self.d, self.N), dtype=torch.float32, device="cuda")
+        lw = torch.empty(self.N, dtype=torch.float32, device="cuda")
+        w = torch.empty(self.N, dtype=torch.float32, device="cuda")
+        anc = torch.empty(self.N, dtype=torch.int32, device="cuda")
+        N.check(N.lib().mkf_bpf_read_debug(self.h, _ptr(x), _ptr(lw), _ptr(w), _ptr(anc),
+                                           _stream(torch, stream)), "mkf_bpf_read_debug")
+        return x, lw, w, anc
+
+    def status(self):
+        s = C.c_int()
+        N.check(N.lib().mkf_bpf_status(self.h, C.byref(s)), "mkf_bpf_status")
+        return s.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                N.lib().mkf_bpf_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+class BatchedBootstrapPF:
+    """All tracks of a synth.BpfBatch (or equivalent) in one persistent launch."""
+
+    def __init__(self, batch, block_threads=256, ctas_per_sm=0):
+        import torch
+        self.torch = torch
+        self.batch = batch
+        m = batch.model
+        self.models = Models(m)
+        self.d, self.J = m["d"], m["J"]
+        tr = (N.BpfTrack * batch.n_tracks)()
+        for b, t in enumerate(batch.tracks):
+            tr[b] = _track_struct(t)
+        self._tracks = tr
+        h = C.c_void_p()
+        N.check(N.lib().mkf_bpf_batch_create(C.byref(self.models.s), batch.n_tracks,
+                                             C.cast(tr, C.c_void_p), batch.n_frames_total,
+                                             C.byref(h)), "mkf_bpf_batch_create")
+        self.h = h
+        self.set_tuning(block_threads, ctas_per_sm)
+
+    def set_tuning(self, block_threads, ctas_per_sm=0):
+        N.check(N.lib().mkf_bpf_batch_set_tuning(self.h, int(block_threads), int(ctas_per_sm)),
+                "mkf_bpf_batch_set_tuning")
+        self.block_threads, self.ctas_per_sm = block_threads, ctas_per_sm
+
+    def device_inputs(self):
+        torch = self.torch
+        return (torch.from_numpy(np.ascontiguousarray(self.batch.det_off, np.int32)).cuda(),
+                torch.from_numpy(np.ascontiguousarray(self.batch.det, np.float32)).cuda())
+
+    def alloc_outputs(self):
+        torch = self.torch
+        G = self.batch.n_frames_total
+        return (torch.empty((G, self.d), dtype=torch.float32, device="cuda"),
+                torch.empty(G, dtype=torch.float32, device="cuda"),
+                torch.empty(G, dtype=torch.float32, device="cuda"),
+                torch.empty(self.batch.n_tracks, dtype=torch.int32, device="cuda"))
+
+    def run(self, det_off, det, outs=None, stream=None):
+        outs = self.alloc_outputs() if outs is None else outs
+        est, ll, ess, st = outs
+        N.check(N.lib().mkf_bpf_batch_run(self.h, _ptr(det_off), _ptr(det), _ptr(est), _ptr(ll),
+                                          _ptr(ess), _ptr(st), _stream(self.torch, stream)),
+                "mkf_bpf_batch_run")
+        return outs
+
+    def run_host(self, det_off, det, outs, stream=None):
+        """Host buffers in and out (pinned numpy views recommended)."""
+        est, ll, ess, st = outs
+        pp = lambda a: a.ctypes.data_as(C.c_void_p)
+        N.check(N.lib().mkf_bpf_batch_run_host(self.h, pp(det_off), pp(det), int(det.shape[0]),
+                                               pp(est), pp(ll), pp(ess), pp(st),
+                                               _stream(self.torch, stream)), "mkf_bpf_batch_run_host")
+        return outs
+
+    def set_debug(self, track, w=None, anc=None):
+        N.check(N.lib().mkf_bpf_batch_set_debug(self.h, int(track), _ptr(w), _ptr(anc)),
+                "mkf_bpf_batch_set_debug")
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                N.lib().mkf_bpf_batch_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass

@@ -1,0 +1,342 @@
+"""CPU oracle for the mkfbodytracker_pdaf filtering hot path.
+
+TEST INFRASTRUCTURE ONLY: an FP64 C restatement of the reference's CPU
+arithmetic (KF_model.cpp, my_gmm.cpp, pf2DRao.cpp, pf2D.cpp, pfPose.cpp
+association), used by the tests as the checker, by ``__graft_entry__.smoke()``
+and by ``bench.py``'s CPU-baseline and reference legs.  The product package
+(``mkfbodytracker_pdaf_gb300``) never imports it.
+
+Parity against the reference's own outputs is UNPINNED: the reference has no
+tests or golden vectors and cannot be built here (ROS and OpenCV are absent).
+Pinned instead: Philox4x32-10 against the published Random123 known-answer
+vectors, the exact resampler against the literal wheel on dyadic weights, and
+the KF/Gaussian pieces against independent closed forms (tests/).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_BUILD = os.path.join(_HERE, "_build")
+_SO = os.path.join(_BUILD, "libmkf_oracle.so")
+_SRC = [os.path.join(_HERE, "mkf_oracle.c")]
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with gcc (no build system).  -ffp-contract=off keeps
+    the bit-exact steps unfused on both x86-64 and aarch64."""
+    os.makedirs(_BUILD, exist_ok=True)
+    newest = max(os.path.getmtime(p) for p in _SRC + [os.path.join(_HERE, "mkf_oracle.h")])
+    if not force and os.path.exists(_SO) and os.path.getmtime(_SO) >= newest:
+        return _SO
+    tmp = _SO + ".tmp%d" % os.getpid()
+    cmd = ["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-std=gnu11",
+           "-o", tmp] + _SRC + ["-lm"]
+    subprocess.check_call(cmd)
+    os.replace(tmp, _SO)
+    return _SO
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(build())
+        _declare(_lib)
+    return _lib
+
+
+P = C.c_void_p
+I = C.c_int
+U32 = C.c_uint32
+U64 = C.c_uint64
+D = C.c_double
+F = C.c_float
+
+
+class Model(C.Structure):
+    """mko_model (RBPF / KF_model set of one arm)."""
+    _fields_ = [("d", I), ("m", I), ("K", I), ("meas_mode", I),
+                ("F", P), ("B", P), ("Q", P), ("H", P), ("BH", P), ("R", P), ("weight", P),
+                ("Bm", P), ("mm", P), ("fx", D), ("fy", D), ("cx", D), ("cy", D)]
+
+
+class BpfParams(C.Structure):
+    _fields_ = [("d", I), ("K", I), ("J", I),
+                ("a", P), ("mb", P), ("mu", P), ("Lq", P), ("S0c", P), ("cumpi", P),
+                ("Bm", P), ("mm", P), ("fx", F), ("fy", F), ("cx", F), ("cy", F),
+                ("kappa", F), ("pd", F), ("sigma", F)]
+
+
+class Track(C.Structure):
+    _fields_ = [("n_particles", I), ("n_frames", I), ("frame_base", C.c_longlong),
+                ("seed", C.c_ulonglong), ("track_id", I), ("param_index", I),
+                ("kappa", F), ("pd", F), ("sigma", F)]
+
+
+def _declare(L):
+    L.mko_philox4x32_10.argtypes = [P, P, P]
+    L.mko_draw_block.argtypes = [U64, U32, U32, U32, U32, P]
+    L.mko_u01_f32.argtypes = [U32]
+    L.mko_u01_f32.restype = F
+    L.mko_particle_draws.argtypes = [U64, U32, U32, U32, I, P, P]
+    L.mko_resample_wheel.argtypes = [P, I, I, D, P, P]
+    L.mko_quantize_f64.argtypes = [P, I, P]
+    L.mko_quantize_f64.restype = I
+    L.mko_quantize_f32.argtypes = [P, I, P]
+    L.mko_quantize_f32.restype = I
+    L.mko_resample_exact.argtypes = [P, I, I, U32, P]
+    L.mko_resample_f64.argtypes = [P, I, I, U32, P]
+    L.mko_resample_f64.restype = I
+    L.mko_resample_f32.argtypes = [P, I, I, U32, P]
+    L.mko_resample_f32.restype = I
+    L.mko_kf_predict.argtypes = [I, P, P, P, P, P]
+    L.mko_kf_update.argtypes = [I, I, P, P, P, P, C.c_uint, P, P]
+    L.mko_kf_update.restype = I
+    L.mko_mvn_logpdf.argtypes = [I, P, P, P, I]
+    L.mko_mvn_logpdf.restype = D
+    L.mko_load_gaussian_ref.argtypes = [I, I, P, P, P, P, D, P, P, P, P, P, P]
+    L.mko_measure.argtypes = [C.POINTER(Model), I, P, P, P]
+    L.mko_rbpf_update.argtypes = [C.POINTER(Model), I, P, P, P, C.c_uint, U32, U32, P, P, P, P, P]
+    L.mko_rbpf_update.restype = I
+    L.mko_rbpf_estimate.argtypes = [I, I, P, P]
+    L.mko_pdaf_weights.argtypes = [I, P, P, P, P, I, D, D, D, P]
+    L.mko_pick_component.argtypes = [P, I, F]
+    L.mko_pick_component.restype = I
+    L.mko_bpf_prior.argtypes = [C.POINTER(BpfParams), P, F, P]
+    L.mko_bpf_propagate.argtypes = [C.POINTER(BpfParams), P, F, P]
+    L.mko_bpf_loglik.argtypes = [C.POINTER(BpfParams), P, P, P]
+    L.mko_bpf_loglik.restype = D
+    L.mko_bpf_run_tracks.argtypes = [I, P, I, I, I, P, P, P, P, P, P, P, P,
+                                     F, F, F, F, P, P, P, P, P, I]
+    L.mko_num_threads.restype = I
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+# ---------------------------------------------------------------- draws
+def philox4x32_10(ctr, key):
+    c = _c(ctr, np.uint32)
+    k = _c(key, np.uint32)
+    o = np.zeros(4, np.uint32)
+    lib().mko_philox4x32_10(_p(c), _p(k), _p(o))
+    return o
+
+
+def draw_block(seed, track, frame, item, stream):
+    o = np.zeros(4, np.uint32)
+    lib().mko_draw_block(seed, track, frame, item, stream, _p(o))
+    return o
+
+
+def particle_draws(seed, track, frame, item, d):
+    eps = np.zeros(d, np.float64)
+    uc = np.zeros(1, np.float32)
+    lib().mko_particle_draws(seed, track, frame, item, d, _p(eps), _p(uc))
+    return eps, float(uc[0])
+
+
+# ---------------------------------------------------------------- resampling
+def resample_wheel(w, N, u, fallback=None):
+    w = _c(w, np.float64)
+    idx = np.zeros(N, np.int32)
+    fb = _c(fallback, np.int32) if fallback is not None else None
+    lib().mko_resample_wheel(_p(w), len(w), N, float(u), _p(fb), _p(idx))
+    return idx
+
+
+def quantize(w):
+    w = np.ascontiguousarray(w)
+    q = np.zeros(len(w), np.uint64)
+    fn = lib().mko_quantize_f32 if w.dtype == np.float32 else lib().mko_quantize_f64
+    if w.dtype != np.float32:
+        w = _c(w, np.float64)
+    ok = fn(_p(w), len(w), _p(q))
+    return q, bool(ok)
+
+
+def resample_exact(q, N, U):
+    q = _c(q, np.uint64)
+    idx = np.zeros(N, np.int32)
+    lib().mko_resample_exact(_p(q), len(q), N, U, _p(idx))
+    return idx
+
+
+def resample(w, N, U):
+    """Quantised exact systematic resampler (+ fallback); dtype decides f32/f64."""
+    w = np.ascontiguousarray(w)
+    idx = np.zeros(N, np.int32)
+    if w.dtype == np.float32:
+        fb = lib().mko_resample_f32(_p(w), len(w), N, U, _p(idx))
+    else:
+        w = _c(w, np.float64)
+        fb = lib().mko_resample_f64(_p(w), len(w), N, U, _p(idx))
+    return idx, bool(fb)
+
+
+# ---------------------------------------------------------------- KF / Gaussian
+def kf_predict(F_, B, Q, x, Pm):
+    x = _c(x, np.float64).copy()
+    Pm = _c(Pm, np.float64).copy()
+    d = len(x)
+    lib().mko_kf_predict(d, _p(_c(F_, np.float64)), _p(_c(B, np.float64)), _p(_c(Q, np.float64)),
+                         _p(x), _p(Pm))
+    return x, Pm
+
+
+def kf_update(H, BH, R, z, x, Pm, mask=None):
+    x = _c(x, np.float64).copy()
+    Pm = _c(Pm, np.float64).copy()
+    H = _c(H, np.float64)
+    m, d = H.shape
+    if mask is None:
+        mask = (1 << m) - 1
+    ok = lib().mko_kf_update(d, m, _p(H), _p(_c(BH, np.float64)), _p(_c(R, np.float64)),
+                             _p(_c(z, np.float64)), mask, _p(x), _p(Pm))
+    return x, Pm, bool(ok)
+
+
+def mvn_logpdf(x, u, S, mode=0):
+    x = _c(x, np.float64)
+    return lib().mko_mvn_logpdf(len(x), _p(x), _p(_c(u, np.float64)), _p(_c(S, np.float64)), mode)
+
+
+def load_gaussian_ref(u, s, Hpca, mpca, g):
+    u = _c(u, np.float64).ravel()
+    d = len(u)
+    Hpca = _c(Hpca, np.float64)
+    Fd = Hpca.shape[1]
+    out = dict(F=np.zeros((d, d)), B=np.zeros(d), Q=np.zeros((d, d)), H=np.zeros((6, d)),
+               BH=np.zeros(6), R=np.zeros((6, 6)))
+    lib().mko_load_gaussian_ref(d, Fd, _p(u), _p(_c(s, np.float64)), _p(Hpca),
+                                _p(_c(mpca, np.float64).ravel()), float(g),
+                                *[_p(out[k]) for k in ("F", "B", "Q", "H", "BH", "R")])
+    return out
+
+
+# ---------------------------------------------------------------- RBPF (A8)
+class RbpfModel:
+    """Holds numpy arrays alive for an mko_model."""
+
+    def __init__(self, d, m, K, F_, B, Q, R, weight, H=None, BH=None, Bm=None, mm=None,
+                 cam=(525.0, 525.0, 319.5, 239.5)):
+        self.arrs = {}
+
+        def keep(name, a):
+            if a is None:
+                return None
+            a = _c(a, np.float64)
+            self.arrs[name] = a
+            return _p(a)
+
+        mode = 0 if H is not None else 1
+        self.s = Model(d, m, K, mode, keep("F", F_), keep("B", B), keep("Q", Q), keep("H", H),
+                       keep("BH", BH), keep("R", R), keep("w", weight), keep("Bm", Bm),
+                       keep("mm", mm), cam[0], cam[1], cam[2], cam[3])
+        self.d, self.m, self.K = d, m, K
+
+    def measure(self, k, x):
+        zh = np.zeros(self.m)
+        Hx = np.zeros((self.m, self.d))
+        lib().mko_measure(C.byref(self.s), k, _p(_c(x, np.float64)), _p(zh), _p(Hx))
+        return zh, Hx
+
+    def update(self, x, Pm, z, U_ind, U_anc, mask=None, alias_prev_anc=None):
+        """x (N,d), P (N,d,d), z (N,m) -> dict; x,P updated in place copies."""
+        x = _c(x, np.float64).copy()
+        Pm = _c(Pm, np.float64).copy()
+        N = x.shape[0]
+        if mask is None:
+            mask = (1 << self.m) - 1
+        out = dict(ind=np.zeros(N, np.int32), logw=np.zeros(N), wn=np.zeros(N),
+                   anc=np.zeros(N, np.int32))
+        pa = _c(alias_prev_anc, np.int32) if alias_prev_anc is not None else None
+        fb = lib().mko_rbpf_update(C.byref(self.s), N, _p(x), _p(Pm), _p(_c(z, np.float64)),
+                                   mask, U_ind, U_anc, _p(pa), _p(out["ind"]), _p(out["logw"]),
+                                   _p(out["wn"]), _p(out["anc"]))
+        out.update(x=x, P=Pm, fallback=bool(fb))
+        return out
+
+
+def pdaf_weights(cand, hat_own, hat_other, var, Pa=0.05, clutter=1e-4, Lc=None):
+    cand = _c(cand, np.float64).reshape(-1, 2)
+    M = cand.shape[0]
+    w = np.zeros(M)
+    has_other = hat_other is not None
+    lib().mko_pdaf_weights(M, _p(cand), _p(_c(Lc, np.float64) if Lc is not None else None),
+                           _p(_c(hat_own, np.float64)),
+                           _p(_c(hat_other if has_other else [0, 0], np.float64)),
+                           int(has_other), float(var), float(Pa), float(clutter), _p(w))
+    return w
+
+
+# ---------------------------------------------------------------- A13
+def bpf_params(model, p, track):
+    """Build BpfParams for parameter block p of a synthetic.BpfBatch-like model."""
+    keep = []
+
+    def ptr(a):
+        a = _c(a, np.float32)
+        keep.append(a)
+        return _p(a)
+
+    d, K, J = model["d"], model["K"], model["J"]
+    s = BpfParams(d, K, J, ptr(model["a"][p]), ptr(model["mb"][p]), ptr(model["mu"][p]),
+                  ptr(model["Lq"][p]), ptr(model["S0c"][p]), ptr(model["cumpi"][p]),
+                  ptr(model["Bm"][p]), ptr(model["mm"][p]), *[float(v) for v in model["cam"]],
+                  float(track["kappa"]), float(track["pd"]), float(track["sigma"]))
+    return s, keep
+
+
+def bpf_prior(params, eps, ucomp):
+    x = np.zeros(params.d)
+    lib().mko_bpf_prior(C.byref(params), _p(_c(eps, np.float64)), float(ucomp), _p(x))
+    return x
+
+
+def bpf_propagate(params, x, eps, ucomp):
+    x = _c(x, np.float64).copy()
+    lib().mko_bpf_propagate(C.byref(params), _p(_c(eps, np.float64)), float(ucomp), _p(x))
+    return x
+
+
+def bpf_loglik(params, x, det_off, det):
+    return lib().mko_bpf_loglik(C.byref(params), _p(_c(x, np.float64)), _p(_c(det_off, np.int32)),
+                                _p(_c(det, np.float32)))
+
+
+def bpf_run_tracks(batch, track_ids, nthreads=0):
+    """Run the FP64 CPU bootstrap filter over the listed tracks of a batch
+    (synthetic.BpfBatch); returns est, loglik, ess arrays (frame-indexed)."""
+    L = lib()
+    m = batch.model
+    d, K, J = m["d"], m["K"], m["J"]
+    tr = (Track * len(track_ids))()
+    for n, b in enumerate(track_ids):
+        t = batch.tracks[b]
+        tr[n] = Track(int(t["n_particles"]), int(t["n_frames"]), int(t["frame_base"]),
+                      int(t["seed"]), int(t["track_id"]), int(t["param_index"]),
+                      float(t["kappa"]), float(t["pd"]), float(t["sigma"]))
+    G = batch.n_frames_total
+    est = np.zeros((G, d), np.float32)
+    ll = np.zeros(G, np.float32)
+    ess = np.zeros(G, np.float32)
+    arrs = [_c(m[k], np.float32) for k in ("a", "mb", "mu", "Lq", "S0c", "cumpi", "Bm", "mm")]
+    L.mko_bpf_run_tracks(len(track_ids), C.cast(tr, C.c_void_p), d, K, J, *[_p(a) for a in arrs],
+                         *[float(v) for v in m["cam"]], _p(_c(batch.det_off, np.int32)),
+                         _p(_c(batch.det, np.float32)), _p(est), _p(ll), _p(ess), int(nthreads))
+    return est, ll, ess
+
+
+def num_threads():
+    return lib().mko_num_threads()

@@ -1,0 +1,165 @@
+/*
+ * mkf_oracle.h -- FP64 CPU restatement of the mkfbodytracker_pdaf filtering hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA product
+ * (mkfbodytracker_pdaf_gb300/csrc) and the timed CPU baseline of bench.py; the
+ * product never links, loads or calls it.
+ *
+ * Parity status: the reference (ROS + OpenCV, rosbuild) has no tests, golden
+ * vectors or fixtures for this path and cannot be built here (no ROS, no
+ * OpenCV), so parity against the reference's own outputs is UNPINNED.  What is
+ * pinned: Philox4x32-10 against the published Random123 known-answer vectors,
+ * the exact systematic resampler against the reference's literal wheel on
+ * dyadic weights (where the wheel's FP arithmetic is exact), and the KF /
+ * Gaussian restatements against independent closed forms in the tests.
+ *
+ * Every function cites the reference file:line it restates.
+ */
+#ifndef MKF_ORACLE_H
+#define MKF_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- K1: Philox4x32-10 counter-based draws (replaces cv::RNG / randn / rand) */
+void mko_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* key = {lo32(seed), hi32(seed) ^ track}, ctr = {frame, item, stream, 0} */
+void mko_draw_block(uint64_t seed, uint32_t track, uint32_t frame, uint32_t item,
+                    uint32_t stream, uint32_t out[4]);
+float mko_u01_f32(uint32_t w);
+/* Box-Muller normals for one particle-frame, d (even, <= 24) normals + 1
+ * component uniform.  Layout: ceil(d/4) blocks at streams 0..; words 2p,2p+1
+ * feed pair p; the component uniform is the low bytes of words 0..2
+ * (libm; the GPU uses its own intrinsics, so parity tests feed GPU-dumped
+ * normals to the oracle instead of these). */
+void mko_particle_draws(uint64_t seed, uint32_t track, uint32_t frame, uint32_t item,
+                        int d, double* eps, float* ucomp);
+
+/* ---- A6: systematic resampling (pf2DRao.cpp:175-210, pf2D.cpp:279-323) */
+/* Literal reference wheel; u in [0,1); fallback[] used when max weight == 0. */
+void mko_resample_wheel(const double* w, int L, int N, double u, const int* fallback, int* idx);
+/* Quantise nonnegative weights to integers with 40 bits below the max (exact
+ * power-of-two scaling then truncation).  Returns 0 when the reference would
+ * take its max-weight-0 fallback (all weights zero/NaN) or a weight is +inf. */
+int mko_quantize_f64(const double* w, int L, uint64_t* q);
+int mko_quantize_f32(const float* w, int L, uint64_t* q);
+/* Exact systematic resampling on integer weights: idx[i] = first j with
+ * Q_j >= (i + U/2^32) * Q_{L-1} / N, evaluated in exact 128-bit integers. */
+void mko_resample_exact(const uint64_t* q, int L, int N, uint32_t U, int* idx);
+/* Full resampler used by every filter: quantise, exact systematic, or the
+ * fallback (idx_i = floor(u_i * L), u_i = Philox(key={U, 0x5EED}, ctr={i,0,0,0})).
+ * Returns 1 if the fallback was taken. */
+int mko_resample_f64(const double* w, int L, int N, uint32_t U, int* idx);
+int mko_resample_f32(const float* w, int L, int N, uint32_t U, int* idx);
+
+/* ---- A4/A5: KF_model (KF_model.cpp:11-25), dense reference form */
+void mko_kf_predict(int d, const double* F, const double* B, const double* Q, double* x, double* P);
+/* mask: bit r set => measurement row r used.  Returns 0 if S is singular. */
+int mko_kf_update(int d, int m, const double* H, const double* BH, const double* R,
+                  const double* z, unsigned mask, double* x, double* P);
+
+/* ---- A7: Gaussian log density (pf2DRao.cpp:34-67).  mode 0 = exact (intended
+ * semantics); 1 = the chol() quirk with OpenCV-2.4 diagonal convention (returned
+ * diagonal holds 1/L_ee); 2 = the quirk with the later convention (holds L_ee). */
+double mko_mvn_logpdf(int m, const double* x, const double* u, const double* S, int mode);
+
+/* ---- A1: my_gmm::loadGaussian (my_gmm.cpp:45-75), reference form.
+ * u: d, s: d*d, Hpca: d*F (pca_proj, rows = PCA dims), mpca: F.  Outputs the
+ * component's F,B,Q (d), H (6*d), BH (6), R (6*6). */
+void mko_load_gaussian_ref(int d, int Fdim, const double* u, const double* s,
+                           const double* Hpca, const double* mpca, double g,
+                           double* F, double* B, double* Q, double* H, double* BH, double* R);
+
+/* ---- A1..A10 model + RBPF (pf2DRao.cpp:125-158) */
+typedef struct {
+  int d, m, K;
+  int meas_mode;          /* 0 LINEAR (H x + BH), 1 PINHOLE (EKF per particle) */
+  const double* F;        /* K*d*d */
+  const double* B;        /* K*d   */
+  const double* Q;        /* K*d*d */
+  const double* H;        /* K*m*d (LINEAR) */
+  const double* BH;       /* K*m   (LINEAR) */
+  const double* R;        /* K*m*m */
+  const double* weight;   /* K (mixture weights pi) */
+  /* PINHOLE: measured joints J = m/2; joint j pixel = pi(Bm_j x + mm_j) */
+  const double* Bm;       /* J*3*d */
+  const double* mm;       /* J*3   */
+  double fx, fy, cx, cy;
+} mko_model;
+
+/* Predicted measurement and its Jacobian for state x (LINEAR or PINHOLE). */
+void mko_measure(const mko_model* M, int k, const double* x, double* zhat, double* Hx);
+
+/* One ParticleFilter::update (pf2DRao.cpp:125-158) with injected uniforms.
+ * x: N*d, P: N*d*d (updated in place, after resampling), z: N*m measurement
+ * columns stored row-per-particle, mask: measurement rows used.
+ * Outputs (optional, may be NULL): ind (N), logw (N), wn (N normalised), anc (N).
+ * alias_prev_anc != NULL (the previous update's ancestors) emulates the shallow
+ * cv::Mat copy-assign quirk (pf2DRao.cpp:153-156 with KF_model.cpp:13-24).
+ * Returns 1 if the resampling fallback was taken. */
+int mko_rbpf_update(const mko_model* M, int N, double* x, double* P, const double* z,
+                    unsigned mask, uint32_t U_ind, uint32_t U_anc, const int* alias_prev_anc,
+                    int* ind, double* logw, double* wn, int* anc);
+/* getEstimator (pf2DRao.cpp:23-31): uniform mean of track states. */
+void mko_rbpf_estimate(int N, int d, const double* x, double* est);
+
+/* ---- A9: PDAF association weights (pfPose.cpp:247-298) over a candidate list.
+ * p_a = N(c; hat_a, var I2) (mvnpdf_multiple, pf2DRao.cpp:69-83, 105-122);
+ * w_j = L_j / (Pa p_own + Pa p_other + clutter (1 - 2 Pa)); L_j = 1 for detections
+ * gives Pa p_own / Z when times Pa (the detection-list adapter).  For a single
+ * target (has_other = 0) the denominator is Pa p_own + clutter (1 - Pa). */
+void mko_pdaf_weights(int M, const double* cand, const double* Lc, const double* hat_own,
+                      const double* hat_other, int has_other, double var, double Pa,
+                      double clutter, double* w);
+
+/* ---- A13: bootstrap PF with the mixture motion model (config 1/2 kernels) */
+typedef struct {
+  int d, K, J;
+  const float* a;        /* K*d */
+  const float* mb;       /* K*d   (1-a)*mu */
+  const float* mu;       /* K*d */
+  const float* Lq;       /* K*d(d+1)/2 packed lower, row-major */
+  const float* S0c;      /* K*d(d+1)/2 chol(Sigma_k), prior */
+  const float* cumpi;    /* K */
+  const float* Bm;       /* J*3*d */
+  const float* mm;       /* J*3   */
+  float fx, fy, cx, cy;
+  float kappa, pd, sigma;
+} mko_bpf_params;
+
+int mko_pick_component(const float* cumpi, int K, float u);
+/* prior draw for one particle: x = mu_k + chol(Sigma_k) eps */
+void mko_bpf_prior(const mko_bpf_params* p, const double* eps, float ucomp, double* x);
+/* propagate x (d) in place with one particle-frame's draws */
+void mko_bpf_propagate(const mko_bpf_params* p, const double* eps, float ucomp, double* x);
+/* log-likelihood of the frame's typed detection lists given the state x.
+ * det_off: J+1 offsets into det (pairs). */
+double mko_bpf_loglik(const mko_bpf_params* p, const double* x, const int* det_off, const float* det);
+
+/* Run whole tracks (timed CPU baseline and end-to-end reference): draws from
+ * Philox + libm Box-Muller, resampling with mko_resample_f64 semantics on FP64
+ * weights.  Tracks are independent; OpenMP over tracks with nthreads. */
+typedef struct {
+  int n_particles, n_frames;
+  long long frame_base;     /* index of frame 0 in the frame-indexed arrays */
+  unsigned long long seed;
+  int track_id;
+  int param_index;
+  float kappa, pd, sigma;
+} mko_track;
+
+void mko_bpf_run_tracks(int n_tracks, const mko_track* tracks, int d, int K, int J,
+                        const float* a, const float* mb, const float* mu, const float* Lq,
+                        const float* S0c, const float* cumpi, const float* Bm, const float* mm,
+                        float fx, float fy, float cx, float cy,
+                        const int* det_off, const float* det,
+                        float* est, float* loglik, float* ess, int nthreads);
+
+int mko_num_threads(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
