@@ -211,8 +211,12 @@ def run_gb300(args):
     build.build()
     from mkfbodytracker_pdaf_gb300.filters import BatchedBootstrapPF
 
+    from mkfbodytracker_pdaf_gb300.autotune import load_tuning
+    tb, cps = load_tuning()
+    tb = args.block_threads or tb
+    cps = cps if args.ctas_per_sm is None else args.ctas_per_sm
     batch = workload(rank, args.tracks)
-    runner = BatchedBootstrapPF(batch, block_threads=args.block_threads, ctas_per_sm=args.ctas_per_sm)
+    runner = BatchedBootstrapPF(batch, block_threads=tb, ctas_per_sm=cps)
     det_off, det = runner.device_inputs()
     outs = runner.alloc_outputs()
     stream = torch.cuda.current_stream()
@@ -324,8 +328,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--tracks", type=int, default=8192)
-    ap.add_argument("--block-threads", type=int, default=256)
-    ap.add_argument("--ctas-per-sm", type=int, default=0)
+    ap.add_argument("--block-threads", type=int, default=None, help="default: autotuned choice")
+    ap.add_argument("--ctas-per-sm", type=int, default=None)
     ap.add_argument("--cpu-sample-tracks", type=int, default=24)
     ap.add_argument("--ref-sample-tracks", type=int, default=16)
     ap.add_argument("--plain-tracks", type=int, default=8)

@@ -1,0 +1,80 @@
+"""Autotuner for the batched persistent kernel: block size (and so particles
+per thread, ceil(N / block)) and resident CTAs per SM.
+
+Run on the target GPU:
+    python -m mkfbodytracker_pdaf_gb300.autotune --tracks 2048 --out tuning.json
+It times every candidate on a seeded subset of the batched-uneven-tracks
+workload (same distributions as the full batch) with CUDA events and writes
+the ranking; ``load_tuning()`` returns the stored best choice (used by the
+benchmark and the runners when present).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+TUNING_FILE = os.path.join(HERE, "tuning_gb300.json")
+# (block_threads, ctas_per_sm): 512x1 and 256x2 compile with a 128-register
+# budget, 256x3 with an 80-register budget (3 CTAs of 71 KB shared memory each)
+CANDIDATES = [(256, 2), (256, 3), (512, 1), (128, 3)]
+
+
+def load_tuning():
+    if os.path.exists(TUNING_FILE):
+        with open(TUNING_FILE) as f:
+            d = json.load(f)
+        return int(d["best"]["block_threads"]), int(d["best"]["ctas_per_sm"])
+    return 256, 2
+
+
+def tune(n_tracks=2048, reps=3, seed=None):
+    import torch
+    from . import build, synth
+    from .filters import BatchedBootstrapPF
+    build.build()
+    kw = {} if seed is None else {"seed": seed}
+    batch = synth.config2_batch(n_tracks=n_tracks, **kw)
+    runner = BatchedBootstrapPF(batch)
+    det_off, det = runner.device_inputs()
+    outs = runner.alloc_outputs()
+    G = batch.n_frames_total
+    res = []
+    for tb, cps in CANDIDATES:
+        try:
+            runner.set_tuning(tb, cps)
+            runner.run(det_off, det, outs)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                runner.run(det_off, det, outs)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            res.append({"block_threads": tb, "ctas_per_sm": cps, "ms": ms, "track_frames_per_s": G / ms * 1e3})
+        except Exception as ex:  # a shape that does not fit is reported, not fatal
+            res.append({"block_threads": tb, "ctas_per_sm": cps, "error": str(ex)})
+    ok = [r for r in res if "ms" in r]
+    best = min(ok, key=lambda r: r["ms"])
+    return {"workload": "batched uneven tracks subset: %d tracks, %d track-frames" % (n_tracks, G),
+            "gpu": torch.cuda.get_device_name(0), "when": time.strftime("%Y-%m-%dT%H:%M:%SZ", time.gmtime()),
+            "results": res, "best": best}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--tracks", type=int, default=2048)
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--out", default=TUNING_FILE)
+    a = ap.parse_args()
+    r = tune(a.tracks, a.reps)
+    with open(a.out, "w") as f:
+        json.dump(r, f, indent=1)
+    print(json.dumps(r))
+
+
+if __name__ == "__main__":
+    main()

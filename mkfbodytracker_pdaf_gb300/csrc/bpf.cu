@@ -114,6 +114,9 @@ __device__ __forceinline__ void prior_sample(const PView& p, const float* eps, f
   }
 }
 
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+
+// x' = A_k x + (I - A_k) mu_k + L_k eps  (rows of a, mb, Ld, Bm are 16-byte aligned: D % 4 == 0)
 template <int D, bool DIAG>
 __device__ __forceinline__ void propagate(const PView& p, const float* eps, float uc, float* x) {
   constexpr int DD = D * (D + 1) / 2;
@@ -123,7 +126,13 @@ __device__ __forceinline__ void propagate(const PView& p, const float* eps, floa
   if (DIAG) {
     const float* l = p.Ld + k * D;
 #pragma unroll
-    for (int r = 0; r < D; ++r) x[r] = fmaf(l[r], eps[r], fmaf(a[r], x[r], mb[r]));
+    for (int r = 0; r < D; r += 4) {
+      float4 av = ld4(a + r), mv = ld4(mb + r), lv = ld4(l + r);
+      x[r + 0] = fmaf(lv.x, eps[r + 0], fmaf(av.x, x[r + 0], mv.x));
+      x[r + 1] = fmaf(lv.y, eps[r + 1], fmaf(av.y, x[r + 1], mv.y));
+      x[r + 2] = fmaf(lv.z, eps[r + 2], fmaf(av.z, x[r + 2], mv.z));
+      x[r + 3] = fmaf(lv.w, eps[r + 3], fmaf(av.w, x[r + 3], mv.w));
+    }
   } else {
     const float* L = p.Lq + k * DD;
     float xn[D];
@@ -149,13 +158,20 @@ __device__ __forceinline__ float loglik(const PView& p, const float* x, const in
   float ll = 0.0f;
   for (int j = 0; j < p.J; ++j) {
     const float* B = p.Bm + j * 3 * D;
-    float q0 = p.mm[j * 3 + 0], q1 = p.mm[j * 3 + 1], q2 = p.mm[j * 3 + 2];
+    // two partial sums per row shorten the dependent FMA chains
+    float q0a = p.mm[j * 3 + 0], q1a = p.mm[j * 3 + 1], q2a = p.mm[j * 3 + 2];
+    float q0b = 0.0f, q1b = 0.0f, q2b = 0.0f;
 #pragma unroll
-    for (int c = 0; c < D; ++c) {
-      q0 = fmaf(B[c], x[c], q0);
-      q1 = fmaf(B[D + c], x[c], q1);
-      q2 = fmaf(B[2 * D + c], x[c], q2);
+    for (int c = 0; c < D; c += 4) {
+      float4 b0 = ld4(B + c), b1 = ld4(B + D + c), b2 = ld4(B + 2 * D + c);
+      q0a = fmaf(b0.x, x[c], q0a); q0b = fmaf(b0.y, x[c + 1], q0b);
+      q1a = fmaf(b1.x, x[c], q1a); q1b = fmaf(b1.y, x[c + 1], q1b);
+      q2a = fmaf(b2.x, x[c], q2a); q2b = fmaf(b2.y, x[c + 1], q2b);
+      q0a = fmaf(b0.z, x[c + 2], q0a); q0b = fmaf(b0.w, x[c + 3], q0b);
+      q1a = fmaf(b1.z, x[c + 2], q1a); q1b = fmaf(b1.w, x[c + 3], q1b);
+      q2a = fmaf(b2.z, x[c + 2], q2a); q2b = fmaf(b2.w, x[c + 3], q2b);
     }
+    const float q0 = q0a + q0b, q1 = q1a + q1b, q2 = q2a + q2b;
     if (!(q2 > kZMin)) { ll += __logf(kappa); continue; }
     float iz = 1.0f / q2;
     float u = fmaf(p.fx * q0, iz, p.cx), v = fmaf(p.fy * q1, iz, p.cy);
@@ -192,37 +208,68 @@ struct BatchArgs {
   int* dbg_anc;
 };
 
+__host__ __device__ constexpr int pad4(int n) { return (n + 3) & ~3; }
+
+// shared-memory parameter block: a | mb | L | Bm | mm | cumpi, every section 16-byte aligned
 template <int D>
 __host__ __device__ constexpr int params_floats(int K, int J, bool diag) {
-  return 2 * K * D + (diag ? K * D : K * D * (D + 1) / 2) + K + J * 3 * D + J * 3;
+  return 2 * K * D + pad4(diag ? K * D : K * D * (D + 1) / 2) + J * 3 * D + pad4(J * 3) + pad4(K);
 }
 
-template <int D, bool DIAG>
-__global__ void __launch_bounds__(512) bpf_batched_kernel(BatchArgs A) {
+// number of targets i in [0, N) with (i 2^32 + U) Qt <= N X 2^32
+__device__ __forceinline__ int count_targets_le(uint64_t X, int N, uint32_t U, uint64_t Qt) {
+  const unsigned __int128 lim = ((unsigned __int128)(uint64_t)N * (unsigned __int128)X) << 32;
+  double est = (double)N * ((double)X / (double)Qt);
+  long long i = (long long)est;
+  if (i < 0) i = 0;
+  if (i > N) i = N;
+  for (int it = 0; it < 64 && i < N && resample_rhs((int)i, U, Qt) <= lim; ++it) ++i;
+  for (int it = 0; it < 64 && i > 0 && resample_rhs((int)(i - 1), U, Qt) > lim; ++it) --i;
+  bool ok = (i == N || resample_rhs((int)i, U, Qt) > lim) && (i == 0 || resample_rhs((int)(i - 1), U, Qt) <= lim);
+  if (!ok) {
+    long long lo = 0, hi = N;
+    while (lo < hi) {
+      long long mid = (lo + hi) >> 1;
+      if (resample_rhs((int)mid, U, Qt) <= lim) lo = mid + 1; else hi = mid;
+    }
+    i = lo;
+  }
+  return (int)i;
+}
+
+// Batched persistent kernel.  Shared memory per CTA: W (float, Nmax) holds the
+// frame's log-weights then weights; ANC (int, Nmax) the ancestors; then the
+// track's model.  Particle states live in this CTA's global slot (two SoA
+// buffers of D x Nmax floats, L2-resident).  Per frame: propagate + score,
+// block max, weights/estimate/ESS, exact systematic resampling by a scatter
+// walk over each thread's contiguous chunk of integer weights.
+template <int D, bool DIAG, int TBMAX, int MINB>
+__global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int TB = blockDim.x, tid = threadIdx.x;
   constexpr int NV = D + 3;
-  uint64_t* sQ = reinterpret_cast<uint64_t*>(smem);                      // 8 Nmax
-  int* sA = reinterpret_cast<int*>(smem + 8 * (size_t)A.Nmax);           // 4 Nmax
-  float* sP = reinterpret_cast<float*>(smem + 12 * (size_t)A.Nmax);      // params
+  const int Nmax = A.Nmax;
+  float* sW = reinterpret_cast<float*>(smem);                            // 4 Nmax
+  int* sA = reinterpret_cast<int*>(smem + 4 * (size_t)Nmax);             // 4 Nmax
+  float* sP = reinterpret_cast<float*>(smem + 8 * (size_t)Nmax);         // params (Nmax % 32 == 0)
   const int K = A.K, J = A.J;
+  const int Lsz = pad4(DIAG ? K * D : K * D * (D + 1) / 2);
   float* s_a = sP;
   float* s_mb = s_a + K * D;
   float* s_L = s_mb + K * D;
-  float* s_cum = s_L + (DIAG ? K * D : K * D * (D + 1) / 2);
-  float* s_Bm = s_cum + K;
+  float* s_Bm = s_L + Lsz;
   float* s_mm = s_Bm + J * 3 * D;
-  float2* s_det = reinterpret_cast<float2*>(sP + ((params_floats<D>(K, J, DIAG) + 1) & ~1));
+  float* s_cum = s_mm + pad4(J * 3);
+  float2* s_det = reinterpret_cast<float2*>(sP + params_floats<D>(K, J, DIAG));
   int* s_cnt = reinterpret_cast<int*>(s_det + MKF_MAX_J * MKF_MAX_DET);
   float* s_red = reinterpret_cast<float*>(s_cnt + 8);                    // 32*NV floats
-  uint64_t* s_red64 = reinterpret_cast<uint64_t*>(s_red + 32 * NV + 2);  // 33 u64 (aligned below)
+  uint64_t* s_red64 = reinterpret_cast<uint64_t*>(s_red + 32 * NV + 2);
   s_red64 = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(s_red64) + 7) & ~uintptr_t(7));
   __shared__ int s_item;
   __shared__ int s_flag;
 
-  float* xa0 = A.scratch + (size_t)blockIdx.x * 2 * D * A.Nmax;
-  float* xb0 = xa0 + (size_t)D * A.Nmax;
-  const int Nmax = A.Nmax;
+  float* xa0 = A.scratch + (size_t)blockIdx.x * 2 * D * Nmax;
+  float* xb0 = xa0 + (size_t)D * Nmax;
 
   for (;;) {
     if (tid == 0) s_item = atomicAdd(A.counter, 1);
@@ -237,8 +284,7 @@ __global__ void __launch_bounds__(512) bpf_batched_kernel(BatchArgs A) {
     const long long g0 = A.fbase[b];
     const unsigned long long seed = A.seed[b];
     const float4 ob = A.obs[b];
-    // stage this track's model in shared memory
-    {
+    {  // stage this track's model in shared memory
       const float* ga = A.m.a + (size_t)mi * K * D;
       const float* gmb = A.m.mb + (size_t)mi * K * D;
       const float* gL = DIAG ? A.m.Ld + (size_t)mi * K * D : A.m.Lq + (size_t)mi * K * D * (D + 1) / 2;
@@ -273,9 +319,10 @@ __global__ void __launch_bounds__(512) bpf_batched_kernel(BatchArgs A) {
     }
     __syncthreads();
 
+    const int E = (N + TB - 1) / TB;                 // contiguous chunk per thread
+    const int j0 = min(N, tid * E), j1 = min(N, j0 + E);
     for (int t = 0; t < T; ++t) {
       const long long g = g0 + t;
-      // this frame's detection lists
       if (tid < J) {
         int lo = A.det_off[g * J + tid], hi = A.det_off[g * J + tid + 1];
         int n = hi - lo;
@@ -301,21 +348,21 @@ __global__ void __launch_bounds__(512) bpf_batched_kernel(BatchArgs A) {
 #pragma unroll
         for (int r = 0; r < D; ++r) xb[(size_t)r * Nmax + i] = x[r];
         float ll = loglik<D>(pv, x, s_cnt, s_det, ob.x, ob.y, ob.z);
-        sA[i] = __float_as_int(ll);
+        sW[i] = ll;
         lmax = fmaxf(lmax, ll);
       }
       const float M = block_max(lmax, s_red);
       const bool fb = !(M > -INFINITY) || !(M < INFINITY);
 
-      // ---- normalised weights, weighted-mean estimate, ESS
+      // ---- weights normalised to the max, weighted-mean estimate, ESS
       float acc[NV];
 #pragma unroll
       for (int c = 0; c < NV; ++c) acc[c] = 0.0f;   // s, s2, wmax, v[D]
       for (int i = tid; i < N; i += TB) {
-        float ll = __int_as_float(sA[i]);
+        float ll = sW[i];
         float w = fb ? 0.0f : (ll == M ? 1.0f : __expf(ll - M));
         if (!(w >= 0.0f)) w = 0.0f;
-        sA[i] = __float_as_int(w);
+        sW[i] = w;
         if (dbg) A.dbg_w[(size_t)t * N + i] = w;
         acc[0] += w;
         acc[1] = fmaf(w, w, acc[1]);
@@ -348,30 +395,27 @@ __global__ void __launch_bounds__(512) bpf_batched_kernel(BatchArgs A) {
       }
       int e = 0;
       frexpf(Wmax, &e);
-      __syncthreads();
 
-      // ---- quantise + exact prefix sums (contiguous chunk per thread)
-      const int E = (N + TB - 1) / TB;
-      const int j0 = min(N, tid * E), j1 = min(N, j0 + E);
+      // ---- exact systematic resampling: chunk sums, block scan, scatter walk
       uint64_t cs = 0;
-      for (int j = j0; j < j1; ++j) cs += quantize_f32(__int_as_float(sA[j]), e);
+      for (int j = j0; j < j1; ++j) cs += quantize_f32(sW[j], e);
       uint64_t Qt;
-      uint64_t pre = block_excl_scan_u64(cs, s_red64, &Qt);
-      for (int j = j0; j < j1; ++j) {
-        pre += quantize_f32(__int_as_float(sA[j]), e);
-        sQ[j] = pre;
-      }
-      __syncthreads();
-
-      // ---- systematic ancestors by exact search
+      uint64_t P = block_excl_scan_u64(cs, s_red64, &Qt);   // includes barriers
       const uint32_t U = resample_uniform(seed, trk, (uint32_t)t);
-      const bool fb2 = fb || Qt == 0;
-      for (int i = tid; i < N; i += TB) {
-        int an = fb2 ? resample_fallback_index(U, i, N) : resample_search(sQ, N, N, resample_rhs(i, U, Qt));
-        sA[i] = an;
-        if (dbg) A.dbg_anc[(size_t)t * N + i] = an;
+      if (fb || Qt == 0) {
+        for (int i = tid; i < N; i += TB) sA[i] = resample_fallback_index(U, i, N);
+      } else if (j0 < j1) {
+        int i = (j0 == 0) ? 0 : count_targets_le(P, N, U, Qt);
+        uint64_t Qj = P;
+        for (int j = j0; j < j1; ++j) {
+          Qj += quantize_f32(sW[j], e);
+          const unsigned __int128 lim = ((unsigned __int128)(uint64_t)N * (unsigned __int128)Qj) << 32;
+          while (i < N && resample_rhs(i, U, Qt) <= lim) sA[i++] = j;
+        }
       }
       __syncthreads();
+      if (dbg)
+        for (int i = tid; i < N; i += TB) A.dbg_anc[(size_t)t * N + i] = sA[i];
       float* tmp = xa; xa = xb; xb = tmp;
     }
     if (tid == 0) A.status[b] = s_flag;
@@ -381,7 +425,7 @@ __global__ void __launch_bounds__(512) bpf_batched_kernel(BatchArgs A) {
 
 static size_t batched_smem_bytes(int D, int Nmax, int K, int J, bool diag) {
   size_t pf = (D == 12) ? params_floats<12>(K, J, diag) : params_floats<24>(K, J, diag);
-  size_t bytes = 12 * (size_t)Nmax + 4 * ((pf + 1) & ~size_t(1)) + 8 * MKF_MAX_J * MKF_MAX_DET + 32 +
+  size_t bytes = 8 * (size_t)Nmax + 4 * pf + 8 * MKF_MAX_J * MKF_MAX_DET + 32 +
                  4 * (32 * (D + 3) + 2) + 8 * 34 + 16;
   return (bytes + 15) & ~size_t(15);
 }
@@ -632,29 +676,6 @@ __global__ void __launch_bounds__(256) bpf_stream_b(StreamArgs A) {
   }
 }
 
-__device__ __forceinline__ int count_targets_le(uint64_t X, int N, uint32_t U, uint64_t Qt) {
-  // number of targets i in [0,N) with (i 2^32 + U) Qt <= N X 2^32
-  const unsigned __int128 lim = ((unsigned __int128)(uint64_t)N * (unsigned __int128)X) << 32;
-  double est = (double)N * ((double)X / (double)Qt);
-  long long i = (long long)est;
-  if (i < 0) i = 0;
-  if (i > N) i = N;
-  // smallest i with R_i > lim
-  for (int it = 0; it < 64 && i < N && resample_rhs((int)i, U, Qt) <= lim; ++it) ++i;
-  for (int it = 0; it < 64 && i > 0 && resample_rhs((int)(i - 1), U, Qt) > lim; ++it) --i;
-  // guarantee correctness if the estimate was far off: binary search fallback
-  bool ok = (i == N || resample_rhs((int)i, U, Qt) > lim) && (i == 0 || resample_rhs((int)(i - 1), U, Qt) <= lim);
-  if (!ok) {
-    long long lo = 0, hi = N;
-    while (lo < hi) {
-      long long mid = (lo + hi) >> 1;
-      if (resample_rhs((int)mid, U, Qt) <= lim) lo = mid + 1; else hi = mid;
-    }
-    i = lo;
-  }
-  return (int)i;
-}
-
 __global__ void __launch_bounds__(256) bpf_stream_c(StreamArgs A, int tile_c) {
   extern __shared__ __align__(16) unsigned char smem_c[];
   uint64_t* sQ = reinterpret_cast<uint64_t*>(smem_c);
@@ -725,6 +746,7 @@ struct mkf_bpf_batch {
   int* counter;
   float* scratch;
   size_t scratch_slots;
+  int last_grid;
   int dbg_track;
   float* dbg_w;
   int* dbg_anc;
@@ -965,9 +987,9 @@ extern "C" int mkf_bpf_batch_set_debug(mkf_bpf_batch_t B, int track, float* d_w,
   return MKF_OK;
 }
 
-template <int D, bool DIAG>
-static int launch_batched(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
-  auto kern = bpf_batched_kernel<D, DIAG>;
+template <int D, bool DIAG, int TBMAX, int MINB>
+static int launch_batched_v(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
+  auto kern = bpf_batched_kernel<D, DIAG, TBMAX, MINB>;
   size_t smem = batched_smem_bytes(D, B->Nmax, B->K, B->J, DIAG);
   MKF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int occ = 0;
@@ -985,10 +1007,19 @@ static int launch_batched(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
     B->scratch_slots = need;
   }
   a.scratch = B->scratch;
+  B->last_grid = (int)grid;
   MKF_CUDA(cudaMemsetAsync(B->counter, 0, sizeof(int), s));
   kern<<<(int)grid, B->tb, smem, s>>>(a);
   MKF_CHECK_LAUNCH("mkf_bpf_batch_run: batched kernel");
   return MKF_OK;
+}
+
+// launch-bound variant by block size and requested residency
+template <int D, bool DIAG>
+static int launch_batched(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
+  if (B->tb > 256) return launch_batched_v<D, DIAG, 512, 1>(B, a, s);
+  if (B->ctas_per_sm >= 3) return launch_batched_v<D, DIAG, 256, 3>(B, a, s);
+  return launch_batched_v<D, DIAG, 256, 2>(B, a, s);
 }
 
 extern "C" int mkf_bpf_batch_run(mkf_bpf_batch_t B, const int* d_det_off, const float* d_det,
