@@ -162,6 +162,86 @@ int mkf_bpf_batch_run_host(mkf_bpf_batch_t h, const int* det_off, const float* d
 int mkf_bpf_batch_set_debug(mkf_bpf_batch_t h, int track, float* d_w, int* d_anc);
 int mkf_bpf_batch_destroy(mkf_bpf_batch_t h);
 
+
+/* --------------------------------------- A1-A5, A7, A8, A10 Rao-Blackwellised PF */
+/* pf2DRao ParticleFilter(int nParticles) + its my_gmm (pf2DRao.h:13-31,
+ * my_gmm.h:20-33), FP64.  Each particle is a Kalman filter (state_params,
+ * my_gmm.h:9-18) whose GMM component is redrawn every update by systematic
+ * resampling of the mixture weights (pf2DRao.cpp:128).  Measurement model:
+ * LINEAR (per component H_k x + BH_k, my_gmm.cpp:59-72) or PINHOLE (EKF per
+ * particle: joint j pixel = pinhole(Bm_j x + mm_j), Jacobian at the
+ * predicted state).  Particle tracks are independent copies after resampling
+ * (the standard RBPF; the reference's shallow cv::Mat copy-assign at
+ * pf2DRao.cpp:153-156 makes duplicates share buffers, which only the oracle
+ * emulates). */
+typedef struct mkf_rbpf* mkf_rbpf_t;
+enum { MKF_MEAS_LINEAR = 0, MKF_MEAS_PINHOLE = 1 };
+/* d in {12, 24}; m <= MKF_MAX_M measurement rows; K <= MKF_MAX_K components;
+ * n_particles <= 65536 */
+int mkf_rbpf_create(int d, int m, int K, int n_particles, int meas_mode, uint64_t seed,
+                    uint32_t track_id, mkf_rbpf_t* out);
+/* my_gmm::loadGaussian(u, s, H, m, w, g) (my_gmm.cpp:45-75), host pointers:
+ * u (d), s (d*d), Hpca (d*F, the pca_proj matrix), mpca (F).  Sets F = g I,
+ * B = (1-g) u, Q = (1-g^2) s, R = 100 I_6, H = H1 Hpca^T, BH = H1 mpca^T with the
+ * head/hand/neck selector H1 of my_gmm.cpp:59-67 (requires m == 6, LINEAR). */
+int mkf_rbpf_load_gaussian(mkf_rbpf_t h, int k, const double* u, const double* s,
+                           const double* Hpca, const double* mpca, int F, double w, double g);
+/* config form of a component: mu (d), a (d, F = diag(a)), Q (d*d), Sigma (d*d,
+ * reset covariance), R (m*m), w; LINEAR additionally H (m*d), BH (m). */
+int mkf_rbpf_set_component(mkf_rbpf_t h, int k, const double* mu, const double* a, const double* Q,
+                           const double* Sigma, const double* R, double w, const double* H,
+                           const double* BH);
+/* PINHOLE geometry: Bm (J*3*d), mm (J*3) with J = m/2, camera intrinsics */
+int mkf_rbpf_set_pinhole(mkf_rbpf_t h, const double* Bm, const double* mm, double fx, double fy,
+                         double cx, double cy);
+/* hand-pixel decode used by the PDAF association: LINEAR: hand = Hd x + hb with
+ * Hd (2*d), hb (2) (rows 0,1 of H_pca^T x + m_pca, pfPose.cpp:222; pf2DRao.cpp:94);
+ * PINHOLE: joint index `joint` of the pinhole geometry. */
+int mkf_rbpf_set_hand_decode(mkf_rbpf_t h, const double* Hd, const double* hb, int joint);
+/* my_gmm::resetTracker(bins) (my_gmm.cpp:30-42): track i <- (mu_bins[i],
+ * Sigma_bins[i]).  bins (host, N) or NULL to draw bins = resample(pi, N) with
+ * Philox uniform word 0 of block (0xFFFFFFFF, 0xFFFFFFFF, 0x102). */
+int mkf_rbpf_reset(mkf_rbpf_t h, const int* bins, mkf_stream_t stream);
+/* ParticleFilter::update(measurement) (pf2DRao.cpp:125-158): d_meas is N rows
+ * of m values (the reference's m x N measurement, one column per particle);
+ * mask selects the rows used.  Uniforms: indicators word 0 of block
+ * (frame, 0xFFFFFFFF, 0x102), ancestors word 0 of (frame, 0xFFFFFFFF, 0x100). */
+int mkf_rbpf_update(mkf_rbpf_t h, uint32_t frame, const double* d_meas, unsigned mask,
+                    mkf_stream_t stream);
+/* the same with explicit uniforms (U/2^32 in [0,1)) */
+int mkf_rbpf_update_u(mkf_rbpf_t h, const double* d_meas, unsigned mask, uint32_t U_ind,
+                      uint32_t U_anc, mkf_stream_t stream);
+/* getEstimator() (pf2DRao.cpp:23-31): uniform mean of the tracks' states */
+int mkf_rbpf_estimate(mkf_rbpf_t h, double* d_est, mkf_stream_t stream);
+/* copies of the filter state / last update into caller device buffers (any may
+ * be NULL): x (N*d), P (N*d*d), logw (N), normalised weights (N), indicators
+ * (N), ancestors (N) */
+int mkf_rbpf_read(mkf_rbpf_t h, double* d_x, double* d_P, double* d_logw, double* d_wn, int* d_ind,
+                  int* d_anc, mkf_stream_t stream);
+/* overwrite the tracks (device pointers x (N*d), P (N*d*d)) */
+int mkf_rbpf_write(mkf_rbpf_t h, const double* d_x, const double* d_P, mkf_stream_t stream);
+int mkf_rbpf_status(mkf_rbpf_t h, int* status);
+int mkf_rbpf_destroy(mkf_rbpf_t h);
+
+/* ------------------------------------------------------- A9 PDAF association */
+/* PFTracker::getMeasurementProposal (pfPose.cpp:210-329) over a detection list,
+ * for the two arm filters at once.  Per arm a: hat_a = the hand pixel decoded
+ * from arm a's getEstimator(); each candidate c_j gets
+ * w_j = Pa p_a(c_j) / (Pa p_a(c_j) + Pa p_o(c_j) + clutter (1 - 2 Pa)),
+ * p = N(c; hat, var I2) with var = 0.8 * roi width (the covariance of
+ * getSampleProb, pf2DRao.cpp:114); the weights are normalised and resampled
+ * (mkf_resample semantics, uniform word 0 of block (frame, 0xFFFFFFFF, 0x103)
+ * of that arm's key) into N bins, and measurement row i of arm a is
+ * [head_x, head_y, c_bins[i].x, c_bins[i].y (, neck_x, neck_y if m == 6)] with
+ * head = (x + w/2, y + h/2), neck = (x + w/2, y + 1.65 h) of the arm's ROI
+ * (pfPose.cpp:303-323).  roi: host, 4 doubles per arm (x_offset, y_offset,
+ * width, height).  d_cand: M candidate (x,y) pairs (device, M <= 65536); when
+ * M == 0 the hand rows are not written (the caller masks them).  d_meas_a:
+ * N*m per arm.  d_bins_a (optional): N per arm. */
+int mkf_pdaf_associate(mkf_rbpf_t arm0, mkf_rbpf_t arm1, uint32_t frame, const double* roi,
+                       const double* d_cand, int M, double Pa, double clutter, double* d_meas0,
+                       double* d_meas1, int* d_bins0, int* d_bins1, mkf_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -62,6 +62,20 @@ SIGNATURES = {
     "mkf_bpf_batch_run_host": (I, [P, P, P, I64, P, P, P, P, P]),
     "mkf_bpf_batch_set_debug": (I, [P, I, P, P]),
     "mkf_bpf_batch_destroy": (I, [P]),
+    "mkf_rbpf_create": (I, [I, I, I, I, I, U64, U32, C.POINTER(P)]),
+    "mkf_rbpf_load_gaussian": (I, [P, I, P, P, P, P, I, C.c_double, C.c_double]),
+    "mkf_rbpf_set_component": (I, [P, I, P, P, P, P, P, C.c_double, P, P]),
+    "mkf_rbpf_set_pinhole": (I, [P, P, P, C.c_double, C.c_double, C.c_double, C.c_double]),
+    "mkf_rbpf_set_hand_decode": (I, [P, P, P, I]),
+    "mkf_rbpf_reset": (I, [P, P, P]),
+    "mkf_rbpf_update": (I, [P, U32, P, C.c_uint, P]),
+    "mkf_rbpf_update_u": (I, [P, P, C.c_uint, U32, U32, P]),
+    "mkf_rbpf_estimate": (I, [P, P, P]),
+    "mkf_rbpf_read": (I, [P, P, P, P, P, P, P, P]),
+    "mkf_rbpf_write": (I, [P, P, P, P]),
+    "mkf_rbpf_status": (I, [P, C.POINTER(I)]),
+    "mkf_rbpf_destroy": (I, [P]),
+    "mkf_pdaf_associate": (I, [P, P, U32, P, P, I, C.c_double, C.c_double, P, P, P, P, P]),
 }
 
 _lib = None

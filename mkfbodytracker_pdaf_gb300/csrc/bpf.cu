@@ -216,27 +216,6 @@ __host__ __device__ constexpr int params_floats(int K, int J, bool diag) {
   return 2 * K * D + pad4(diag ? K * D : K * D * (D + 1) / 2) + J * 3 * D + pad4(J * 3) + pad4(K);
 }
 
-// number of targets i in [0, N) with (i 2^32 + U) Qt <= N X 2^32
-__device__ __forceinline__ int count_targets_le(uint64_t X, int N, uint32_t U, uint64_t Qt) {
-  const unsigned __int128 lim = ((unsigned __int128)(uint64_t)N * (unsigned __int128)X) << 32;
-  double est = (double)N * ((double)X / (double)Qt);
-  long long i = (long long)est;
-  if (i < 0) i = 0;
-  if (i > N) i = N;
-  for (int it = 0; it < 64 && i < N && resample_rhs((int)i, U, Qt) <= lim; ++it) ++i;
-  for (int it = 0; it < 64 && i > 0 && resample_rhs((int)(i - 1), U, Qt) > lim; ++it) --i;
-  bool ok = (i == N || resample_rhs((int)i, U, Qt) > lim) && (i == 0 || resample_rhs((int)(i - 1), U, Qt) <= lim);
-  if (!ok) {
-    long long lo = 0, hi = N;
-    while (lo < hi) {
-      long long mid = (lo + hi) >> 1;
-      if (resample_rhs((int)mid, U, Qt) <= lim) lo = mid + 1; else hi = mid;
-    }
-    i = lo;
-  }
-  return (int)i;
-}
-
 // Batched persistent kernel.  Shared memory per CTA: W (float, Nmax) holds the
 // frame's log-weights then weights; ANC (int, Nmax) the ancestors; then the
 // track's model.  Particle states live in this CTA's global slot (two SoA

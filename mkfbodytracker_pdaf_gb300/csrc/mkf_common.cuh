@@ -185,6 +185,43 @@ __device__ __forceinline__ int resample_fallback_index(uint32_t U, int i, int L)
   u32x4 o = philox4x32_10(u32x4{(uint32_t)i, 0u, 0u, 0u}, U, 0x5EEDu);
   return (int)(((uint64_t)o.x * (uint64_t)L) >> 32);
 }
+// number of targets i in [0, N) with (i 2^32 + U) Qt <= N X 2^32
+__device__ __forceinline__ int count_targets_le(uint64_t X, int N, uint32_t U, uint64_t Qt) {
+  const unsigned __int128 lim = ((unsigned __int128)(uint64_t)N * (unsigned __int128)X) << 32;
+  double est = (double)N * ((double)X / (double)Qt);
+  long long i = (long long)est;
+  if (i < 0) i = 0;
+  if (i > N) i = N;
+  for (int it = 0; it < 64 && i < N && resample_rhs((int)i, U, Qt) <= lim; ++it) ++i;
+  for (int it = 0; it < 64 && i > 0 && resample_rhs((int)(i - 1), U, Qt) > lim; ++it) --i;
+  bool ok = (i == N || resample_rhs((int)i, U, Qt) > lim) && (i == 0 || resample_rhs((int)(i - 1), U, Qt) <= lim);
+  if (!ok) {
+    long long lo = 0, hi = N;
+    while (lo < hi) {
+      long long mid = (lo + hi) >> 1;
+      if (resample_rhs((int)mid, U, Qt) <= lim) lo = mid + 1; else hi = mid;
+    }
+    i = lo;
+  }
+  return (int)i;
+}
+
+// Scatter walk of exact systematic resampling for one thread's contiguous chunk
+// [j0, j1) of integer weights q_j (get(j)), whose exclusive prefix is P: emits
+// ancestors j for every target i whose rule "first j with N Q_j 2^32 >=
+// (i 2^32 + U) Qt" lands in the chunk.
+template <typename GetQ>
+__device__ __forceinline__ void scatter_walk(int j0, int j1, uint64_t P, int N, uint32_t U, uint64_t Qt,
+                                             GetQ get, int* anc) {
+  if (j0 >= j1) return;
+  int i = (j0 == 0) ? 0 : count_targets_le(P, N, U, Qt);
+  uint64_t Qj = P;
+  for (int j = j0; j < j1; ++j) {
+    Qj += get(j);
+    const unsigned __int128 lim = ((unsigned __int128)(uint64_t)N * (unsigned __int128)Qj) << 32;
+    while (i < N && resample_rhs(i, U, Qt) <= lim) anc[i++] = j;
+  }
+}
 #endif  // __CUDACC__
 
 }  // namespace mkf

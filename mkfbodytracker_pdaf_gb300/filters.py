@@ -184,3 +184,156 @@ class BatchedBootstrapPF:
                 self.h = None
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------- RBPF (pf2DRao)
+MEAS_LINEAR, MEAS_PINHOLE = 0, 1
+
+
+def _d(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def _hp(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+class RaoBlackwellisedPF:
+    """pf2DRao ParticleFilter(nParticles) with its my_gmm (pf2DRao.h:13-31):
+    loadGaussian / resetTracker / update(measurement) / getEstimator, FP64 on
+    the GPU.  Measurements are (N, m) CUDA tensors, one row per particle."""
+
+    def __init__(self, d, m, K, n_particles, meas_mode=MEAS_LINEAR, seed=0, track_id=0):
+        import torch
+        self.torch = torch
+        self.d, self.m, self.K, self.N, self.mode = d, m, K, n_particles, meas_mode
+        h = C.c_void_p()
+        N.check(N.lib().mkf_rbpf_create(d, m, K, n_particles, meas_mode, int(seed), int(track_id),
+                                        C.byref(h)), "mkf_rbpf_create")
+        self.h = h
+        self.est = torch.zeros(d, dtype=torch.float64, device="cuda")
+
+    # my_gmm::loadGaussian (reference form: F = gI, Q = (1-g^2) s, R = 100 I6, H = H1 Hpca^T)
+    def loadGaussian(self, k, u, s, Hpca, mpca, w, g):
+        Hpca = _d(Hpca)
+        N.check(N.lib().mkf_rbpf_load_gaussian(self.h, k, _hp(_d(u).ravel()), _hp(_d(s)), _hp(Hpca),
+                                               _hp(_d(mpca).ravel()), Hpca.shape[1], float(w), float(g)),
+                "mkf_rbpf_load_gaussian")
+
+    def set_component(self, k, mu, a, Q, Sigma, R, w, H=None, BH=None):
+        N.check(N.lib().mkf_rbpf_set_component(
+            self.h, k, _hp(_d(mu)), _hp(_d(a)), _hp(_d(Q)), _hp(_d(Sigma)), _hp(_d(R)), float(w),
+            _hp(_d(H) if H is not None else None), _hp(_d(BH) if BH is not None else None)),
+            "mkf_rbpf_set_component")
+
+    def set_pinhole(self, Bm, mm, cam):
+        fx, fy, cx, cy = cam
+        N.check(N.lib().mkf_rbpf_set_pinhole(self.h, _hp(_d(Bm)), _hp(_d(mm)), fx, fy, cx, cy),
+                "mkf_rbpf_set_pinhole")
+
+    def set_hand_decode(self, Hd=None, hb=None, joint=1):
+        N.check(N.lib().mkf_rbpf_set_hand_decode(self.h, _hp(_d(Hd) if Hd is not None else None),
+                                                 _hp(_d(hb) if hb is not None else None), joint),
+                "mkf_rbpf_set_hand_decode")
+
+    def resetTracker(self, bins=None, stream=None):
+        b = np.ascontiguousarray(bins, np.int32) if bins is not None else None
+        N.check(N.lib().mkf_rbpf_reset(self.h, _hp(b), _stream(self.torch, stream)), "mkf_rbpf_reset")
+
+    def update(self, meas, mask=None, frame=0, U=None, stream=None):
+        mask = (1 << self.m) - 1 if mask is None else mask
+        if U is None:
+            N.check(N.lib().mkf_rbpf_update(self.h, int(frame), _ptr(meas), mask, _stream(self.torch, stream)),
+                    "mkf_rbpf_update")
+        else:
+            N.check(N.lib().mkf_rbpf_update_u(self.h, _ptr(meas), mask, int(U[0]), int(U[1]),
+                                              _stream(self.torch, stream)), "mkf_rbpf_update_u")
+
+    def getEstimator(self, out=None, stream=None):
+        out = self.est if out is None else out
+        N.check(N.lib().mkf_rbpf_estimate(self.h, _ptr(out), _stream(self.torch, stream)), "mkf_rbpf_estimate")
+        return out
+
+    def read(self, stream=None):
+        t = self.torch
+        d, Np = self.d, self.N
+        o = dict(x=t.empty((Np, d), dtype=t.float64, device="cuda"),
+                 P=t.empty((Np, d, d), dtype=t.float64, device="cuda"),
+                 logw=t.empty(Np, dtype=t.float64, device="cuda"),
+                 wn=t.empty(Np, dtype=t.float64, device="cuda"),
+                 ind=t.empty(Np, dtype=t.int32, device="cuda"),
+                 anc=t.empty(Np, dtype=t.int32, device="cuda"))
+        N.check(N.lib().mkf_rbpf_read(self.h, _ptr(o["x"]), _ptr(o["P"]), _ptr(o["logw"]), _ptr(o["wn"]),
+                                      _ptr(o["ind"]), _ptr(o["anc"]), _stream(t, stream)), "mkf_rbpf_read")
+        return o
+
+    def write(self, x, P, stream=None):
+        N.check(N.lib().mkf_rbpf_write(self.h, _ptr(x), _ptr(P), _stream(self.torch, stream)), "mkf_rbpf_write")
+
+    def status(self):
+        s = C.c_int()
+        N.check(N.lib().mkf_rbpf_status(self.h, C.byref(s)), "mkf_rbpf_status")
+        return s.value
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                N.lib().mkf_rbpf_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+
+def pdaf_associate(arm0, arm1, frame, roi, cand, Pa=0.05, clutter=1e-4, meas=None, bins=None, stream=None):
+    """PFTracker::getMeasurementProposal over a detection list (pfPose.cpp:210-329).
+    roi: (2, 4) host array of (x_offset, y_offset, width, height) per arm;
+    cand: (M, 2) float64 CUDA tensor.  Returns (meas0, meas1, bins0, bins1)."""
+    torch = arm0.torch
+    roi = _d(roi).reshape(8)
+    if meas is None:
+        meas = (torch.zeros((arm0.N, arm0.m), dtype=torch.float64, device="cuda"),
+                torch.zeros((arm1.N, arm1.m), dtype=torch.float64, device="cuda"))
+    if bins is None:
+        bins = (torch.zeros(arm0.N, dtype=torch.int32, device="cuda"),
+                torch.zeros(arm1.N, dtype=torch.int32, device="cuda"))
+    M = 0 if cand is None else int(cand.shape[0])
+    N.check(N.lib().mkf_pdaf_associate(arm0.h, arm1.h, int(frame), _hp(roi), _ptr(cand) if M else None, M,
+                                       float(Pa), float(clutter), _ptr(meas[0]), _ptr(meas[1]),
+                                       _ptr(bins[0]), _ptr(bins[1]), _stream(torch, stream)),
+            "mkf_pdaf_associate")
+    return meas[0], meas[1], bins[0], bins[1]
+
+
+class PoseTracker:
+    """ROS-free replacement of PFTracker's per-frame flow (pfPose.cpp:332-385):
+    with a head ROI present, associate hand candidates (PDAF) and update both
+    arms, then read both estimates; with no ROI the frame is skipped
+    (pfPose.cpp:370-378).  Arms are RaoBlackwellisedPF instances."""
+
+    def __init__(self, arm0, arm1, Pa=0.05, clutter=1e-4):
+        self.arms = (arm0, arm1)
+        self.Pa, self.clutter = Pa, clutter
+        torch = arm0.torch
+        self.torch = torch
+        self.meas = (torch.zeros((arm0.N, arm0.m), dtype=torch.float64, device="cuda"),
+                     torch.zeros((arm1.N, arm1.m), dtype=torch.float64, device="cuda"))
+        self.bins = (torch.zeros(arm0.N, dtype=torch.int32, device="cuda"),
+                     torch.zeros(arm1.N, dtype=torch.int32, device="cuda"))
+        self.est = (torch.zeros(arm0.d, dtype=torch.float64, device="cuda"),
+                    torch.zeros(arm1.d, dtype=torch.float64, device="cuda"))
+
+    def step(self, frame, roi, cand):
+        """roi: (2,4) per-arm ROI or None (no face -> skip); cand: (M,2) CUDA float64."""
+        if roi is None:
+            return None
+        M = 0 if cand is None else int(cand.shape[0])
+        pdaf_associate(self.arms[0], self.arms[1], frame, roi, cand, self.Pa, self.clutter,
+                       meas=self.meas, bins=self.bins)
+        for a in range(2):
+            arm = self.arms[a]
+            mask = (1 << arm.m) - 1
+            if M == 0:
+                mask &= ~0b1100          # no hand candidate: hand rows unused
+            arm.update(self.meas[a], mask=mask, frame=frame)
+            arm.getEstimator(self.est[a])
+        return self.est

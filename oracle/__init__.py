@@ -340,3 +340,75 @@ def bpf_run_tracks(batch, track_ids, nthreads=0):
 
 def num_threads():
     return lib().mko_num_threads()
+
+
+# ---------------------------------------------------------------- config 0: PFTracker flow
+def scene_roi(heads_a):
+    """ROI (x_offset, y_offset, width, height) from an arm's head list (cx, cy, w)."""
+    cx, cy, w = heads_a[0]
+    return np.array([cx - w / 2.0, cy - w / 2.0, w, w])
+
+
+def rbpf_model_from_arm(arm, cam=(525.0, 525.0, 319.5, 239.5)):
+    return RbpfModel(arm["d"], arm["m"], arm["K"], arm["F"], arm["B"], arm["Q"], arm["R"], arm["weight"],
+                     Bm=arm["Bm"], mm=arm["mm"], cam=cam)
+
+
+def project_joint(arm, x, joint, cam=(525.0, 525.0, 319.5, 239.5)):
+    p = arm["Bm"][joint] @ x + arm["mm"][joint]
+    return np.array([cam[0] * p[0] / p[2] + cam[2], cam[1] * p[1] / p[2] + cam[3]])
+
+
+def pose_tracker_run(scene, N, seed, T=None, Pa=0.05, clutter=1e-4, hand_joint=1, alias=False):
+    """CPU restatement of PFTracker's frame loop (pfPose.cpp:210-385) on the
+    config-0 scene: per frame, PDAF association of the pooled hand detections
+    to each arm (pfPose.cpp:247-301), the per-particle measurement columns
+    (303-323), both arms' ParticleFilter::update (325-326) and getEstimator
+    (347-348).  A frame without a head ROI for either arm is skipped
+    (370-378).  Draws follow the library's Philox conventions."""
+    T = len(scene.frames) if T is None else T
+    arms = scene.arms
+    models = [rbpf_model_from_arm(a) for a in arms]
+    d = arms[0]["d"]
+    xs, Ps, prev = [], [], [None, None]
+    for a in range(2):
+        U0 = int(draw_block(seed, a, 0xFFFFFFFF, 0xFFFFFFFF, 0x102)[0])
+        bins, _ = resample(arms[a]["weight"], N, U0)
+        xs.append(arms[a]["mu"][bins].copy())
+        Ps.append(arms[a]["Sigma"][bins].copy())
+    est = np.full((2, T, d), np.nan)
+    skipped = np.zeros(T, bool)
+    for t in range(T):
+        fr = scene.frames[t]
+        if any(len(fr["heads"][a]) == 0 for a in range(2)):
+            skipped[t] = True
+            continue
+        rois = [scene_roi(fr["heads"][a]) for a in range(2)]
+        ests = [xs[a].mean(0) for a in range(2)]
+        hats = [project_joint(arms[a], ests[a], hand_joint) for a in range(2)]
+        hands = fr["hands"]
+        M = len(hands)
+        for a in range(2):
+            o = 1 - a
+            r = rois[a]
+            head = (r[0] + r[2] / 2.0, r[1] + 0.5 * r[3])
+            z = np.zeros((N, arms[a]["m"]))
+            z[:, 0], z[:, 1] = head
+            mask = (1 << arms[a]["m"]) - 1
+            if M:
+                w = pdaf_weights(hands, hats[a], hats[o], 0.8 * r[2], Pa, clutter)
+                wn = w / w.sum()
+                U = int(draw_block(seed, a, t, 0xFFFFFFFF, 0x103)[0])
+                bins, _ = resample(wn, N, U)
+                z[:, 2:4] = hands[bins]
+            else:
+                mask &= ~0b1100
+            Ui = int(draw_block(seed, a, t, 0xFFFFFFFF, 0x102)[0])
+            Ua = int(draw_block(seed, a, t, 0xFFFFFFFF, 0x100)[0])
+            out = models[a].update(xs[a], Ps[a], z, Ui, Ua, mask=mask,
+                                   alias_prev_anc=prev[a] if alias else None)
+            xs[a], Ps[a] = out["x"], out["P"]
+            prev[a] = out["anc"]
+        for a in range(2):
+            est[a, t] = xs[a].mean(0)
+    return est, skipped
