@@ -242,6 +242,55 @@ int mkf_pdaf_associate(mkf_rbpf_t arm0, mkf_rbpf_t arm1, uint32_t frame, const d
                        const double* d_cand, int M, double Pa, double clutter, double* d_meas0,
                        double* d_meas1, int* d_bins0, int* d_bins1, mkf_stream_t stream);
 
+/* ------------------------------------------- A11 mixture KF forward / adjoint */
+/* Deterministic counterpart of ParticleFilter::update (pf2DRao.cpp:125-158):
+ * per frame every component k predicts from the collapsed posterior
+ * (x = a_k*x + (1-a_k)*mu_k, P = A_k P A_k + Lq_k Lq_k^T; my_gmm.cpp:53-58,
+ * KF_model.cpp:11-15), runs sequential PDAF/EKF updates over the measured
+ * joints (Bar-Shalom combined innovation; PDA weights as pfPose.cpp:247-298)
+ * giving l_k = sum_j log[(1-P_D) kappa + P_D sum_i N(z_i; zhat, S)]; then
+ * c_t = log sum_k pi_k exp(l_k), w_k = pi_k exp(l_k - c_t), moment-matched
+ * collapse and symmetrisation of P.  logL = sum_t c_t (FP32 math, FP64 sums).
+ * theta (flat, FP64) = [mu (K*d), a (K*d), Lq packed lower (K*d(d+1)/2), sigma];
+ * pi and the prior covariances S0 are fixed.  The backward pass is a
+ * hand-written reverse sweep with sqrt(T) checkpointing: the forward stores
+ * the collapsed state every ceil(sqrt(T)) frames; the backward recomputes
+ * each segment from its checkpoint and reverses it frame by frame.
+ * Gradients are reduced across tracks in a fixed order (deterministic). */
+typedef struct mkf_mixkf* mkf_mixkf_t;
+typedef struct mkf_mix_model {
+  int d, K, J;
+  const double* pi;    /* K */
+  const double* S0;    /* K*d*d */
+  double fx, fy, cx, cy;
+} mkf_mix_model;
+/* tracks: n_frames, frame_base (global frame index), their bodies Bm
+ * (n_tracks*J*3*d), mm (n_tracks*J*3), P_D and kappa; all host pointers.
+ * d in {12, 24}, K <= 32, J <= 4. */
+int mkf_mixkf_create(const mkf_mix_model* model, int n_tracks, const int* n_frames,
+                     const int64_t* frame_base, const double* Bm, const double* mm,
+                     const double* p_detect, const double* kappa, int64_t n_frames_total,
+                     mkf_mixkf_t* out);
+/* theta: host (mkf_mixkf_set_theta) or device (mkf_mixkf_set_theta_device) */
+int mkf_mixkf_set_theta(mkf_mixkf_t h, const double* theta);
+int mkf_mixkf_set_theta_device(mkf_mixkf_t h, const double* d_theta, mkf_stream_t stream);
+int mkf_mixkf_theta_size(mkf_mixkf_t h);
+/* forward: per-track logL (optional, n_tracks doubles) and the total (1 double),
+ * device pointers; stores the checkpoints the backward pass needs */
+int mkf_mixkf_forward(mkf_mixkf_t h, const int* d_det_off, const float* d_det, double* d_loglik,
+                      double* d_total, mkf_stream_t stream);
+/* backward: d logL_total / d theta into d_grad (theta-sized, device) */
+int mkf_mixkf_backward(mkf_mixkf_t h, const int* d_det_off, const float* d_det, double* d_grad,
+                       mkf_stream_t stream);
+int mkf_mixkf_status(mkf_mixkf_t h, int* status);
+int mkf_mixkf_destroy(mkf_mixkf_t h);
+/* one Adam step on device (maximising when maximize != 0):
+ * m = b1 m + (1-b1) g; v = b2 v + (1-b2) g^2; theta +/-= lr mhat/(sqrt(vhat)+eps).
+ * Entries with mask[i] == 0 (optional) are left unchanged. */
+int mkf_adam_step(double* d_theta, const double* d_grad, double* d_m, double* d_v, const uint8_t* d_mask,
+                  int n, int step, double lr, double b1, double b2, double eps, int maximize,
+                  mkf_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

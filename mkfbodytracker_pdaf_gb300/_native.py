@@ -35,6 +35,11 @@ class BpfModels(C.Structure):
                 ("fx", F), ("fy", F), ("cx", F), ("cy", F)]
 
 
+class MixModelDesc(C.Structure):
+    _fields_ = [("d", I), ("K", I), ("J", I), ("pi", P), ("S0", P),
+                ("fx", C.c_double), ("fy", C.c_double), ("cx", C.c_double), ("cy", C.c_double)]
+
+
 class BpfTrack(C.Structure):
     _fields_ = [("n_particles", C.c_int32), ("n_frames", C.c_int32), ("frame_base", C.c_int64),
                 ("seed", C.c_uint64), ("track_id", C.c_uint32), ("model_index", C.c_int32),
@@ -76,6 +81,15 @@ SIGNATURES = {
     "mkf_rbpf_status": (I, [P, C.POINTER(I)]),
     "mkf_rbpf_destroy": (I, [P]),
     "mkf_pdaf_associate": (I, [P, P, U32, P, P, I, C.c_double, C.c_double, P, P, P, P, P]),
+    "mkf_mixkf_create": (I, [C.POINTER(MixModelDesc), I, P, P, P, P, P, P, I64, C.POINTER(P)]),
+    "mkf_mixkf_set_theta": (I, [P, P]),
+    "mkf_mixkf_set_theta_device": (I, [P, P, P]),
+    "mkf_mixkf_theta_size": (I, [P]),
+    "mkf_mixkf_forward": (I, [P, P, P, P, P, P]),
+    "mkf_mixkf_backward": (I, [P, P, P, P, P]),
+    "mkf_mixkf_status": (I, [P, C.POINTER(I)]),
+    "mkf_mixkf_destroy": (I, [P]),
+    "mkf_adam_step": (I, [P, P, P, P, P, I, I, C.c_double, C.c_double, C.c_double, C.c_double, I, P]),
 }
 
 _lib = None

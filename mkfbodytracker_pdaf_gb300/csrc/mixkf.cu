@@ -1,0 +1,937 @@
+// mixkf.cu -- mixture Kalman filter (GPB1 over the GMM components) with PDAF
+// association, its log marginal likelihood, and the hand-written adjoint with
+// sqrt(T) checkpointing.
+//
+// Reference pieces: KF_model::predict/update (KF_model.cpp:11-25), the motion
+// model of my_gmm::loadGaussian (my_gmm.cpp:45-75) generalised to
+// A_k = diag(a_k), Q_k = Lq_k Lq_k^T, the mixture over components that
+// pf2DRao redraws every frame (pf2DRao.cpp:128), and the PDA association
+// weights of pfPose.cpp:247-298.
+//
+// Launch shape: one CTA per track (static round-robin over a persistent grid,
+// so every reduction has a fixed order), one warp per mixture component.  A
+// warp's predict/update/reverse runs lane-parallel over matrix entries; the
+// collapse and its reverse are CTA-wide.  Per-warp buffers (joint records,
+// component outputs, adjoints) live in the CTA's global scratch slot (L1/L2
+// resident); the collapsed state and its adjoint live in shared memory.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "mkf_common.cuh"
+
+namespace mkf {
+
+constexpr int kMixMaxC = MKF_MAX_DET;
+constexpr float kMixZMin = 0.05f;
+
+// joint record layout (floats)
+enum {
+  R_VIS = 0, R_N = 1, R_P3 = 2, R_IZ = 5, R_ZH = 6, R_JP = 8, R_S = 14, R_SI = 18, R_LD = 22,
+  R_ELL = 23, R_B0 = 24, R_NB = 25, R_M = 27, R_NU = 31, R_E = 63, R_BETA = 79, R_H = 95
+};
+__host__ __device__ inline int rec_size(int d) { return (R_H + 9 * d + d * d + 3) & ~3; }
+__host__ __device__ inline int rec_U(int d) { return R_H + 2 * d; }
+__host__ __device__ inline int rec_Kg(int d) { return R_H + 4 * d; }
+__host__ __device__ inline int rec_W(int d) { return R_H + 6 * d; }
+__host__ __device__ inline int rec_X(int d) { return R_H + 8 * d; }
+__host__ __device__ inline int rec_Pin(int d) { return R_H + 9 * d; }
+
+struct CompLayout {   // per-component block inside a CTA slot (floats)
+  int rec0, xk, Pk, xb, Pb, Xin, Pin, Dkb, tmp, gmu, ga, gL, size;
+};
+__host__ __device__ inline CompLayout comp_layout(int d, int J) {
+  CompLayout L;
+  int o = 0;
+  L.rec0 = o; o += J * rec_size(d);
+  L.xk = o; o += d; L.Pk = o; o += d * d;
+  L.xb = o; o += d; L.Pb = o; o += d * d;
+  L.Xin = o; o += d; L.Pin = o; o += d * d;
+  L.Dkb = o; o += d;
+  L.tmp = o; o += 8 * d;
+  L.gmu = o; o += d; L.ga = o; o += d; L.gL = o; o += d * (d + 1) / 2;
+  L.size = (o + 3) & ~3;
+  return L;
+}
+
+struct MixDev {
+  int d, K, J, DD;
+  const float *mu, *a, *Lq, *Q, *logpi, *pi, *S0;
+  float sigma, fx, fy, cx, cy;
+};
+
+struct MixArgs {
+  MixDev M;
+  int n_tracks, C;
+  const int* n_frames;
+  const long long* frame_base;
+  const float* Bm;
+  const float* mm;
+  const float* pd;
+  const float* kappa;
+  const int* det_off;
+  const float2* det;
+  const long long* ck_off;     // per track offset (floats) into ck
+  float* ck;
+  double* ll;                  // per track logL
+  float* slots;                // gridDim.x * slot_floats
+  long long slot_floats;
+  double* gacc;                // gridDim.x * ng (backward)
+  int ng;
+  int* status;
+};
+
+__device__ __forceinline__ float wsum(float v) { return warp_sum(v); }
+
+// ---------------------------------------------------------------- forward pieces
+// sequential PDAF/EKF update of one joint for one component (whole warp)
+__device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const float* Bj, const float* mj,
+                           int n, const float2* z, float pd, float kappa, bool rec, int lane) {
+  const int d = M.d;
+  float* H = R + R_H;
+  float* U = R + rec_U(d);
+  float* Kg = R + rec_Kg(d);
+  float* W = R + rec_W(d);
+  if (rec) {
+    float* Rx = R + rec_X(d);
+    float* RP = R + rec_Pin(d);
+    for (int i = lane; i < d; i += 32) Rx[i] = x[i];
+    for (int i = lane; i < d * d; i += 32) RP[i] = P[i];
+  }
+  float pt = 0.0f;
+  if (lane < 3) {
+    pt = mj[lane];
+    for (int c = 0; c < d; ++c) pt = fmaf(Bj[lane * d + c], x[c], pt);
+  }
+  const float p0 = __shfl_sync(0xffffffffu, pt, 0), p1 = __shfl_sync(0xffffffffu, pt, 1),
+              p2 = __shfl_sync(0xffffffffu, pt, 2);
+  if (!(p2 > kMixZMin)) {
+    if (rec && lane == 0) R[R_VIS] = 0.0f;
+    __syncwarp();
+    return logf(kappa);
+  }
+  const float iz = 1.0f / p2;
+  const float zh0 = M.fx * p0 * iz + M.cx, zh1 = M.fy * p1 * iz + M.cy;
+  const float J00 = M.fx * iz, J02 = -M.fx * p0 * iz * iz, J11 = M.fy * iz, J12 = -M.fy * p1 * iz * iz;
+  for (int i = lane; i < 2 * d; i += 32) {
+    const int a = i / d, c = i - a * d;
+    H[i] = (a == 0) ? fmaf(J00, Bj[c], J02 * Bj[2 * d + c]) : fmaf(J11, Bj[d + c], J12 * Bj[2 * d + c]);
+  }
+  __syncwarp();
+  for (int i = lane; i < 2 * d; i += 32) {
+    const int r = i >> 1, a = i & 1;
+    float s = 0.0f;
+    for (int c = 0; c < d; ++c) s = fmaf(P[r * d + c], H[a * d + c], s);
+    U[i] = s;
+  }
+  __syncwarp();
+  float sv = 0.0f;
+  if (lane < 4) {
+    const int a = lane >> 1, b = lane & 1;
+    for (int r = 0; r < d; ++r) sv = fmaf(H[a * d + r], U[r * 2 + b], sv);
+    if (a == b) sv += M.sigma * M.sigma;
+  }
+  const float S00 = __shfl_sync(0xffffffffu, sv, 0), S01 = __shfl_sync(0xffffffffu, sv, 1),
+              S10 = __shfl_sync(0xffffffffu, sv, 2), S11 = __shfl_sync(0xffffffffu, sv, 3);
+  const float det = S00 * S11 - S01 * S10;
+  const float Si00 = S11 / det, Si01 = -S01 / det, Si10 = -S10 / det, Si11 = S00 / det;
+  const float ld = logf(det);
+  const float c0 = pd * 0.15915494309189535f, b = (1.0f - pd) * kappa;
+  float e = 0.0f, n0 = 0.0f, n1 = 0.0f;
+  if (lane < n) {
+    n0 = z[lane].x - zh0;
+    n1 = z[lane].y - zh1;
+    const float q = n0 * (Si00 * n0 + Si01 * n1) + n1 * (Si10 * n0 + Si11 * n1);
+    e = c0 * expf(-0.5f * q - 0.5f * ld);
+  }
+  const float ell = b + wsum(e);
+  const float beta = e / ell, beta0 = b / ell;
+  const float nb0 = wsum(beta * n0), nb1 = wsum(beta * n1);
+  const float C00 = wsum(beta * n0 * n0) - nb0 * nb0;
+  const float C01 = wsum(beta * n0 * n1) - nb0 * nb1;
+  const float C11 = wsum(beta * n1 * n1) - nb1 * nb1;
+  const float M00 = (1.0f - beta0) * S00 - C00, M01 = (1.0f - beta0) * S01 - C01;
+  const float M10 = (1.0f - beta0) * S10 - C01, M11 = (1.0f - beta0) * S11 - C11;
+  for (int i = lane; i < 2 * d; i += 32) {
+    const int r = i >> 1, a = i & 1;
+    Kg[i] = U[r * 2] * (a ? Si01 : Si00) + U[r * 2 + 1] * (a ? Si11 : Si10);
+  }
+  __syncwarp();
+  for (int i = lane; i < 2 * d; i += 32) {
+    const int r = i >> 1, a = i & 1;
+    W[i] = Kg[r * 2] * (a ? M01 : M00) + Kg[r * 2 + 1] * (a ? M11 : M10);
+  }
+  __syncwarp();
+  if (lane < d) x[lane] += Kg[lane * 2] * nb0 + Kg[lane * 2 + 1] * nb1;
+  for (int i = lane; i < d * d; i += 32) {
+    const int r = i / d, c = i - r * d;
+    P[i] -= W[r * 2] * Kg[c * 2] + W[r * 2 + 1] * Kg[c * 2 + 1];
+  }
+  if (rec) {
+    if (lane == 0) {
+      R[R_VIS] = 1.0f; R[R_N] = (float)n;
+      R[R_P3] = p0; R[R_P3 + 1] = p1; R[R_P3 + 2] = p2; R[R_IZ] = iz;
+      R[R_ZH] = zh0; R[R_ZH + 1] = zh1;
+      R[R_JP] = J00; R[R_JP + 1] = 0.0f; R[R_JP + 2] = J02; R[R_JP + 3] = 0.0f; R[R_JP + 4] = J11; R[R_JP + 5] = J12;
+      R[R_S] = S00; R[R_S + 1] = S01; R[R_S + 2] = S10; R[R_S + 3] = S11;
+      R[R_SI] = Si00; R[R_SI + 1] = Si01; R[R_SI + 2] = Si10; R[R_SI + 3] = Si11;
+      R[R_LD] = ld; R[R_ELL] = ell; R[R_B0] = beta0; R[R_NB] = nb0; R[R_NB + 1] = nb1;
+      R[R_M] = M00; R[R_M + 1] = M01; R[R_M + 2] = M10; R[R_M + 3] = M11;
+    }
+    if (lane < kMixMaxC) {
+      R[R_NU + 2 * lane] = n0; R[R_NU + 2 * lane + 1] = n1;
+      R[R_E + lane] = e; R[R_BETA + lane] = beta;
+    }
+  }
+  __syncwarp();
+  return logf(ell);
+}
+
+// ---------------------------------------------------------------- reverse pieces
+__device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, float pd, float kappa, float* xb,
+                          float* Pb, float gl, float* tmp, float& sb, int lane) {
+  if (R[R_VIS] == 0.0f) return;
+  const int d = M.d;
+  const int n = (int)R[R_N];
+  const float* H = R + R_H;
+  const float* U = R + rec_U(d);
+  const float* Kg = R + rec_Kg(d);
+  const float* W = R + rec_W(d);
+  const float* Pin = R + rec_Pin(d);
+  float* Kgb = tmp;
+  float* Wb = tmp + 2 * d;
+  float* Ub = tmp + 4 * d;
+  float* Hb = tmp + 6 * d;
+  const float nb0 = R[R_NB], nb1 = R[R_NB + 1];
+  const float S[4] = {R[R_S], R[R_S + 1], R[R_S + 2], R[R_S + 3]};
+  const float Si[4] = {R[R_SI], R[R_SI + 1], R[R_SI + 2], R[R_SI + 3]};
+  const float Mm[4] = {R[R_M], R[R_M + 1], R[R_M + 2], R[R_M + 3]};
+  const float beta0 = R[R_B0], ell = R[R_ELL];
+  const float b = (1.0f - pd) * kappa;
+  // x' = x + Kg nb
+  float t0 = 0.0f, t1 = 0.0f;
+  if (lane < d) { t0 = Kg[lane * 2] * xb[lane]; t1 = Kg[lane * 2 + 1] * xb[lane]; }
+  float nbb0 = wsum(t0), nbb1 = wsum(t1);
+  // P' = P - W Kg^T
+  for (int i = lane; i < 2 * d; i += 32) {
+    const int r = i >> 1, a = i & 1;
+    float s = 0.0f, t = 0.0f;
+    for (int c = 0; c < d; ++c) {
+      s = fmaf(Pb[r * d + c], Kg[c * 2 + a], s);
+      t = fmaf(Pb[c * d + r], W[c * 2 + a], t);
+    }
+    Wb[i] = -s;
+    Kgb[i] = xb[r] * (a ? nb1 : nb0) - t;
+  }
+  __syncwarp();
+  // W = Kg M
+  float m00 = 0.0f, m01 = 0.0f, m10 = 0.0f, m11 = 0.0f;
+  if (lane < d) {
+    m00 = Kg[lane * 2] * Wb[lane * 2]; m01 = Kg[lane * 2] * Wb[lane * 2 + 1];
+    m10 = Kg[lane * 2 + 1] * Wb[lane * 2]; m11 = Kg[lane * 2 + 1] * Wb[lane * 2 + 1];
+  }
+  const float Mb[4] = {wsum(m00), wsum(m01), wsum(m10), wsum(m11)};
+  for (int i = lane; i < 2 * d; i += 32) {
+    const int r = i >> 1, a = i & 1;
+    Kgb[i] += Wb[r * 2] * Mm[a * 2] + Wb[r * 2 + 1] * Mm[a * 2 + 1];
+  }
+  // M = (1 - beta0) S - Cn
+  float Sb[4], Cnb[4];
+  float b0b = 0.0f;
+  for (int q = 0; q < 4; ++q) { Sb[q] = (1.0f - beta0) * Mb[q]; b0b -= Mb[q] * S[q]; Cnb[q] = -Mb[q]; }
+  const float Cs0 = 2.0f * Cnb[0], Cs1 = Cnb[1] + Cnb[2], Cs3 = 2.0f * Cnb[3];
+  float n0 = 0.0f, n1 = 0.0f, be = 0.0f, ee = 0.0f, betab = 0.0f, nub0 = 0.0f, nub1 = 0.0f;
+  if (lane < n) {
+    n0 = R[R_NU + 2 * lane]; n1 = R[R_NU + 2 * lane + 1]; be = R[R_BETA + lane]; ee = R[R_E + lane];
+    betab = n0 * (Cnb[0] * n0 + Cnb[1] * n1) + n1 * (Cnb[2] * n0 + Cnb[3] * n1);
+    nub0 = be * (Cs0 * n0 + Cs1 * n1);
+    nub1 = be * (Cs1 * n0 + Cs3 * n1);
+  }
+  nbb0 -= Cs0 * nb0 + Cs1 * nb1;
+  nbb1 -= Cs1 * nb0 + Cs3 * nb1;
+  __syncwarp();
+  // Kg = U Si
+  for (int i = lane; i < 2 * d; i += 32) {
+    const int r = i >> 1, a = i & 1;
+    Ub[i] = Kgb[r * 2] * Si[a * 2] + Kgb[r * 2 + 1] * Si[a * 2 + 1];
+  }
+  float s00 = 0.0f, s01 = 0.0f, s10 = 0.0f, s11 = 0.0f;
+  if (lane < d) {
+    s00 = U[lane * 2] * Kgb[lane * 2]; s01 = U[lane * 2] * Kgb[lane * 2 + 1];
+    s10 = U[lane * 2 + 1] * Kgb[lane * 2]; s11 = U[lane * 2 + 1] * Kgb[lane * 2 + 1];
+  }
+  float Sib[4] = {wsum(s00), wsum(s01), wsum(s10), wsum(s11)};
+  // nb = sum beta nu
+  if (lane < n) {
+    betab += n0 * nbb0 + n1 * nbb1;
+    nub0 += be * nbb0;
+    nub1 += be * nbb1;
+  }
+  // beta = e / ell, beta0 = b / ell, log ell
+  const float num = b0b * b + wsum(betab * ee);
+  const float ellb = -num / (ell * ell) + gl / ell;
+  float ldp = 0.0f, q00 = 0.0f, q01 = 0.0f, q11 = 0.0f;
+  if (lane < n) {
+    const float eb = betab / ell + ellb;
+    const float qb = -0.5f * ee * eb;
+    ldp = qb;
+    nub0 += qb * (2.0f * Si[0] * n0 + (Si[1] + Si[2]) * n1);
+    nub1 += qb * ((Si[2] + Si[1]) * n0 + 2.0f * Si[3] * n1);
+    q00 = qb * n0 * n0; q01 = qb * n0 * n1; q11 = qb * n1 * n1;
+  }
+  const float ldb = wsum(ldp);
+  Sib[0] += wsum(q00);
+  const float q01s = wsum(q01);
+  Sib[1] += q01s; Sib[2] += q01s;
+  Sib[3] += wsum(q11);
+  const float zhb0 = -wsum(nub0), zhb1 = -wsum(nub1);
+  // ld = log det S ; Si = S^-1
+  Sb[0] += ldb * Si[0]; Sb[1] += ldb * Si[2]; Sb[2] += ldb * Si[1]; Sb[3] += ldb * Si[3];
+  {
+    float T1[4];
+    for (int a = 0; a < 2; ++a)
+      for (int c = 0; c < 2; ++c) T1[a * 2 + c] = Si[a] * Sib[c] + Si[2 + a] * Sib[2 + c];
+    for (int a = 0; a < 2; ++a)
+      for (int c = 0; c < 2; ++c) Sb[a * 2 + c] -= T1[a * 2] * Si[c * 2] + T1[a * 2 + 1] * Si[c * 2 + 1];
+  }
+  if (lane == 0) sb += 2.0f * M.sigma * (Sb[0] + Sb[3]);
+  __syncwarp();
+  // S = H U + sigma^2 I
+  for (int i = lane; i < 2 * d; i += 32) {
+    const int a = i / d, r = i - a * d;
+    Hb[i] = Sb[a * 2] * U[r * 2] + Sb[a * 2 + 1] * U[r * 2 + 1];
+  }
+  for (int i = lane; i < 2 * d; i += 32) {
+    const int r = i >> 1, c = i & 1;
+    Ub[i] += H[r] * Sb[c] + H[d + r] * Sb[2 + c];
+  }
+  __syncwarp();
+  // U = P H^T
+  for (int i = lane; i < d * d; i += 32) {
+    const int r = i / d, c = i - r * d;
+    Pb[i] += Ub[r * 2] * H[c] + Ub[r * 2 + 1] * H[d + c];
+  }
+  for (int i = lane; i < 2 * d; i += 32) {
+    const int a = i / d, c = i - a * d;
+    float s = 0.0f;
+    for (int r = 0; r < d; ++r) s = fmaf(Ub[r * 2 + a], Pin[r * d + c], s);
+    Hb[i] += s;
+  }
+  __syncwarp();
+  // H = Jp Bj
+  float jb = 0.0f;
+  if (lane < 6) {
+    const int a = lane / 3, t = lane - a * 3;
+    for (int c = 0; c < d; ++c) jb = fmaf(Hb[a * d + c], Bj[t * d + c], jb);
+  }
+  float Jb[6];
+  for (int q = 0; q < 6; ++q) Jb[q] = __shfl_sync(0xffffffffu, jb, q);
+  const float iz = R[R_IZ], iz2 = iz * iz, iz3 = iz2 * iz;
+  const float J00 = R[R_JP], J02 = R[R_JP + 2], J11 = R[R_JP + 4], J12 = R[R_JP + 5];
+  const float p0 = R[R_P3], p1 = R[R_P3 + 1];
+  const float pb0 = J00 * zhb0 + Jb[2] * (-M.fx * iz2);
+  const float pb1 = J11 * zhb1 + Jb[5] * (-M.fy * iz2);
+  const float pb2 = J02 * zhb0 + J12 * zhb1 + Jb[0] * (-M.fx * iz2) + Jb[2] * (2.0f * M.fx * p0 * iz3) +
+                    Jb[4] * (-M.fy * iz2) + Jb[5] * (2.0f * M.fy * p1 * iz3);
+  if (lane < d) xb[lane] += Bj[lane] * pb0 + Bj[d + lane] * pb1 + Bj[2 * d + lane] * pb2;
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------- CTA-wide frame pieces
+struct Smem {
+  float *xh, *Ph, *xo, *Po, *Xb, *Pb, *Pcb, *xt;
+  float2* det;
+  int* cnt;
+  float *w, *l, *wb, *red;
+  double* dred;
+};
+
+__device__ void load_frame_dets(const MixArgs& A, long long g, Smem& s, int tid, int TB) {
+  const int J = A.M.J;
+  if (tid < J) {
+    int n = A.det_off[g * J + tid + 1] - A.det_off[g * J + tid];
+    if (n > kMixMaxC) { n = kMixMaxC; atomicOr(A.status, MKF_ST_TRUNC); }
+    s.cnt[tid] = n < 0 ? 0 : n;
+  }
+  __syncthreads();
+  for (int q = tid; q < J * kMixMaxC; q += TB) {
+    const int j = q / kMixMaxC, i = q - j * kMixMaxC;
+    if (i < s.cnt[j]) s.det[j * kMixMaxC + i] = A.det[A.det_off[g * J + j] + i];
+  }
+  __syncthreads();
+}
+
+// one frame forward (all warps); returns c_t (valid in every thread)
+__device__ float frame_forward(const MixArgs& A, float* slot, const CompLayout& CL, const float* Bm,
+                               const float* mm, float pd, float kappa, Smem& s, bool rec) {
+  const MixDev& M = A.M;
+  const int d = M.d, K = M.K, J = M.J;
+  const int tid = threadIdx.x, TB = blockDim.x, lane = tid & 31, k = tid >> 5;
+  float* cb = slot + (size_t)k * CL.size;
+  float* xk = cb + CL.xk;
+  float* Pk = cb + CL.Pk;
+  const float* a = M.a + k * d;
+  const float* mu = M.mu + k * d;
+  if (lane < d) xk[lane] = fmaf(a[lane], s.xh[lane], (1.0f - a[lane]) * mu[lane]);
+  const float* Qk = M.Q + (size_t)k * d * d;
+  for (int i = lane; i < d * d; i += 32) {
+    const int r = i / d, c = i - r * d;
+    Pk[i] = fmaf(a[r] * a[c], s.Ph[i], Qk[i]);
+  }
+  __syncwarp();
+  float ll = 0.0f;
+  for (int j = 0; j < J; ++j)
+    ll += joint_fwd(M, cb + CL.rec0 + j * rec_size(d), xk, Pk, Bm + j * 3 * d, mm + j * 3, s.cnt[j],
+                    s.det + j * kMixMaxC, pd, kappa, rec, lane);
+  if (lane == 0) s.l[k] = M.logpi[k] + ll;
+  __syncthreads();
+  if (k == 0) {
+    const float v = lane < K ? s.l[lane] : -INFINITY;
+    const float mx = warp_max(v);
+    const float sum = warp_sum(lane < K ? expf(v - mx) : 0.0f);
+    const float c = mx + logf(sum);
+    if (lane < K) s.w[lane] = expf(v - c);
+    if (lane == 0) s.red[0] = c;
+  }
+  __syncthreads();
+  for (int r = tid; r < d; r += TB) {
+    float v = 0.0f;
+    for (int q = 0; q < K; ++q) v = fmaf(s.w[q], slot[(size_t)q * CL.size + CL.xk + r], v);
+    s.xo[r] = v;
+  }
+  __syncthreads();
+  for (int i = tid; i < d * d; i += TB) {
+    const int r = i / d, c = i - r * d;
+    if (r > c) continue;
+    float v = 0.0f;
+    for (int q = 0; q < K; ++q) {
+      const float* bq = slot + (size_t)q * CL.size;
+      const float Dr = bq[CL.xk + r] - s.xo[r], Dc = bq[CL.xk + c] - s.xo[c];
+      v = fmaf(s.w[q], 0.5f * (bq[CL.Pk + i] + bq[CL.Pk + c * d + r]) + Dr * Dc, v);
+    }
+    s.Po[i] = v;
+    s.Po[c * d + r] = v;
+  }
+  __syncthreads();
+  return s.red[0];
+}
+
+__device__ void prior_state(const MixDev& M, Smem& s, int tid, int TB) {
+  const int d = M.d, K = M.K;
+  for (int r = tid; r < d; r += TB) {
+    float v = 0.0f;
+    for (int k = 0; k < K; ++k) v = fmaf(M.pi[k], M.mu[k * d + r], v);
+    s.xh[r] = v;
+  }
+  __syncthreads();
+  for (int i = tid; i < d * d; i += TB) {
+    const int r = i / d, c = i - r * d;
+    float v = 0.0f;
+    for (int k = 0; k < K; ++k)
+      v = fmaf(M.pi[k], M.S0[(size_t)k * d * d + i] + (M.mu[k * d + r] - s.xh[r]) * (M.mu[k * d + c] - s.xh[c]), v);
+    s.Ph[i] = v;
+  }
+  __syncthreads();
+}
+
+__device__ void carve(Smem& s, float* base, int d) {
+  float* p = base;
+  s.xh = p; p += d; s.Ph = p; p += d * d;
+  s.xo = p; p += d; s.Po = p; p += d * d;
+  s.Xb = p; p += d; s.Pb = p; p += d * d;
+  s.Pcb = p; p += d * d;
+  s.xt = p; p += d;
+  p = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(p) + 7) & ~uintptr_t(7));
+  s.det = reinterpret_cast<float2*>(p); p += 2 * kMixMaxC * MKF_MAX_J;
+  s.cnt = reinterpret_cast<int*>(p); p += 8;
+  s.w = p; p += 32; s.l = p; p += 32; s.wb = p; p += 32;
+  s.red = p; p += 64;
+  p = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(p) + 7) & ~uintptr_t(7));
+  s.dred = reinterpret_cast<double*>(p);
+}
+
+size_t mix_smem_bytes(int d) {
+  return sizeof(float) * (size_t)(4 * d + 4 * d * d + d + 2 * kMixMaxC * MKF_MAX_J + 8 + 32 * 3 + 64 + 8) +
+         sizeof(double) * 40 + 64;
+}
+
+// ---------------------------------------------------------------- forward kernel
+__global__ void __launch_bounds__(1024) mix_forward_kernel(MixArgs A) {
+  extern __shared__ __align__(16) float msm[];
+  Smem s;
+  carve(s, msm, A.M.d);
+  const int d = A.M.d, J = A.M.J;
+  const int tid = threadIdx.x, TB = blockDim.x;
+  const CompLayout CL = comp_layout(d, J);
+  float* slot = A.slots + (size_t)blockIdx.x * A.slot_floats;
+  for (int b = blockIdx.x; b < A.n_tracks; b += gridDim.x) {
+    const int T = A.n_frames[b];
+    const long long g0 = A.frame_base[b];
+    const float* Bm = A.Bm + (size_t)b * J * 3 * d;
+    const float* mm = A.mm + (size_t)b * J * 3;
+    const float pd = A.pd[b], kappa = A.kappa[b];
+    float* ck = A.ck + A.ck_off[b];
+    prior_state(A.M, s, tid, TB);
+    double L = 0.0;
+    for (int t = 0; t < T; ++t) {
+      if (t % A.C == 0) {
+        float* c = ck + (size_t)(t / A.C) * (d + d * d);
+        for (int i = tid; i < d; i += TB) c[i] = s.xh[i];
+        for (int i = tid; i < d * d; i += TB) c[d + i] = s.Ph[i];
+      }
+      load_frame_dets(A, g0 + t, s, tid, TB);
+      L += (double)frame_forward(A, slot, CL, Bm, mm, pd, kappa, s, false);
+      for (int i = tid; i < d; i += TB) s.xh[i] = s.xo[i];
+      for (int i = tid; i < d * d; i += TB) s.Ph[i] = s.Po[i];
+      __syncthreads();
+    }
+    if (tid == 0) A.ll[b] = L;
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------- backward kernel
+__global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
+  extern __shared__ __align__(16) float msm[];
+  Smem s;
+  carve(s, msm, A.M.d);
+  const MixDev& M = A.M;
+  const int d = M.d, J = M.J, K = M.K, DD = M.DD;
+  const int tid = threadIdx.x, TB = blockDim.x, lane = tid & 31, k = tid >> 5;
+  const CompLayout CL = comp_layout(d, J);
+  float* slot = A.slots + (size_t)blockIdx.x * A.slot_floats;
+  float* seg = slot + (size_t)K * CL.size;                 // C states of d + d*d
+  double* gacc = A.gacc + (size_t)blockIdx.x * A.ng;       // mu, a, Lq, sigma
+  float* cb = slot + (size_t)k * CL.size;
+  const float* a = M.a + k * d;
+  const float* mu = M.mu + k * d;
+  const float* Lk = M.Lq + k * DD;
+  float sbl = 0.0f;                                         // sigma adjoint, per lane
+  for (int i = lane; i < 2 * d + DD; i += 32) cb[CL.gmu + i] = 0.0f;
+  for (int b = blockIdx.x; b < A.n_tracks; b += gridDim.x) {
+    const int T = A.n_frames[b];
+    const long long g0 = A.frame_base[b];
+    const float* Bm = A.Bm + (size_t)b * J * 3 * d;
+    const float* mm = A.mm + (size_t)b * J * 3;
+    const float pd = A.pd[b], kappa = A.kappa[b];
+    const float* ck = A.ck + A.ck_off[b];
+    for (int i = tid; i < d; i += TB) s.Xb[i] = 0.0f;
+    for (int i = tid; i < d * d; i += TB) s.Pb[i] = 0.0f;
+    __syncthreads();
+    const int nck = (T + A.C - 1) / A.C;
+    for (int sg = nck - 1; sg >= 0; --sg) {
+      const int t0 = sg * A.C, t1 = min(T, t0 + A.C);
+      // recompute the segment's collapsed states from its checkpoint
+      const float* c0 = ck + (size_t)sg * (d + d * d);
+      for (int i = tid; i < d + d * d; i += TB) seg[i] = c0[i];
+      for (int i = tid; i < d; i += TB) s.xh[i] = c0[i];
+      for (int i = tid; i < d * d; i += TB) s.Ph[i] = c0[d + i];
+      __syncthreads();
+      for (int t = t0; t < t1 - 1; ++t) {
+        load_frame_dets(A, g0 + t, s, tid, TB);
+        frame_forward(A, slot, CL, Bm, mm, pd, kappa, s, false);
+        float* st = seg + (size_t)(t - t0 + 1) * (d + d * d);
+        for (int i = tid; i < d; i += TB) { s.xh[i] = s.xo[i]; st[i] = s.xo[i]; }
+        for (int i = tid; i < d * d; i += TB) { s.Ph[i] = s.Po[i]; st[d + i] = s.Po[i]; }
+        __syncthreads();
+      }
+      // reverse the segment
+      for (int t = t1 - 1; t >= t0; --t) {
+        const float* st = seg + (size_t)(t - t0) * (d + d * d);
+        for (int i = tid; i < d; i += TB) s.xh[i] = st[i];
+        for (int i = tid; i < d * d; i += TB) s.Ph[i] = st[d + i];
+        load_frame_dets(A, g0 + t, s, tid, TB);
+        frame_forward(A, slot, CL, Bm, mm, pd, kappa, s, true);
+        // collapse reverse: P' = sym(sum w (P_k + D D^T)), x' = sum w x_k, softmax (dc = 1)
+        for (int i = tid; i < d * d; i += TB) {
+          const int r = i / d, c = i - r * d;
+          s.Pcb[i] = 0.5f * (s.Pb[i] + s.Pb[c * d + r]);
+        }
+        __syncthreads();
+        const float wk = s.w[k];
+        float* xk = cb + CL.xk;
+        float* Pk = cb + CL.Pk;
+        float* Dkb = cb + CL.Dkb;
+        if (lane < d) {
+          float v = 0.0f;
+          for (int c = 0; c < d; ++c) v = fmaf(s.Pcb[lane * d + c], xk[c] - s.xo[c], v);
+          Dkb[lane] = 2.0f * wk * v;
+        }
+        __syncthreads();
+        for (int r = tid; r < d; r += TB) {
+          float v = s.Xb[r];
+          for (int q = 0; q < K; ++q) v -= slot[(size_t)q * CL.size + CL.Dkb + r];
+          s.xt[r] = v;
+        }
+        __syncthreads();
+        float wbp = (lane < d) ? xk[lane] * s.xt[lane] : 0.0f;
+        for (int i = lane; i < d * d; i += 32) {
+          const int r = i / d, c = i - r * d;
+          wbp = fmaf(s.Pcb[i], Pk[i] + (xk[r] - s.xo[r]) * (xk[c] - s.xo[c]), wbp);
+        }
+        const float wbk = wsum(wbp);
+        if (lane == 0) s.wb[k] = wbk;
+        __syncthreads();
+        if (k == 0) {
+          const float v = lane < K ? s.w[lane] * s.wb[lane] : 0.0f;
+          const float sw = wsum(v);
+          if (lane == 0) s.red[1] = sw;
+        }
+        __syncthreads();
+        const float lb = wk * (wbk - s.red[1]) + wk;
+        float* xb = cb + CL.xb;
+        float* Pb = cb + CL.Pb;
+        float* Xin = cb + CL.Xin;
+        float* Pin = cb + CL.Pin;
+        if (wk > 0.0f) {
+          if (lane < d) xb[lane] = Dkb[lane] + wk * s.xt[lane];
+          for (int i = lane; i < d * d; i += 32) Pb[i] = wk * s.Pcb[i];
+          __syncwarp();
+          for (int j = J - 1; j >= 0; --j)
+            joint_bwd(M, cb + CL.rec0 + j * rec_size(d), Bm + j * 3 * d, pd, kappa, xb, Pb, lb, cb + CL.tmp, sbl, lane);
+          // predict reverse: x = a*xh + (1-a)*mu ; P = A Ph A + Q
+          float* gmu = cb + CL.gmu;
+          float* ga = cb + CL.ga;
+          float* gL = cb + CL.gL;
+          if (lane < d) {
+            Xin[lane] = a[lane] * xb[lane];
+            gmu[lane] += (1.0f - a[lane]) * xb[lane];
+            float g = (s.xh[lane] - mu[lane]) * xb[lane];
+            for (int c = 0; c < d; ++c)
+              g += (Pb[lane * d + c] * s.Ph[lane * d + c] + Pb[c * d + lane] * s.Ph[c * d + lane]) * a[c];
+            ga[lane] += g;
+          }
+          for (int i = lane; i < d * d; i += 32) {
+            const int r = i / d, c = i - r * d;
+            Pin[i] = a[r] * a[c] * Pb[i];
+          }
+          for (int i = lane; i < DD; i += 32) {
+            int r = (int)((sqrtf(8.0f * i + 1.0f) - 1.0f) * 0.5f);
+            while (r * (r + 1) / 2 > i) --r;
+            while ((r + 1) * (r + 2) / 2 <= i) ++r;
+            const int c = i - r * (r + 1) / 2;
+            float g = 0.0f;
+            for (int t2 = c; t2 < d; ++t2) g = fmaf(Pb[r * d + t2] + Pb[t2 * d + r], Lk[t2 * (t2 + 1) / 2 + c], g);
+            gL[i] += g;
+          }
+        } else {
+          if (lane < d) Xin[lane] = 0.0f;
+          for (int i = lane; i < d * d; i += 32) Pin[i] = 0.0f;
+        }
+        __syncthreads();
+        for (int r = tid; r < d; r += TB) {
+          float v = 0.0f;
+          for (int q = 0; q < K; ++q) v += slot[(size_t)q * CL.size + CL.Xin + r];
+          s.Xb[r] = v;
+        }
+        for (int i = tid; i < d * d; i += TB) {
+          float v = 0.0f;
+          for (int q = 0; q < K; ++q) v += slot[(size_t)q * CL.size + CL.Pin + i];
+          s.Pb[i] = v;
+        }
+        __syncthreads();
+      }
+      // flush this segment's FP32 parameter adjoints into the CTA's FP64 accumulators
+      for (int i = lane; i < d; i += 32) {
+        gacc[k * d + i] += (double)cb[CL.gmu + i];
+        gacc[K * d + k * d + i] += (double)cb[CL.ga + i];
+      }
+      for (int i = lane; i < DD; i += 32) gacc[2 * K * d + k * DD + i] += (double)cb[CL.gL + i];
+      for (int i = lane; i < 2 * d + DD; i += 32) cb[CL.gmu + i] = 0.0f;
+      __syncthreads();
+    }
+    // prior: x = sum pi mu, P = sum pi (S0 + D D^T)
+    for (int r = tid; r < d; r += TB) {
+      float v = 0.0f;
+      for (int q = 0; q < K; ++q) v = fmaf(M.pi[q], M.mu[q * d + r], v);
+      s.xh[r] = v;
+    }
+    __syncthreads();
+    if (lane < d) {
+      float v = 0.0f;
+      for (int c = 0; c < d; ++c) v = fmaf(s.Pb[lane * d + c] + s.Pb[c * d + lane], mu[c] - s.xh[c], v);
+      cb[CL.Dkb + lane] = M.pi[k] * v;
+    }
+    __syncthreads();
+    for (int r = tid; r < d; r += TB) {
+      float v = s.Xb[r];
+      for (int q = 0; q < K; ++q) v -= slot[(size_t)q * CL.size + CL.Dkb + r];
+      s.xt[r] = v;
+    }
+    __syncthreads();
+    if (lane < d) gacc[k * d + lane] += (double)(cb[CL.Dkb + lane] + M.pi[k] * s.xt[lane]);
+    __syncthreads();
+  }
+  // sigma: per-warp lane 0 partials, fixed-order sum
+  if (lane == 0) s.dred[k] = (double)sbl;
+  __syncthreads();
+  if (tid == 0) {
+    double v = 0.0;
+    for (int q = 0; q < K; ++q) v += s.dred[q];
+    gacc[A.ng - 1] += v;
+  }
+}
+
+// fixed-order reduction of the per-CTA FP64 accumulators
+__global__ void mix_reduce_kernel(const double* gacc, int nslots, int ng, double* grad) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < ng; q += gridDim.x * blockDim.x) {
+    double v = 0.0;
+    for (int s = 0; s < nslots; ++s) v += gacc[(size_t)s * ng + q];
+    grad[q] = v;
+  }
+}
+
+__global__ void mix_total_kernel(const double* ll, int n, double* total) {
+  __shared__ double red[32];
+  double v = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) v += ll[i];
+  v = warp_sum_d(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[q];
+    *total = t;
+  }
+}
+
+// theta (FP64, flat) -> FP32 device parameters and Q = Lq Lq^T
+__global__ void mix_prepare_kernel(const double* theta, int d, int K, float* mu, float* a, float* Lq, float* Q,
+                                   float* sigma) {
+  const int DD = d * (d + 1) / 2;
+  const int n1 = K * d, n2 = 2 * K * d, n3 = n2 + K * DD;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n3 + 1 + K * d * d; i += gridDim.x * blockDim.x) {
+    if (i < n1) mu[i] = (float)theta[i];
+    else if (i < n2) a[i - n1] = (float)theta[i];
+    else if (i < n3) Lq[i - n2] = (float)theta[i];
+    else if (i == n3) *sigma = (float)theta[n3];
+    else {
+      const int q = i - n3 - 1, k = q / (d * d), rc = q - k * d * d, r = rc / d, c = rc - r * d;
+      const double* L = theta + n2 + (size_t)k * DD;
+      double v = 0.0;
+      for (int s2 = 0; s2 <= (r < c ? r : c); ++s2) v += L[r * (r + 1) / 2 + s2] * L[c * (c + 1) / 2 + s2];
+      Q[q] = (float)v;
+    }
+  }
+}
+
+__global__ void adam_kernel(double* th, const double* g, double* m, double* v, const uint8_t* mask, int n,
+                            double c1, double c2, double lr, double b1, double b2, double eps, double sgn) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (mask && !mask[i]) continue;
+    const double gi = g[i];
+    m[i] = b1 * m[i] + (1.0 - b1) * gi;
+    v[i] = b2 * v[i] + (1.0 - b2) * gi * gi;
+    th[i] += sgn * lr * (m[i] / c1) / (sqrt(v[i] / c2) + eps);
+  }
+}
+
+}  // namespace mkf
+
+using namespace mkf;
+
+struct mkf_mixkf {
+  int d, K, J, DD, n_tracks, C, ng, grid, tpb;
+  long long G;
+  float *mu, *a, *Lq, *Q, *logpi, *pi, *S0, *sigma_d;
+  float sigma_h;
+  double* theta_dev;
+  int *n_frames;
+  long long *frame_base, *ck_off;
+  float *Bm, *mm, *pd, *kappa, *ck, *slots;
+  double *ll, *gacc, *total;
+  long long slot_floats;
+  int* status;
+  double fx, fy, cx, cy;
+  bool have_theta;
+};
+
+static int mix_grid(mkf_mixkf* h) {
+  const size_t smem = mix_smem_bytes(h->d);
+  int occ = 0;
+  MKF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mix_backward_kernel, h->tpb, smem));
+  int occ2 = 0;
+  MKF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, mix_forward_kernel, h->tpb, smem));
+  occ = std::max(1, std::min(occ, occ2));
+  h->grid = std::min(h->n_tracks, num_sms() * occ);
+  return MKF_OK;
+}
+
+extern "C" int mkf_mixkf_create(const mkf_mix_model* model, int n_tracks, const int* n_frames,
+                                const int64_t* frame_base, const double* Bm, const double* mm,
+                                const double* p_detect, const double* kappa, int64_t n_frames_total,
+                                mkf_mixkf_t* out) {
+  MKF_ARG(model && n_frames && frame_base && Bm && mm && p_detect && kappa && out, "mkf_mixkf_create: null argument");
+  MKF_ARG(model->d == 12 || model->d == 24, "mkf_mixkf_create: d must be 12 or 24");
+  MKF_ARG(model->K >= 1 && model->K <= 32, "mkf_mixkf_create: K must be in [1, 32]");
+  MKF_ARG(model->J >= 1 && model->J <= MKF_MAX_J, "mkf_mixkf_create: J out of range");
+  MKF_ARG(n_tracks >= 1 && model->pi && model->S0, "mkf_mixkf_create: bad tracks or model");
+  const int d = model->d, K = model->K, J = model->J, DD = d * (d + 1) / 2;
+  int maxT = 0;
+  for (int b = 0; b < n_tracks; ++b) {
+    MKF_ARG(n_frames[b] >= 0 && frame_base[b] >= 0 && frame_base[b] + n_frames[b] <= n_frames_total,
+            "mkf_mixkf_create: frame range");
+    MKF_ARG(p_detect[b] > 0.0 && p_detect[b] < 1.0 && kappa[b] > 0.0, "mkf_mixkf_create: p_detect/kappa");
+    maxT = std::max(maxT, n_frames[b]);
+  }
+  mkf_mixkf* h = new (std::nothrow) mkf_mixkf();
+  if (!h) return MKF_ERR_NOMEM;
+  memset(h, 0, sizeof(*h));
+  h->d = d; h->K = K; h->J = J; h->DD = DD; h->n_tracks = n_tracks; h->G = n_frames_total;
+  h->C = std::max(1, (int)std::ceil(std::sqrt((double)std::max(1, maxT))));
+  h->ng = 2 * K * d + K * DD + 1;
+  h->tpb = 32 * K;
+  h->fx = model->fx; h->fy = model->fy; h->cx = model->cx; h->cy = model->cy;
+  std::vector<long long> ckoff(n_tracks);
+  long long ck_total = 0;
+  for (int b = 0; b < n_tracks; ++b) {
+    ckoff[b] = ck_total;
+    ck_total += (long long)((n_frames[b] + h->C - 1) / h->C) * (d + d * d);
+  }
+  std::vector<float> f_Bm((size_t)n_tracks * J * 3 * d), f_mm((size_t)n_tracks * J * 3), f_pd(n_tracks), f_k(n_tracks);
+  for (size_t i = 0; i < f_Bm.size(); ++i) f_Bm[i] = (float)Bm[i];
+  for (size_t i = 0; i < f_mm.size(); ++i) f_mm[i] = (float)mm[i];
+  for (int b = 0; b < n_tracks; ++b) { f_pd[b] = (float)p_detect[b]; f_k[b] = (float)kappa[b]; }
+  std::vector<float> f_pi(K), f_lpi(K), f_S0((size_t)K * d * d);
+  for (int k = 0; k < K; ++k) {
+    f_pi[k] = (float)model->pi[k];
+    f_lpi[k] = model->pi[k] > 0.0 ? (float)std::log(model->pi[k]) : -INFINITY;
+  }
+  for (size_t i = 0; i < f_S0.size(); ++i) f_S0[i] = (float)model->S0[i];
+  std::vector<long long> fb(frame_base, frame_base + n_tracks);
+  cudaError_t e = cudaSuccess;
+  auto al = [&](void** p, size_t bytes) { if (e == cudaSuccess) e = cudaMalloc(p, std::max<size_t>(bytes, 8)); };
+  auto cp = [&](void* dst, const void* src, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+  };
+  al((void**)&h->mu, sizeof(float) * K * d); al((void**)&h->a, sizeof(float) * K * d);
+  al((void**)&h->Lq, sizeof(float) * K * DD); al((void**)&h->Q, sizeof(float) * K * d * d);
+  al((void**)&h->logpi, sizeof(float) * K); al((void**)&h->pi, sizeof(float) * K);
+  al((void**)&h->S0, sizeof(float) * K * d * d); al((void**)&h->sigma_d, sizeof(float));
+  al((void**)&h->theta_dev, sizeof(double) * h->ng);
+  al((void**)&h->n_frames, sizeof(int) * n_tracks); al((void**)&h->frame_base, sizeof(long long) * n_tracks);
+  al((void**)&h->ck_off, sizeof(long long) * n_tracks);
+  al((void**)&h->Bm, sizeof(float) * f_Bm.size()); al((void**)&h->mm, sizeof(float) * f_mm.size());
+  al((void**)&h->pd, sizeof(float) * n_tracks); al((void**)&h->kappa, sizeof(float) * n_tracks);
+  al((void**)&h->ck, sizeof(float) * std::max<long long>(1, ck_total));
+  al((void**)&h->ll, sizeof(double) * n_tracks); al((void**)&h->total, sizeof(double));
+  al((void**)&h->status, sizeof(int));
+  cp(h->pi, f_pi.data(), sizeof(float) * K); cp(h->logpi, f_lpi.data(), sizeof(float) * K);
+  cp(h->S0, f_S0.data(), sizeof(float) * f_S0.size());
+  cp(h->n_frames, n_frames, sizeof(int) * n_tracks); cp(h->frame_base, fb.data(), sizeof(long long) * n_tracks);
+  cp(h->ck_off, ckoff.data(), sizeof(long long) * n_tracks);
+  cp(h->Bm, f_Bm.data(), sizeof(float) * f_Bm.size()); cp(h->mm, f_mm.data(), sizeof(float) * f_mm.size());
+  cp(h->pd, f_pd.data(), sizeof(float) * n_tracks); cp(h->kappa, f_k.data(), sizeof(float) * n_tracks);
+  if (e == cudaSuccess) e = cudaMemset(h->status, 0, sizeof(int));
+  if (e != cudaSuccess) {
+    mkf_mixkf_destroy(h);
+    return cuda_fail(e, "mkf_mixkf_create: allocation", __FILE__, __LINE__);
+  }
+  int st = mix_grid(h);
+  if (st) { mkf_mixkf_destroy(h); return st; }
+  const CompLayout CL = comp_layout(d, J);
+  h->slot_floats = ((long long)K * CL.size + (long long)h->C * (d + d * d) + 63) & ~63LL;
+  e = cudaMalloc(&h->slots, sizeof(float) * (size_t)h->slot_floats * h->grid);
+  if (e == cudaSuccess) e = cudaMalloc(&h->gacc, sizeof(double) * (size_t)h->ng * h->grid);
+  if (e != cudaSuccess) {
+    mkf_mixkf_destroy(h);
+    return cuda_fail(e, "mkf_mixkf_create: scratch allocation", __FILE__, __LINE__);
+  }
+  *out = h;
+  return MKF_OK;
+}
+
+extern "C" int mkf_mixkf_theta_size(mkf_mixkf_t h) { return h ? h->ng : 0; }
+
+extern "C" int mkf_mixkf_set_theta_device(mkf_mixkf_t h, const double* d_theta, mkf_stream_t stream) {
+  MKF_ARG(h && d_theta, "mkf_mixkf_set_theta_device: null argument");
+  cudaStream_t s = (cudaStream_t)stream;
+  const int n = h->ng + h->K * h->d * h->d;
+  mix_prepare_kernel<<<(n + 255) / 256, 256, 0, s>>>(d_theta, h->d, h->K, h->mu, h->a, h->Lq, h->Q, h->sigma_d);
+  MKF_CHECK_LAUNCH("mkf_mixkf_set_theta_device");
+  MKF_CUDA(cudaMemcpyAsync(&h->sigma_h, h->sigma_d, sizeof(float), cudaMemcpyDeviceToHost, s));
+  MKF_CUDA(cudaStreamSynchronize(s));
+  h->have_theta = true;
+  return MKF_OK;
+}
+
+extern "C" int mkf_mixkf_set_theta(mkf_mixkf_t h, const double* theta) {
+  MKF_ARG(h && theta, "mkf_mixkf_set_theta: null argument");
+  MKF_ARG(theta[h->ng - 1] > 0.0, "mkf_mixkf_set_theta: sigma must be positive");
+  MKF_CUDA(cudaMemcpy(h->theta_dev, theta, sizeof(double) * h->ng, cudaMemcpyHostToDevice));
+  return mkf_mixkf_set_theta_device(h, h->theta_dev, nullptr);
+}
+
+static MixArgs mix_args(mkf_mixkf* h, const int* det_off, const float* det) {
+  MixArgs A;
+  memset(&A, 0, sizeof(A));
+  A.M.d = h->d; A.M.K = h->K; A.M.J = h->J; A.M.DD = h->DD;
+  A.M.mu = h->mu; A.M.a = h->a; A.M.Lq = h->Lq; A.M.Q = h->Q; A.M.logpi = h->logpi; A.M.pi = h->pi;
+  A.M.S0 = h->S0; A.M.sigma = h->sigma_h;
+  A.M.fx = (float)h->fx; A.M.fy = (float)h->fy; A.M.cx = (float)h->cx; A.M.cy = (float)h->cy;
+  A.n_tracks = h->n_tracks; A.C = h->C;
+  A.n_frames = h->n_frames; A.frame_base = h->frame_base; A.Bm = h->Bm; A.mm = h->mm;
+  A.pd = h->pd; A.kappa = h->kappa; A.det_off = det_off; A.det = reinterpret_cast<const float2*>(det);
+  A.ck_off = h->ck_off; A.ck = h->ck; A.ll = h->ll; A.slots = h->slots; A.slot_floats = h->slot_floats;
+  A.gacc = h->gacc; A.ng = h->ng; A.status = h->status;
+  return A;
+}
+
+extern "C" int mkf_mixkf_forward(mkf_mixkf_t h, const int* d_det_off, const float* d_det, double* d_loglik,
+                                 double* d_total, mkf_stream_t stream) {
+  MKF_ARG(h && d_det_off && d_det, "mkf_mixkf_forward: null argument");
+  if (!h->have_theta) { set_error("mkf_mixkf_forward: set theta first"); return MKF_ERR_STATE; }
+  cudaStream_t s = (cudaStream_t)stream;
+  MixArgs A = mix_args(h, d_det_off, d_det);
+  const size_t smem = mix_smem_bytes(h->d);
+  mix_forward_kernel<<<h->grid, h->tpb, smem, s>>>(A);
+  MKF_CHECK_LAUNCH("mkf_mixkf_forward");
+  if (d_loglik) MKF_CUDA(cudaMemcpyAsync(d_loglik, h->ll, sizeof(double) * h->n_tracks, cudaMemcpyDeviceToDevice, s));
+  mix_total_kernel<<<1, 256, 0, s>>>(h->ll, h->n_tracks, d_total ? d_total : h->total);
+  MKF_CHECK_LAUNCH("mkf_mixkf_forward: total");
+  return MKF_OK;
+}
+
+extern "C" int mkf_mixkf_backward(mkf_mixkf_t h, const int* d_det_off, const float* d_det, double* d_grad,
+                                  mkf_stream_t stream) {
+  MKF_ARG(h && d_det_off && d_det && d_grad, "mkf_mixkf_backward: null argument");
+  if (!h->have_theta) { set_error("mkf_mixkf_backward: set theta first"); return MKF_ERR_STATE; }
+  cudaStream_t s = (cudaStream_t)stream;
+  MixArgs A = mix_args(h, d_det_off, d_det);
+  MKF_CUDA(cudaMemsetAsync(h->gacc, 0, sizeof(double) * (size_t)h->ng * h->grid, s));
+  const size_t smem = mix_smem_bytes(h->d);
+  mix_backward_kernel<<<h->grid, h->tpb, smem, s>>>(A);
+  MKF_CHECK_LAUNCH("mkf_mixkf_backward");
+  mix_reduce_kernel<<<(h->ng + 255) / 256, 256, 0, s>>>(h->gacc, h->grid, h->ng, d_grad);
+  MKF_CHECK_LAUNCH("mkf_mixkf_backward: reduce");
+  return MKF_OK;
+}
+
+extern "C" int mkf_mixkf_status(mkf_mixkf_t h, int* status) {
+  MKF_ARG(h && status, "mkf_mixkf_status: null argument");
+  MKF_CUDA(cudaMemcpy(status, h->status, sizeof(int), cudaMemcpyDeviceToHost));
+  return MKF_OK;
+}
+
+extern "C" int mkf_mixkf_destroy(mkf_mixkf_t h) {
+  if (!h) return MKF_OK;
+  void* ps[] = {h->mu, h->a, h->Lq, h->Q, h->logpi, h->pi, h->S0, h->sigma_d, h->theta_dev, h->n_frames,
+                h->frame_base, h->ck_off, h->Bm, h->mm, h->pd, h->kappa, h->ck, h->ll, h->total, h->status,
+                h->slots, h->gacc};
+  for (void* p : ps) if (p) cudaFree(p);
+  delete h;
+  return MKF_OK;
+}
+
+extern "C" int mkf_adam_step(double* d_theta, const double* d_grad, double* d_m, double* d_v, const uint8_t* d_mask,
+                             int n, int step, double lr, double b1, double b2, double eps, int maximize,
+                             mkf_stream_t stream) {
+  MKF_ARG(d_theta && d_grad && d_m && d_v && n > 0 && step >= 1, "mkf_adam_step: bad argument");
+  const double c1 = 1.0 - std::pow(b1, step), c2 = 1.0 - std::pow(b2, step);
+  adam_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(d_theta, d_grad, d_m, d_v, d_mask, n, c1, c2, lr,
+                                                                  b1, b2, eps, maximize ? 1.0 : -1.0);
+  MKF_CHECK_LAUNCH("mkf_adam_step");
+  return MKF_OK;
+}

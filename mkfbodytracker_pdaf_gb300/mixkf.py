@@ -1,0 +1,109 @@
+"""Host-side API of the mixture Kalman filter log-likelihood and its adjoint
+(forward/backward pair of the C ABI), and the on-device Adam fitting loop of
+the motion model.
+
+theta (flat FP64) = [mu (K*d), a (K*d), Lq packed lower (K*d(d+1)/2), sigma].
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _native as N
+from .filters import _ptr, _stream
+
+
+def theta_from(mu, a, Lq_packed, sigma):
+    return np.concatenate([np.ravel(mu), np.ravel(a), np.ravel(Lq_packed), [float(sigma)]]).astype(np.float64)
+
+
+def theta_split(theta, K, d):
+    DD = d * (d + 1) // 2
+    return (theta[:K * d].reshape(K, d), theta[K * d:2 * K * d].reshape(K, d),
+            theta[2 * K * d:2 * K * d + K * DD].reshape(K, DD), float(theta[-1]))
+
+
+class MixtureKF:
+    """Batched mixture KF over the tracks of a synth.MixBatch-like object."""
+
+    def __init__(self, batch, pi, S0, cam=(525.0, 525.0, 319.5, 239.5)):
+        import torch
+        self.torch = torch
+        self.batch = batch
+        self.K, self.d = np.asarray(S0).shape[0], np.asarray(S0).shape[1]
+        self.J = batch.Bm.shape[1]
+        self._pi = np.ascontiguousarray(pi, np.float64)
+        self._S0 = np.ascontiguousarray(S0, np.float64)
+        desc = N.MixModelDesc(self.d, self.K, self.J, self._pi.ctypes.data_as(C.c_void_p),
+                              self._S0.ctypes.data_as(C.c_void_p), *cam)
+        nt = batch.n_tracks
+        nf = np.array([t["n_frames"] for t in batch.tracks], np.int32)
+        fb = np.array([t["frame_base"] for t in batch.tracks], np.int64)
+        Bm = np.ascontiguousarray(np.stack([batch.Bm[t["body"]] for t in batch.tracks]), np.float64)
+        mm = np.ascontiguousarray(np.stack([batch.mm[t["body"]] for t in batch.tracks]), np.float64)
+        pd = np.array([t["pd"] for t in batch.tracks], np.float64)
+        kp = np.array([t["kappa"] for t in batch.tracks], np.float64)
+        pp = lambda a: a.ctypes.data_as(C.c_void_p)
+        h = C.c_void_p()
+        N.check(N.lib().mkf_mixkf_create(C.byref(desc), nt, pp(nf), pp(fb), pp(Bm), pp(mm), pp(pd), pp(kp),
+                                         batch.n_frames_total, C.byref(h)), "mkf_mixkf_create")
+        self.h = h
+        self.n_theta = N.lib().mkf_mixkf_theta_size(h)
+        self.det_off = torch.from_numpy(np.ascontiguousarray(batch.det_off, np.int32)).cuda()
+        self.det = torch.from_numpy(np.ascontiguousarray(batch.det, np.float32)).cuda()
+        self.ll = torch.zeros(nt, dtype=torch.float64, device="cuda")
+        self.total = torch.zeros(1, dtype=torch.float64, device="cuda")
+        self.grad = torch.zeros(self.n_theta, dtype=torch.float64, device="cuda")
+
+    def set_theta(self, theta):
+        if hasattr(theta, "data_ptr"):
+            N.check(N.lib().mkf_mixkf_set_theta_device(self.h, _ptr(theta), _stream(self.torch)),
+                    "mkf_mixkf_set_theta_device")
+        else:
+            th = np.ascontiguousarray(theta, np.float64)
+            assert th.size == self.n_theta
+            N.check(N.lib().mkf_mixkf_set_theta(self.h, th.ctypes.data_as(C.c_void_p)), "mkf_mixkf_set_theta")
+
+    def forward(self, stream=None):
+        N.check(N.lib().mkf_mixkf_forward(self.h, _ptr(self.det_off), _ptr(self.det), _ptr(self.ll),
+                                          _ptr(self.total), _stream(self.torch, stream)), "mkf_mixkf_forward")
+        return self.total
+
+    def backward(self, stream=None):
+        N.check(N.lib().mkf_mixkf_backward(self.h, _ptr(self.det_off), _ptr(self.det), _ptr(self.grad),
+                                           _stream(self.torch, stream)), "mkf_mixkf_backward")
+        return self.grad
+
+    def status(self):
+        s = C.c_int()
+        N.check(N.lib().mkf_mixkf_status(self.h, C.byref(s)), "mkf_mixkf_status")
+        return s.value
+
+    def fit_adam(self, theta0, steps, lr=1e-2, mask=None, callback=None):
+        """Maximise the total logL with Adam on the device (theta, moments, mask
+        and gradient stay in HBM; one forward + backward + update per step)."""
+        torch = self.torch
+        th = torch.from_numpy(np.ascontiguousarray(theta0, np.float64)).cuda()
+        m = torch.zeros_like(th)
+        v = torch.zeros_like(th)
+        mk = None if mask is None else torch.from_numpy(np.ascontiguousarray(mask, np.uint8)).cuda()
+        hist = []
+        for it in range(1, steps + 1):
+            self.set_theta(th)
+            self.forward()
+            self.backward()
+            N.check(N.lib().mkf_adam_step(_ptr(th), _ptr(self.grad), _ptr(m), _ptr(v), _ptr(mk), self.n_theta, it,
+                                          float(lr), 0.9, 0.999, 1e-8, 1, _stream(torch)), "mkf_adam_step")
+            if callback is not None:
+                callback(it, th, self.total)
+            hist.append(self.total)
+        return th, hist
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                N.lib().mkf_mixkf_destroy(self.h)
+                self.h = None
+        except Exception:
+            pass

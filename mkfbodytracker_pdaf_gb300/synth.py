@@ -365,3 +365,60 @@ def make_rbpf_scene(seed=MASTER_SEED, T=500, d=12, K=15, lam=3.0, pd=0.9, max_de
         rng.shuffle(hands)
         frames.append(dict(heads=heads, hands=hands))
     return RbpfScene(arms, frames, np.stack(truths))
+
+
+# ----------------------------------------------------------------- configs 3/4: mixture KF
+class MixBatch:
+    """Tracks sharing one motion model (theta), each with its own body
+    (basis + mean pose + depth) and detection lists.  det_off indexes
+    (global frame g, joint j) lists like BpfBatch."""
+
+    def __init__(self, gmm, tracks, Bm, mm, det_off, det, truth, cam=CAM):
+        self.gmm, self.tracks, self.Bm, self.mm = gmm, tracks, Bm, mm
+        self.det_off, self.det, self.truth, self.cam = det_off, det, truth, cam
+        self.n_frames_total = int(sum(t["n_frames"] for t in tracks))
+        self.J = Bm.shape[1]
+
+    @property
+    def n_tracks(self):
+        return len(self.tracks)
+
+    def theta_true(self, sigma=SIGMA_PX):
+        return dict(mu=self.gmm["mu"], a=self.gmm["a"], Lq=pack_lower(self.gmm["Lq"]), sigma=sigma,
+                    pi=self.gmm["pi"], S0=self.gmm["Sigma"])
+
+
+def make_mix_batch(seed, n_tracks, T, K=15, d=12, lam=3.0, pd=0.9, layout="arm4", max_det=16, chunk=2048):
+    rng = np.random.default_rng(seed)
+    gmm = make_gmm(rng, d, K)
+    Bs, mbar, measured = make_body(rng, d, n=n_tracks, layout=layout)
+    J = len(measured)
+    G = n_tracks * T
+    truth = np.zeros((G, d), np.float32)
+    for s0 in range(0, n_tracks, chunk):
+        n = min(chunk, n_tracks - s0)
+        g = {k: np.broadcast_to(v, (n,) + v.shape) for k, v in gmm.items()}
+        xs = simulate_states(rng, g, T, n=n)
+        truth[s0 * T:(s0 + n) * T] = xs.reshape(n * T, d)
+    bidx = np.repeat(np.arange(n_tracks), T)
+    full = np.einsum("gij,gj->gi", Bs[bidx], truth.astype(np.float64)) + mbar[bidx]
+    P3 = full.reshape(G, -1, 3)[:, list(measured)]
+    px = project(P3) + rng.normal(0, SIGMA_PX, (G, J, 2))
+    det_mask = (rng.random((G, J)) < pd) & (P3[..., 2] > 0.05)
+    off, pts = _lists_from(rng, px.reshape(G * J, 1, 2), det_mask.reshape(G * J, 1),
+                           np.full(G * J, lam), max_det, shuffle=False)
+    tracks = [dict(n_frames=T, frame_base=b * T, body=b, pd=float(min(pd, 0.999)),
+                   kappa=float(max(lam, 0.01) / (IMG_W * IMG_H))) for b in range(n_tracks)]
+    Bm = Bs.reshape(n_tracks, -1, 3, d)[:, list(measured)].copy()
+    mm = mbar.reshape(n_tracks, -1, 3)[:, list(measured)].copy()
+    return MixBatch(gmm, tracks, Bm, mm, off.astype(np.int32), pts, truth)
+
+
+def config3_batch(n_tracks=1024, T=1000, seed=MASTER_SEED + 3):
+    """Differentiation workload: B=1024 x T=1000, K=15, d=12, PDAF over <=16 candidates."""
+    return make_mix_batch(seed, n_tracks, T, K=15, d=12, lam=3.0, pd=0.9)
+
+
+def config4_batch(n_tracks=16384, T=500, seed=MASTER_SEED + 4):
+    """Fitting workload: ground-truth GMM K=32, d=24 (8 joints x 3D), lambda=5."""
+    return make_mix_batch(seed, n_tracks, T, K=32, d=24, lam=5.0, pd=0.9, layout="body8")

@@ -23,7 +23,7 @@ import numpy as np
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _BUILD = os.path.join(_HERE, "_build")
 _SO = os.path.join(_BUILD, "libmkf_oracle.so")
-_SRC = [os.path.join(_HERE, "mkf_oracle.c")]
+_SRC = [os.path.join(_HERE, "mkf_oracle.c"), os.path.join(_HERE, "mkf_oracle_mix.c")]
 _lib = None
 
 
@@ -78,6 +78,11 @@ class Track(C.Structure):
                 ("kappa", F), ("pd", F), ("sigma", F)]
 
 
+class MixParams(C.Structure):
+    _fields_ = [("d", I), ("K", I), ("J", I), ("mu", P), ("a", P), ("Lq", P), ("pi", P), ("S0", P),
+                ("sigma", D), ("fx", D), ("fy", D), ("cx", D), ("cy", D)]
+
+
 def _declare(L):
     L.mko_philox4x32_10.argtypes = [P, P, P]
     L.mko_draw_block.argtypes = [U64, U32, U32, U32, U32, P]
@@ -114,6 +119,12 @@ def _declare(L):
     L.mko_bpf_run_tracks.argtypes = [I, P, I, I, I, P, P, P, P, P, P, P, P,
                                      F, F, F, F, P, P, P, P, P, I]
     L.mko_num_threads.restype = I
+    L.mko_mix_forward.argtypes = [C.POINTER(MixParams), I, C.c_longlong, P, P, D, D, P, P]
+    L.mko_mix_forward.restype = D
+    L.mko_mix_adjoint.argtypes = [C.POINTER(MixParams), I, C.c_longlong, P, P, D, D, P, P, P, P, P, P]
+    L.mko_mix_adjoint.restype = D
+    L.mko_mix_batch.argtypes = [C.POINTER(MixParams), I, P, P, P, P, P, P, P, P, I, P, P, P, P, P, I]
+    L.mko_mix_batch.restype = D
 
 
 def _p(a):
@@ -412,3 +423,51 @@ def pose_tracker_run(scene, N, seed, T=None, Pa=0.05, clutter=1e-4, hand_joint=1
         for a in range(2):
             est[a, t] = xs[a].mean(0)
     return est, skipped
+
+
+# ---------------------------------------------------------------- A11 mixture KF + adjoint
+class MixModel:
+    """FP64 mixture-KF parameters (theta = mu, a, Lq packed, sigma; fixed pi, S0, camera)."""
+
+    def __init__(self, mu, a, Lq, sigma, pi, S0, cam=(525.0, 525.0, 319.5, 239.5), J=2):
+        self.mu, self.a, self.Lq = _c(mu, np.float64), _c(a, np.float64), _c(Lq, np.float64)
+        self.pi, self.S0 = _c(pi, np.float64), _c(S0, np.float64)
+        self.K, self.d = self.mu.shape
+        self.sigma = float(sigma)
+        self.cam = cam
+        self.J = J
+        self.s = MixParams(self.d, self.K, J, _p(self.mu), _p(self.a), _p(self.Lq), _p(self.pi), _p(self.S0),
+                           self.sigma, *cam)
+
+    def theta(self):
+        return np.concatenate([self.mu.ravel(), self.a.ravel(), self.Lq.ravel(), [self.sigma]])
+
+    def with_theta(self, th):
+        K, d = self.K, self.d
+        DD = d * (d + 1) // 2
+        mu = th[:K * d].reshape(K, d)
+        a = th[K * d:2 * K * d].reshape(K, d)
+        Lq = th[2 * K * d:2 * K * d + K * DD].reshape(K, DD)
+        return MixModel(mu, a, Lq, th[-1], self.pi, self.S0, self.cam, self.J)
+
+
+def mix_batch(model, batch, grad=False, nthreads=0, tracks=None):
+    """Sum over tracks of the mixture-KF logL (and its gradient as a flat theta
+    vector) for a synth.MixBatch-like object."""
+    ids = list(range(batch.n_tracks)) if tracks is None else list(tracks)
+    nf = np.array([batch.tracks[b]["n_frames"] for b in ids], np.int32)
+    fb = np.array([batch.tracks[b]["frame_base"] for b in ids], np.int64)
+    Bm = _c(np.stack([batch.Bm[batch.tracks[b]["body"]] for b in ids]), np.float64)
+    mm = _c(np.stack([batch.mm[batch.tracks[b]["body"]] for b in ids]), np.float64)
+    pd = np.array([batch.tracks[b]["pd"] for b in ids], np.float64)
+    kp = np.array([batch.tracks[b]["kappa"] for b in ids], np.float64)
+    K, d = model.K, model.d
+    DD = d * (d + 1) // 2
+    ll = np.zeros(len(ids))
+    g = [np.zeros(K * d), np.zeros(K * d), np.zeros(K * DD), np.zeros(1)]
+    tot = lib().mko_mix_batch(C.byref(model.s), len(ids), _p(nf), _p(fb), _p(Bm), _p(mm), _p(pd), _p(kp),
+                              _p(_c(batch.det_off, np.int32)), _p(_c(batch.det, np.float32)), int(grad),
+                              _p(ll), *[_p(x) for x in g], int(nthreads))
+    if grad:
+        return tot, ll, np.concatenate(g)
+    return tot, ll

@@ -159,7 +159,46 @@ void mko_bpf_run_tracks(int n_tracks, const mko_track* tracks, int d, int K, int
 
 int mko_num_threads(void);
 
+/* ---- A11: deterministic mixture KF (GPB1 over the K components) with PDAF
+ * over each measured joint's candidate list, and its reverse-mode adjoint.
+ * Not a single reference function: it is the component-marginalised analogue
+ * of ParticleFilter::update (pf2DRao.cpp:125-158, which redraws the component
+ * every frame i.i.d. from pi, pf2DRao.cpp:128) built from KF_model
+ * (KF_model.cpp:11-25) and the PDA weighting of pfPose.cpp:247-298.
+ * Per frame: per component predict (x = a*x + (1-a)*mu, P = A P A + Lq Lq^T),
+ * sequential PDAF/EKF updates over the joints (Bar-Shalom combined innovation),
+ * l_k = sum_j log[(1-P_D) kappa + P_D sum_i N(z_i; zhat, S)], mixture weights
+ * w_k ~ pi_k exp(l_k), c_t = log sum_k pi_k exp(l_k), moment-matched collapse,
+ * symmetrisation of P.  logL = sum_t c_t.  Parameters differentiated: mu, a,
+ * Lq (packed lower), sigma (R = sigma^2 I2 per joint). */
+typedef struct {
+  int d, K, J;
+  const double* mu;    /* K*d */
+  const double* a;     /* K*d */
+  const double* Lq;    /* K*d(d+1)/2 */
+  const double* pi;    /* K */
+  const double* S0;    /* K*d*d prior covariances (not differentiated) */
+  double sigma;
+  double fx, fy, cx, cy;
+} mko_mix_params;
+
+/* one track: T frames at frame_base; Bm (J*3*d), mm (J*3) its body; det_off
+ * indexes (global frame g, joint j) lists as for the bootstrap filter */
+double mko_mix_forward(const mko_mix_params* p, int T, long long frame_base, const double* Bm,
+                       const double* mm, double pd, double kappa, const int* det_off, const float* det);
+/* logL and its gradient (accumulated into g_mu (K*d), g_a (K*d), g_Lq (K*DD), g_sigma) */
+double mko_mix_adjoint(const mko_mix_params* p, int T, long long frame_base, const double* Bm,
+                       const double* mm, double pd, double kappa, const int* det_off, const float* det,
+                       double* g_mu, double* g_a, double* g_Lq, double* g_sigma);
+/* batch over tracks (OpenMP); body arrays stacked per track; returns sum logL;
+ * per-track logL in ll (optional); gradients summed if grad != 0 */
+double mko_mix_batch(const mko_mix_params* p, int n_tracks, const int* n_frames, const long long* frame_base,
+                     const double* Bm, const double* mm, const double* pd, const double* kappa,
+                     const int* det_off, const float* det, int grad, double* ll, double* g_mu,
+                     double* g_a, double* g_Lq, double* g_sigma, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif
 #endif
+

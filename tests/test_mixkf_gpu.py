@@ -1,0 +1,67 @@
+"""GPU mixture-KF log-likelihood and hand-written adjoint (sqrt(T)
+checkpointing) against the FP64 CPU forward/adjoint and FP64 central finite
+differences."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(olib, n_tracks=6, T=40, K=6, seed=5):
+    from mkfbodytracker_pdaf_gb300 import mixkf, synth
+    b = synth.make_mix_batch(seed, n_tracks, T, K=K, d=12)
+    tt = b.theta_true()
+    om = olib.MixModel(tt["mu"], tt["a"], tt["Lq"], tt["sigma"], tt["pi"], tt["S0"])
+    th = om.theta()
+    g = mixkf.MixtureKF(b, tt["pi"], tt["S0"])
+    return b, om, th, g
+
+
+def test_forward_matches_oracle(cuda, olib):
+    b, om, th, g = _setup(olib)
+    g.set_theta(th)
+    tot = g.forward().item()
+    ll = g.ll.cpu().numpy()
+    L, ll_ref = olib.mix_batch(om, b)
+    np.testing.assert_allclose(ll, ll_ref, rtol=1e-4)
+    assert abs(tot - L) <= 1e-4 * abs(L)
+    assert g.status() == 0
+
+
+def test_gradient_matches_fp64_adjoint_and_fd(cuda, olib):
+    b, om, th, g = _setup(olib, n_tracks=4, T=37)        # T not a multiple of the checkpoint stride
+    g.set_theta(th)
+    g.forward()
+    grad = g.backward().cpu().numpy()
+    L, _, gref = olib.mix_batch(om, b, grad=True)
+    rng = np.random.default_rng(3)
+    rel = []
+    for _ in range(16):
+        v = rng.standard_normal(th.size)
+        v /= np.linalg.norm(v)
+        rel.append(abs(v @ grad - v @ gref) / max(abs(v @ gref), 1e-6))
+    assert max(rel) < 1e-3, max(rel)
+    # per-block agreement with FP64 central differences (relative step 1e-6)
+    K, d = 6, 12
+    blocks = {"mu": slice(0, K * d), "a": slice(K * d, 2 * K * d), "Lq": slice(2 * K * d, th.size - 1),
+              "sigma": slice(th.size - 1, th.size)}
+    for name, sl in blocks.items():
+        v = np.zeros(th.size)
+        v[sl] = rng.standard_normal(v[sl].size)
+        v /= np.linalg.norm(v)
+        h = 1e-6 * max(1.0, np.abs(th).max())
+        Lp, _ = olib.mix_batch(om.with_theta(th + h * v), b)
+        Lm, _ = olib.mix_batch(om.with_theta(th - h * v), b)
+        fd = (Lp - Lm) / (2 * h)
+        assert abs(v @ gref - fd) <= 1e-6 * max(1.0, abs(fd)), (name, v @ gref, fd)
+        assert abs(v @ grad - fd) <= 1e-3 * max(1.0, abs(fd)), (name, v @ grad, fd)
+
+
+def test_gradient_deterministic(cuda, olib):
+    b, om, th, g = _setup(olib, n_tracks=5, T=20)
+    g.set_theta(th)
+    g.forward()
+    g1 = g.backward().cpu().numpy().copy()
+    g.forward()
+    g2 = g.backward().cpu().numpy()
+    np.testing.assert_array_equal(g1, g2)
