@@ -321,6 +321,243 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------- extra workloads
+def _events(torch):
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def run_sweep(args):
+    """Particle-count sweep (config 1): one track, T=200, N = 2^12 .. 2^22,
+    through the plain per-track C-ABI path (three grid-wide kernels per frame).
+    Reports particle-frames/s and the HBM roofline fraction at 112 B per
+    particle-frame."""
+    import torch
+    from mkfbodytracker_pdaf_gb300 import build, synth
+    from mkfbodytracker_pdaf_gb300.filters import BootstrapParticleFilter
+    build.build()
+    peak, peak_kind = load_peaks()
+    rows = []
+    T = args.sweep_frames
+    for lg in range(12, 23, 2):
+        N = 1 << lg
+        batch = synth.config1_batch(N, n_frames=T)
+        t = batch.tracks[0]
+        J = batch.model["J"]
+        lo = batch.det_off.astype(np.int64)
+        det = torch.from_numpy(batch.det.copy()).cuda()
+        offs = torch.from_numpy(lo.astype(np.int32)).cuda()
+        pf = BootstrapParticleFilter(batch.model, t)
+        est = torch.empty((T, batch.model["d"]), dtype=torch.float32, device="cuda")
+        ll = torch.empty(T, dtype=torch.float32, device="cuda")
+        ess = torch.empty(T, dtype=torch.float32, device="cuda")
+
+        def run_all():
+            pf.reset()
+            for f in range(T):
+                pf.update(f, offs[f * J:], det, est=est[f], loglik=ll[f], ess=ess[f])
+
+        for _ in range(args.warmup):
+            run_all()
+        torch.cuda.synchronize()
+        e0, e1 = _events(torch)
+        e0.record()
+        for _ in range(args.steps):
+            run_all()
+        e1.record()
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1000 / args.steps
+        pfs = N * T / sec
+        ach = BYTES_PER_PF * N * T / sec / 1e9
+        rows.append({"N": N, "T": T, "ms_per_track": sec * 1e3, "particle_frames_per_s": pfs,
+                     "track_frames_per_s": T / sec, "achieved_GBps": ach, "frac_of_" + peak_kind + "_hbm": ach / peak,
+                     "l2_resident": N <= (1 << 18)})
+    print(json.dumps({"workload": "particle-count sweep, one track, T=%d, plain per-track path" % T,
+                      "unit": "particle-frames/s", "peak_hbm_GBps": peak, "rows": rows}), flush=True)
+
+
+def run_plain0(args):
+    """Config 0: two arms, K=15, d=12, N=1000 particles per arm, T=500, FP64
+    Rao-Blackwellised filters + PDAF association through PoseTracker, against
+    the CPU restatement of the reference frame loop."""
+    import torch
+    import oracle
+    from mkfbodytracker_pdaf_gb300 import build, synth
+    from mkfbodytracker_pdaf_gb300.filters import MEAS_PINHOLE, PoseTracker, RaoBlackwellisedPF
+    build.build()
+    oracle.build()
+    T, N, seed = 500, 1000, synth.MASTER_SEED
+    sc = synth.make_rbpf_scene(T=T)
+
+    def make():
+        arms = []
+        for a in range(2):
+            arm = sc.arms[a]
+            pf = RaoBlackwellisedPF(12, 4, 15, N, meas_mode=MEAS_PINHOLE, seed=seed, track_id=a)
+            for k in range(15):
+                pf.set_component(k, arm["mu"][k], np.diag(arm["F"][k]), arm["Q"][k], arm["Sigma"][k],
+                                 arm["R"][k], arm["weight"][k])
+            pf.set_pinhole(arm["Bm"], arm["mm"], synth.CAM)
+            pf.set_hand_decode(joint=1)
+            pf.resetTracker()
+            arms.append(pf)
+        return PoseTracker(arms[0], arms[1])
+
+    rois = [None if any(len(h) == 0 for h in fr["heads"]) else np.stack([oracle.scene_roi(fr["heads"][a]) for a in range(2)])
+            for fr in sc.frames]
+    cands = [torch.from_numpy(fr["hands"]).cuda() if len(fr["hands"]) else None for fr in sc.frames]
+    est = np.full((2, T, 12), np.nan)
+    times = []
+    for rep in range(args.warmup + args.steps):
+        trk = make()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for t in range(T):
+            e = trk.step(t, rois[t], cands[t])
+            if rep == 0 and e is not None:
+                for a in range(2):
+                    est[a, t] = e[a].cpu().numpy()
+        torch.cuda.synchronize()
+        if rep >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    gpu_s = float(np.median(times))
+    t0 = time.perf_counter()
+    est_c, skipped = oracle.pose_tracker_run(sc, N, seed, T=T)
+    cpu_s = time.perf_counter() - t0
+    ok = ~skipped
+    rel = float(np.abs(est[:, ok] - est_c[:, ok]).max() / np.abs(est_c[:, ok]).max())
+    err = float(np.abs(est_c[:, ok] - sc.truth[:, ok]).mean())
+    print(json.dumps({"workload": "config 0: 2 arms x T=%d, N=%d, K=15, d=12, FP64 RBPF + PDAF" % (T, N),
+                      "gpu_track_frames_per_s": 2 * T / gpu_s, "gpu_s": gpu_s,
+                      "cpu_track_frames_per_s": 2 * T / cpu_s, "cpu_s": cpu_s, "cpu_threads": 1,
+                      "max_rel_est_err_vs_cpu": rel, "mean_abs_latent_err_vs_truth": err,
+                      "frames_skipped": int(skipped.sum())}), flush=True)
+
+
+def run_adjoint(args):
+    """Config 3: mixture-KF logL over B=1024 x T=1000, K=15, d=12; forward and
+    backward times, backward/forward ratio, and gradient accuracy against the
+    FP64 CPU adjoint and FP64 central differences on a track subset."""
+    import torch
+    import oracle
+    from mkfbodytracker_pdaf_gb300 import build, mixkf, synth
+    build.build()
+    oracle.build()
+    b = synth.config3_batch(n_tracks=args.adj_tracks, T=args.adj_frames)
+    tt = b.theta_true()
+    om = oracle.MixModel(tt["mu"], tt["a"], tt["Lq"], tt["sigma"], tt["pi"], tt["S0"])
+    th = om.theta()
+    g = mixkf.MixtureKF(b, tt["pi"], tt["S0"])
+    g.set_theta(th)
+    for _ in range(args.warmup):
+        g.forward()
+        g.backward()
+    torch.cuda.synchronize()
+    fwd, bwd = [], []
+    for _ in range(args.steps):
+        e0, e1 = _events(torch)
+        e2 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        g.forward()
+        e1.record()
+        g.backward()
+        e2.record()
+        torch.cuda.synchronize()
+        fwd.append(e0.elapsed_time(e1))
+        bwd.append(e1.elapsed_time(e2))
+    L_gpu = g.forward().item()
+    grad = g.backward().cpu().numpy()
+    # accuracy on a subset (FP64 CPU adjoint and central differences, 64 directions)
+    sub = list(range(min(args.adj_check_tracks, b.n_tracks)))
+    sb = synth.MixBatch(b.gmm, [b.tracks[i] for i in sub], b.Bm, b.mm, b.det_off, b.det, b.truth)
+    gs = mixkf.MixtureKF(sb, tt["pi"], tt["S0"])
+    gs.set_theta(th)
+    gs.forward()
+    grad_s = gs.backward().cpu().numpy()
+    t0 = time.perf_counter()
+    L_c, _, gref = oracle.mix_batch(om, sb, grad=True)
+    cpu_adj_s = time.perf_counter() - t0
+    rng = np.random.default_rng(64)
+    rel_fd, rel_adj, rel_cpu_fd = [], [], []
+    for _ in range(args.fd_dirs):
+        v = rng.standard_normal(th.size)
+        v /= np.linalg.norm(v)
+        h = 1e-6 * max(1.0, np.abs(th).max())
+        Lp, _ = oracle.mix_batch(om.with_theta(th + h * v), sb)
+        Lm, _ = oracle.mix_batch(om.with_theta(th - h * v), sb)
+        fd = (Lp - Lm) / (2 * h)
+        rel_fd.append(abs(v @ grad_s - fd) / max(abs(fd), 1e-9))
+        rel_cpu_fd.append(abs(v @ gref - fd) / max(abs(fd), 1e-9))
+        rel_adj.append(abs(v @ grad_s - v @ gref) / max(abs(v @ gref), 1e-9))
+    L_sub_gpu = float(gs.ll.sum().item())
+    tf = float(np.median(fwd))
+    tb = float(np.median(bwd))
+    print(json.dumps({
+        "workload": "config 3: mixture-KF logL, B=%d x T=%d, K=15, d=12, PDAF <=16 candidates, FP32 + FP64 sums"
+                    % (b.n_tracks, args.adj_frames),
+        "forward_ms": tf, "backward_ms": tb, "backward_over_forward": tb / tf,
+        "track_frames_per_s_forward": b.n_frames_total / tf * 1e3,
+        "gradient_evals_per_s": 1e3 / (tf + tb), "logL": L_gpu,
+        "checkpoint_stride": int(np.ceil(np.sqrt(args.adj_frames))),
+        "check_subset_tracks": len(sub), "logL_rel_err_subset": abs(L_sub_gpu - L_c) / abs(L_c),
+        "fd_directions": args.fd_dirs,
+        "grad_rel_err_vs_fd": {"median": float(np.median(rel_fd)), "max": float(np.max(rel_fd))},
+        "grad_rel_err_vs_cpu_adjoint": {"median": float(np.median(rel_adj)), "max": float(np.max(rel_adj))},
+        "cpu_adjoint_rel_err_vs_fd": {"median": float(np.median(rel_cpu_fd)), "max": float(np.max(rel_cpu_fd))},
+        "cpu_adjoint_s_subset": cpu_adj_s}), flush=True)
+
+
+def run_fit(args):
+    """Config 4: fit the motion model (K=32, d=24) by gradient on the device
+    from data the filter's own generative model produced."""
+    import torch
+    from mkfbodytracker_pdaf_gb300 import build, mixkf, synth
+    build.build()
+    b = synth.config4_batch(n_tracks=args.fit_tracks, T=args.fit_frames)
+    tt = b.theta_true()
+    K, d = 32, 24
+    th_true = mixkf.theta_from(tt["mu"], tt["a"], tt["Lq"], tt["sigma"])
+    rng = np.random.default_rng(4)
+    mu0 = tt["mu"] + rng.normal(0, 0.3, tt["mu"].shape)
+    Lq0 = tt["Lq"] * np.sqrt(1.5)                 # covariances x1.5
+    th0 = mixkf.theta_from(mu0, tt["a"], Lq0, tt["sigma"] * np.sqrt(1.5))
+    g = mixkf.MixtureKF(b, tt["pi"], tt["S0"])
+    g.set_theta(th0)
+    L0 = g.forward().item()
+    g.set_theta(th_true)
+    Ltrue = g.forward().item()
+    times = []
+    hist = []
+
+    def cb(it, th, tot):
+        if it % 10 == 0 or it == 1:
+            hist.append((it, float(tot.item())))
+
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    th, _ = g.fit_adam(th0, args.fit_steps, lr=args.fit_lr, callback=cb)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    thf = th.cpu().numpy()
+    g.set_theta(thf)
+    Lf = g.forward().item()
+    mu_f, a_f, L_f, s_f = mixkf.theta_split(thf, K, d)
+    mu_0 = mu0
+    err = lambda x, y: float(np.abs(x - y).mean())
+    Qt = np.einsum("kij,klj->kil", synth.unpack_lower(tt["Lq"], d), synth.unpack_lower(tt["Lq"], d))
+    Qf = np.einsum("kij,klj->kil", synth.unpack_lower(L_f, d), synth.unpack_lower(L_f, d))
+    Q0 = np.einsum("kij,klj->kil", synth.unpack_lower(Lq0, d), synth.unpack_lower(Lq0, d))
+    print(json.dumps({
+        "workload": "config 4: fit K=32, d=24 from B=%d x T=%d, %d Adam steps (lr %g) on the device"
+                    % (b.n_tracks, args.fit_frames, args.fit_steps, args.fit_lr),
+        "seconds_total": wall, "seconds_per_gradient_eval": wall / args.fit_steps,
+        "logL_init": L0, "logL_final": Lf, "logL_true_params": Ltrue, "logL_history": hist,
+        "recovery": {"mu_mae_init": err(mu_0, tt["mu"]), "mu_mae_final": err(mu_f, tt["mu"]),
+                     "a_mae_init": 0.0, "a_mae_final": err(a_f, tt["a"]),
+                     "Q_mae_init": err(Q0, Qt), "Q_mae_final": err(Qf, Qt),
+                     "sigma_init": float(th0[-1]), "sigma_final": s_f, "sigma_true": float(tt["sigma"])}}),
+          flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -336,11 +573,29 @@ def main():
     ap.add_argument("--plain-frames", type=int, default=300)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="batched", choices=["batched", "sweep", "plain0", "adjoint", "fit"])
+    ap.add_argument("--sweep-frames", type=int, default=200)
+    ap.add_argument("--adj-tracks", type=int, default=1024)
+    ap.add_argument("--adj-frames", type=int, default=1000)
+    ap.add_argument("--adj-check-tracks", type=int, default=8)
+    ap.add_argument("--fd-dirs", type=int, default=64)
+    ap.add_argument("--fit-tracks", type=int, default=16384)
+    ap.add_argument("--fit-frames", type=int, default=500)
+    ap.add_argument("--fit-steps", type=int, default=200)
+    ap.add_argument("--fit-lr", type=float, default=0.02)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "sweep":
+        run_sweep(args)
+    elif args.workload == "plain0":
+        run_plain0(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
+    elif args.workload == "fit":
+        run_fit(args)
     else:
         run_gb300(args)
 

@@ -39,14 +39,30 @@ __host__ __device__ inline int rec_W(int d) { return R_H + 6 * d; }
 __host__ __device__ inline int rec_X(int d) { return R_H + 8 * d; }
 __host__ __device__ inline int rec_Pin(int d) { return R_H + 9 * d; }
 
-struct CompLayout {   // per-component block inside a CTA slot (floats)
-  int rec0, xk, Pk, xb, Pb, Xin, Pin, Dkb, tmp, gmu, ga, gL, size;
+// Per-frame record block (floats): for each component its joint records, its
+// updated state (xk, Pk); then the frame's input state, mixture weights and
+// collapsed mean.  A backward segment keeps one block per frame.
+struct FrameLayout {
+  int comp_size, comp_xk, comp_Pk, xin, Pin, w, xo, size;
 };
-__host__ __device__ inline CompLayout comp_layout(int d, int J) {
-  CompLayout L;
+__host__ __device__ inline FrameLayout frame_layout(int d, int K, int J) {
+  FrameLayout L;
+  L.comp_xk = J * rec_size(d);
+  L.comp_Pk = L.comp_xk + d;
+  L.comp_size = (L.comp_Pk + d * d + 3) & ~3;
+  int o = K * L.comp_size;
+  L.xin = o; o += d; L.Pin = o; o += d * d;
+  L.w = o; o += 32; L.xo = o; o += d;
+  L.size = (o + 31) & ~31;
+  return L;
+}
+// Per-component adjoint work block (floats)
+struct WorkLayout {
+  int xb, Pb, Xin, Pin, Dkb, tmp, gmu, ga, gL, size;
+};
+__host__ __device__ inline WorkLayout work_layout(int d) {
+  WorkLayout L;
   int o = 0;
-  L.rec0 = o; o += J * rec_size(d);
-  L.xk = o; o += d; L.Pk = o; o += d * d;
   L.xb = o; o += d; L.Pb = o; o += d * d;
   L.Xin = o; o += d; L.Pin = o; o += d * d;
   L.Dkb = o; o += d;
@@ -87,16 +103,21 @@ __device__ __forceinline__ float wsum(float v) { return warp_sum(v); }
 
 // ---------------------------------------------------------------- forward pieces
 // sequential PDAF/EKF update of one joint for one component (whole warp)
+// R: this warp's scratch record (shared memory, R_H + 8d floats); x, P: the
+// component state (shared memory, updated in place); Rg: when non-null the
+// global record that keeps this update for the reverse sweep
+template <int D>
 __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const float* Bj, const float* mj,
-                           int n, const float2* z, float pd, float kappa, bool rec, int lane) {
-  const int d = M.d;
+                           int n, const float2* z, float pd, float kappa, float* Rg, int lane) {
+  constexpr int d = D;
   float* H = R + R_H;
   float* U = R + rec_U(d);
   float* Kg = R + rec_Kg(d);
   float* W = R + rec_W(d);
+  const bool rec = Rg != nullptr;
   if (rec) {
-    float* Rx = R + rec_X(d);
-    float* RP = R + rec_Pin(d);
+    float* Rx = Rg + rec_X(d);
+    float* RP = Rg + rec_Pin(d);
     for (int i = lane; i < d; i += 32) Rx[i] = x[i];
     for (int i = lane; i < d * d; i += 32) RP[i] = P[i];
   }
@@ -108,7 +129,7 @@ __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const 
   const float p0 = __shfl_sync(0xffffffffu, pt, 0), p1 = __shfl_sync(0xffffffffu, pt, 1),
               p2 = __shfl_sync(0xffffffffu, pt, 2);
   if (!(p2 > kMixZMin)) {
-    if (rec && lane == 0) R[R_VIS] = 0.0f;
+    if (rec && lane == 0) Rg[R_VIS] = 0.0f;
     __syncwarp();
     return logf(kappa);
   }
@@ -169,31 +190,33 @@ __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const 
     const int r = i / d, c = i - r * d;
     P[i] -= W[r * 2] * Kg[c * 2] + W[r * 2 + 1] * Kg[c * 2 + 1];
   }
-  if (rec) {
-    if (lane == 0) {
-      R[R_VIS] = 1.0f; R[R_N] = (float)n;
-      R[R_P3] = p0; R[R_P3 + 1] = p1; R[R_P3 + 2] = p2; R[R_IZ] = iz;
-      R[R_ZH] = zh0; R[R_ZH + 1] = zh1;
-      R[R_JP] = J00; R[R_JP + 1] = 0.0f; R[R_JP + 2] = J02; R[R_JP + 3] = 0.0f; R[R_JP + 4] = J11; R[R_JP + 5] = J12;
-      R[R_S] = S00; R[R_S + 1] = S01; R[R_S + 2] = S10; R[R_S + 3] = S11;
-      R[R_SI] = Si00; R[R_SI + 1] = Si01; R[R_SI + 2] = Si10; R[R_SI + 3] = Si11;
-      R[R_LD] = ld; R[R_ELL] = ell; R[R_B0] = beta0; R[R_NB] = nb0; R[R_NB + 1] = nb1;
-      R[R_M] = M00; R[R_M + 1] = M01; R[R_M + 2] = M10; R[R_M + 3] = M11;
-    }
-    if (lane < kMixMaxC) {
-      R[R_NU + 2 * lane] = n0; R[R_NU + 2 * lane + 1] = n1;
-      R[R_E + lane] = e; R[R_BETA + lane] = beta;
-    }
+  if (lane == 0) {
+    R[R_VIS] = 1.0f; R[R_N] = (float)n;
+    R[R_P3] = p0; R[R_P3 + 1] = p1; R[R_P3 + 2] = p2; R[R_IZ] = iz;
+    R[R_ZH] = zh0; R[R_ZH + 1] = zh1;
+    R[R_JP] = J00; R[R_JP + 1] = 0.0f; R[R_JP + 2] = J02; R[R_JP + 3] = 0.0f; R[R_JP + 4] = J11; R[R_JP + 5] = J12;
+    R[R_S] = S00; R[R_S + 1] = S01; R[R_S + 2] = S10; R[R_S + 3] = S11;
+    R[R_SI] = Si00; R[R_SI + 1] = Si01; R[R_SI + 2] = Si10; R[R_SI + 3] = Si11;
+    R[R_LD] = ld; R[R_ELL] = ell; R[R_B0] = beta0; R[R_NB] = nb0; R[R_NB + 1] = nb1;
+    R[R_M] = M00; R[R_M + 1] = M01; R[R_M + 2] = M10; R[R_M + 3] = M11;
   }
+  if (lane < kMixMaxC) {
+    R[R_NU + 2 * lane] = n0; R[R_NU + 2 * lane + 1] = n1;
+    R[R_E + lane] = e; R[R_BETA + lane] = beta;
+  }
+  __syncwarp();
+  if (rec)
+    for (int i = lane; i < rec_X(d); i += 32) Rg[i] = R[i];
   __syncwarp();
   return logf(ell);
 }
 
 // ---------------------------------------------------------------- reverse pieces
+template <int D>
 __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, float pd, float kappa, float* xb,
                           float* Pb, float gl, float* tmp, float& sb, int lane) {
   if (R[R_VIS] == 0.0f) return;
-  const int d = M.d;
+  constexpr int d = D;
   const int n = (int)R[R_N];
   const float* H = R + R_H;
   const float* U = R + rec_U(d);
@@ -340,38 +363,61 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
 }
 
 // ---------------------------------------------------------------- CTA-wide frame pieces
+constexpr int kDetBlock = 32;     // frames of detection lists prefetched at once
+
 struct Smem {
   float *xh, *Ph, *xo, *Po, *Xb, *Pb, *Pcb, *xt;
-  float2* det;
-  int* cnt;
+  float2* det;          // this frame's lists (points into dblk)
+  int* cnt;             // this frame's counts (points into dcnt)
+  float2* dblk;         // [kDetBlock][MKF_MAX_J][kMixMaxC]
+  int* dcnt;            // [kDetBlock][MKF_MAX_J]
   float *w, *l, *wb, *red;
   double* dred;
 };
 
-__device__ void load_frame_dets(const MixArgs& A, long long g, Smem& s, int tid, int TB) {
+// Prefetch the lists of frames g .. g+n-1 (n <= kDetBlock) into shared memory:
+// one coalesced pass instead of two dependent DRAM round trips per frame.
+__device__ void load_det_block(const MixArgs& A, long long g, int n, Smem& s, int tid, int TB) {
   const int J = A.M.J;
-  if (tid < J) {
-    int n = A.det_off[g * J + tid + 1] - A.det_off[g * J + tid];
-    if (n > kMixMaxC) { n = kMixMaxC; atomicOr(A.status, MKF_ST_TRUNC); }
-    s.cnt[tid] = n < 0 ? 0 : n;
+  __syncthreads();
+  for (int q = tid; q < n * J; q += TB) {
+    int c = A.det_off[g * J + q + 1] - A.det_off[g * J + q];
+    if (c > kMixMaxC) { c = kMixMaxC; atomicOr(A.status, MKF_ST_TRUNC); }
+    s.dcnt[(q / J) * MKF_MAX_J + (q % J)] = c < 0 ? 0 : c;
   }
   __syncthreads();
-  for (int q = tid; q < J * kMixMaxC; q += TB) {
-    const int j = q / kMixMaxC, i = q - j * kMixMaxC;
-    if (i < s.cnt[j]) s.det[j * kMixMaxC + i] = A.det[A.det_off[g * J + j] + i];
+  for (int q = tid; q < n * J * kMixMaxC; q += TB) {
+    const int f = q / (J * kMixMaxC), r = q - f * J * kMixMaxC, j = r / kMixMaxC, i = r - j * kMixMaxC;
+    if (i < s.dcnt[f * MKF_MAX_J + j])
+      s.dblk[(f * MKF_MAX_J + j) * kMixMaxC + i] = A.det[A.det_off[(g + f) * J + j] + i];
   }
   __syncthreads();
 }
 
-// one frame forward (all warps); returns c_t (valid in every thread)
-__device__ float frame_forward(const MixArgs& A, float* slot, const CompLayout& CL, const float* Bm,
-                               const float* mm, float pd, float kappa, Smem& s, bool rec) {
+__device__ __forceinline__ void select_frame_dets(Smem& s, int f) {
+  s.det = s.dblk + (size_t)f * MKF_MAX_J * kMixMaxC;
+  s.cnt = s.dcnt + f * MKF_MAX_J;
+}
+
+// per-warp shared scratch of the frame forward: xk (d), Pk (d*d), record (R_H + 8d)
+__host__ __device__ inline int fwd_scratch_floats(int d) { return (d + d * d + R_H + 8 * d + 3) & ~3; }
+
+// one frame forward (all warps); each warp's component lives in its shared
+// scratch (stride SR floats from scr); when frg is non-null the component
+// records and states are also kept in the global frame record frg.  Returns
+// c_t (valid in every thread); s.w, s.xo, s.Po hold the mixture weights and
+// the collapsed posterior
+template <int D>
+__device__ float frame_forward(const MixArgs& A, float* scr, int SR, float* frg, const FrameLayout& FL,
+                               const float* Bm, const float* mm, float pd, float kappa, Smem& s) {
   const MixDev& M = A.M;
-  const int d = M.d, K = M.K, J = M.J;
+  constexpr int d = D;
+  const int K = M.K, J = M.J;
   const int tid = threadIdx.x, TB = blockDim.x, lane = tid & 31, k = tid >> 5;
-  float* cb = slot + (size_t)k * CL.size;
-  float* xk = cb + CL.xk;
-  float* Pk = cb + CL.Pk;
+  float* xk = scr + (size_t)k * SR;
+  float* Pk = xk + d;
+  float* R = Pk + d * d;
+  float* cg = frg ? frg + (size_t)k * FL.comp_size : nullptr;
   const float* a = M.a + k * d;
   const float* mu = M.mu + k * d;
   if (lane < d) xk[lane] = fmaf(a[lane], s.xh[lane], (1.0f - a[lane]) * mu[lane]);
@@ -383,8 +429,12 @@ __device__ float frame_forward(const MixArgs& A, float* slot, const CompLayout& 
   __syncwarp();
   float ll = 0.0f;
   for (int j = 0; j < J; ++j)
-    ll += joint_fwd(M, cb + CL.rec0 + j * rec_size(d), xk, Pk, Bm + j * 3 * d, mm + j * 3, s.cnt[j],
-                    s.det + j * kMixMaxC, pd, kappa, rec, lane);
+    ll += joint_fwd<D>(M, R, xk, Pk, Bm + j * 3 * d, mm + j * 3, s.cnt[j], s.det + j * kMixMaxC, pd, kappa,
+                       cg ? cg + j * rec_size(d) : nullptr, lane);
+  if (cg) {
+    for (int i = lane; i < d; i += 32) cg[FL.comp_xk + i] = xk[i];
+    for (int i = lane; i < d * d; i += 32) cg[FL.comp_Pk + i] = Pk[i];
+  }
   if (lane == 0) s.l[k] = M.logpi[k] + ll;
   __syncthreads();
   if (k == 0) {
@@ -398,7 +448,8 @@ __device__ float frame_forward(const MixArgs& A, float* slot, const CompLayout& 
   __syncthreads();
   for (int r = tid; r < d; r += TB) {
     float v = 0.0f;
-    for (int q = 0; q < K; ++q) v = fmaf(s.w[q], slot[(size_t)q * CL.size + CL.xk + r], v);
+#pragma unroll 4
+    for (int q = 0; q < K; ++q) v = fmaf(s.w[q], scr[(size_t)q * SR + r], v);
     s.xo[r] = v;
   }
   __syncthreads();
@@ -406,10 +457,11 @@ __device__ float frame_forward(const MixArgs& A, float* slot, const CompLayout& 
     const int r = i / d, c = i - r * d;
     if (r > c) continue;
     float v = 0.0f;
+#pragma unroll 4
     for (int q = 0; q < K; ++q) {
-      const float* bq = slot + (size_t)q * CL.size;
-      const float Dr = bq[CL.xk + r] - s.xo[r], Dc = bq[CL.xk + c] - s.xo[c];
-      v = fmaf(s.w[q], 0.5f * (bq[CL.Pk + i] + bq[CL.Pk + c * d + r]) + Dr * Dc, v);
+      const float* bq = scr + (size_t)q * SR;
+      const float Dr = bq[r] - s.xo[r], Dc = bq[c] - s.xo[c];
+      v = fmaf(s.w[q], 0.5f * (bq[d + i] + bq[d + c * d + r]) + Dr * Dc, v);
     }
     s.Po[i] = v;
     s.Po[c * d + r] = v;
@@ -418,8 +470,10 @@ __device__ float frame_forward(const MixArgs& A, float* slot, const CompLayout& 
   return s.red[0];
 }
 
+template <int D>
 __device__ void prior_state(const MixDev& M, Smem& s, int tid, int TB) {
-  const int d = M.d, K = M.K;
+  constexpr int d = D;
+  const int K = M.K;
   for (int r = tid; r < d; r += TB) {
     float v = 0.0f;
     for (int k = 0; k < K; ++k) v = fmaf(M.pi[k], M.mu[k * d + r], v);
@@ -436,7 +490,7 @@ __device__ void prior_state(const MixDev& M, Smem& s, int tid, int TB) {
   __syncthreads();
 }
 
-__device__ void carve(Smem& s, float* base, int d) {
+__device__ float* carve(Smem& s, float* base, int d) {
   float* p = base;
   s.xh = p; p += d; s.Ph = p; p += d * d;
   s.xo = p; p += d; s.Po = p; p += d * d;
@@ -444,28 +498,37 @@ __device__ void carve(Smem& s, float* base, int d) {
   s.Pcb = p; p += d * d;
   s.xt = p; p += d;
   p = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(p) + 7) & ~uintptr_t(7));
-  s.det = reinterpret_cast<float2*>(p); p += 2 * kMixMaxC * MKF_MAX_J;
-  s.cnt = reinterpret_cast<int*>(p); p += 8;
+  s.dblk = reinterpret_cast<float2*>(p); p += 2 * kDetBlock * MKF_MAX_J * kMixMaxC;
+  s.dcnt = reinterpret_cast<int*>(p); p += kDetBlock * MKF_MAX_J;
+  s.det = s.dblk;
+  s.cnt = s.dcnt;
   s.w = p; p += 32; s.l = p; p += 32; s.wb = p; p += 32;
   s.red = p; p += 64;
   p = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(p) + 7) & ~uintptr_t(7));
   s.dred = reinterpret_cast<double*>(p);
+  p += 2 * 40;
+  return reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
 }
 
+// bytes of the shared state carved by carve() (an upper bound, 16-byte multiple)
 size_t mix_smem_bytes(int d) {
-  return sizeof(float) * (size_t)(4 * d + 4 * d * d + d + 2 * kMixMaxC * MKF_MAX_J + 8 + 32 * 3 + 64 + 8) +
-         sizeof(double) * 40 + 64;
+  size_t b = sizeof(float) * (size_t)(4 * d + 4 * d * d + d + 2 * kDetBlock * MKF_MAX_J * kMixMaxC +
+                                      kDetBlock * MKF_MAX_J + 32 * 3 + 64 + 8) +
+             sizeof(double) * 40 + 64;
+  return (b + 15) & ~size_t(15);
 }
 
 // ---------------------------------------------------------------- forward kernel
+template <int D>
 __global__ void __launch_bounds__(1024) mix_forward_kernel(MixArgs A) {
   extern __shared__ __align__(16) float msm[];
   Smem s;
-  carve(s, msm, A.M.d);
-  const int d = A.M.d, J = A.M.J;
+  float* scr = carve(s, msm, D);                 // per-warp component scratch follows
+  constexpr int d = D;
+  const int J = A.M.J;
   const int tid = threadIdx.x, TB = blockDim.x;
-  const CompLayout CL = comp_layout(d, J);
-  float* slot = A.slots + (size_t)blockIdx.x * A.slot_floats;
+  const FrameLayout FL = frame_layout(d, A.M.K, J);
+  const int SR = fwd_scratch_floats(d);
   for (int b = blockIdx.x; b < A.n_tracks; b += gridDim.x) {
     const int T = A.n_frames[b];
     const long long g0 = A.frame_base[b];
@@ -473,7 +536,7 @@ __global__ void __launch_bounds__(1024) mix_forward_kernel(MixArgs A) {
     const float* mm = A.mm + (size_t)b * J * 3;
     const float pd = A.pd[b], kappa = A.kappa[b];
     float* ck = A.ck + A.ck_off[b];
-    prior_state(A.M, s, tid, TB);
+    prior_state<D>(A.M, s, tid, TB);
     double L = 0.0;
     for (int t = 0; t < T; ++t) {
       if (t % A.C == 0) {
@@ -481,8 +544,9 @@ __global__ void __launch_bounds__(1024) mix_forward_kernel(MixArgs A) {
         for (int i = tid; i < d; i += TB) c[i] = s.xh[i];
         for (int i = tid; i < d * d; i += TB) c[d + i] = s.Ph[i];
       }
-      load_frame_dets(A, g0 + t, s, tid, TB);
-      L += (double)frame_forward(A, slot, CL, Bm, mm, pd, kappa, s, false);
+      if (t % kDetBlock == 0) load_det_block(A, g0 + t, min(kDetBlock, T - t), s, tid, TB);
+      select_frame_dets(s, t % kDetBlock);
+      L += (double)frame_forward<D>(A, scr, SR, nullptr, FL, Bm, mm, pd, kappa, s);
       for (int i = tid; i < d; i += TB) s.xh[i] = s.xo[i];
       for (int i = tid; i < d * d; i += TB) s.Ph[i] = s.Po[i];
       __syncthreads();
@@ -493,23 +557,34 @@ __global__ void __launch_bounds__(1024) mix_forward_kernel(MixArgs A) {
 }
 
 // ---------------------------------------------------------------- backward kernel
+// Per segment of C frames: recompute the frames from the segment's checkpoint
+// keeping every frame's records (one forward), then reverse them.
+// STAGE: the per-component adjoint work blocks live in shared memory (used
+// when they fit), so the fixed-order cross-component sums read shared memory;
+// otherwise they stay in the global slot.  Records always stay in the slot.
+template <int D, bool STAGE>
 __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
   extern __shared__ __align__(16) float msm[];
   Smem s;
-  carve(s, msm, A.M.d);
+  float* scr = carve(s, msm, D);
   const MixDev& M = A.M;
-  const int d = M.d, J = M.J, K = M.K, DD = M.DD;
+  constexpr int d = D, DD = D * (D + 1) / 2;
+  const int J = M.J, K = M.K;
   const int tid = threadIdx.x, TB = blockDim.x, lane = tid & 31, k = tid >> 5;
-  const CompLayout CL = comp_layout(d, J);
+  const FrameLayout FL = frame_layout(d, K, J);
+  const WorkLayout WL = work_layout(d);
+  const int SR = fwd_scratch_floats(d);
   float* slot = A.slots + (size_t)blockIdx.x * A.slot_floats;
-  float* seg = slot + (size_t)K * CL.size;                 // C states of d + d*d
+  float* frames = slot + (size_t)K * WL.size;               // C frame records
   double* gacc = A.gacc + (size_t)blockIdx.x * A.ng;       // mu, a, Lq, sigma
-  float* cb = slot + (size_t)k * CL.size;
+  float* wb = STAGE ? scr + (size_t)K * SR + (size_t)k * WL.size     // this component's work block
+                    : slot + (size_t)k * WL.size;
+  float* const wbase = STAGE ? scr + (size_t)K * SR : slot;
   const float* a = M.a + k * d;
   const float* mu = M.mu + k * d;
   const float* Lk = M.Lq + k * DD;
   float sbl = 0.0f;                                         // sigma adjoint, per lane
-  for (int i = lane; i < 2 * d + DD; i += 32) cb[CL.gmu + i] = 0.0f;
+  for (int i = lane; i < 2 * d + DD; i += 32) wb[WL.gmu + i] = 0.0f;
   for (int b = blockIdx.x; b < A.n_tracks; b += gridDim.x) {
     const int T = A.n_frames[b];
     const long long g0 = A.frame_base[b];
@@ -523,53 +598,61 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
     const int nck = (T + A.C - 1) / A.C;
     for (int sg = nck - 1; sg >= 0; --sg) {
       const int t0 = sg * A.C, t1 = min(T, t0 + A.C);
-      // recompute the segment's collapsed states from its checkpoint
+      // ---- recompute the segment from its checkpoint, keeping every frame's records
       const float* c0 = ck + (size_t)sg * (d + d * d);
-      for (int i = tid; i < d + d * d; i += TB) seg[i] = c0[i];
       for (int i = tid; i < d; i += TB) s.xh[i] = c0[i];
       for (int i = tid; i < d * d; i += TB) s.Ph[i] = c0[d + i];
       __syncthreads();
-      for (int t = t0; t < t1 - 1; ++t) {
-        load_frame_dets(A, g0 + t, s, tid, TB);
-        frame_forward(A, slot, CL, Bm, mm, pd, kappa, s, false);
-        float* st = seg + (size_t)(t - t0 + 1) * (d + d * d);
-        for (int i = tid; i < d; i += TB) { s.xh[i] = s.xo[i]; st[i] = s.xo[i]; }
-        for (int i = tid; i < d * d; i += TB) { s.Ph[i] = s.Po[i]; st[d + i] = s.Po[i]; }
+      for (int t = t0; t < t1; ++t) {
+        float* fr = frames + (size_t)(t - t0) * FL.size;
+        for (int i = tid; i < d; i += TB) fr[FL.xin + i] = s.xh[i];
+        for (int i = tid; i < d * d; i += TB) fr[FL.Pin + i] = s.Ph[i];
+        if ((t - t0) % kDetBlock == 0) load_det_block(A, g0 + t, min(kDetBlock, t1 - t), s, tid, TB);
+        select_frame_dets(s, (t - t0) % kDetBlock);
+        frame_forward<D>(A, scr, SR, fr, FL, Bm, mm, pd, kappa, s);
+        for (int i = tid; i < K; i += TB) fr[FL.w + i] = s.w[i];
+        for (int i = tid; i < d; i += TB) { fr[FL.xo + i] = s.xo[i]; s.xh[i] = s.xo[i]; }
+        for (int i = tid; i < d * d; i += TB) s.Ph[i] = s.Po[i];
         __syncthreads();
       }
-      // reverse the segment
+      // ---- reverse the segment
       for (int t = t1 - 1; t >= t0; --t) {
-        const float* st = seg + (size_t)(t - t0) * (d + d * d);
-        for (int i = tid; i < d; i += TB) s.xh[i] = st[i];
-        for (int i = tid; i < d * d; i += TB) s.Ph[i] = st[d + i];
-        load_frame_dets(A, g0 + t, s, tid, TB);
-        frame_forward(A, slot, CL, Bm, mm, pd, kappa, s, true);
+        const float* fr = frames + (size_t)(t - t0) * FL.size;
+        // stage the frame's input state, mixture weights and collapsed mean
+        for (int i = tid; i < d; i += TB) { s.xh[i] = fr[FL.xin + i]; s.xo[i] = fr[FL.xo + i]; }
+        for (int i = tid; i < d * d; i += TB) s.Ph[i] = fr[FL.Pin + i];
+        for (int i = tid; i < K; i += TB) s.w[i] = fr[FL.w + i];
+        const float* cb = fr + (size_t)k * FL.comp_size;
+        const float* xin = s.xh;
+        const float* Pin = s.Ph;
+        const float* xo = s.xo;
+        const float* xk = cb + FL.comp_xk;
+        const float* Pk = cb + FL.comp_Pk;
+        const float wk = fr[FL.w + k];
         // collapse reverse: P' = sym(sum w (P_k + D D^T)), x' = sum w x_k, softmax (dc = 1)
         for (int i = tid; i < d * d; i += TB) {
           const int r = i / d, c = i - r * d;
           s.Pcb[i] = 0.5f * (s.Pb[i] + s.Pb[c * d + r]);
         }
         __syncthreads();
-        const float wk = s.w[k];
-        float* xk = cb + CL.xk;
-        float* Pk = cb + CL.Pk;
-        float* Dkb = cb + CL.Dkb;
+        float* Dkb = wb + WL.Dkb;
         if (lane < d) {
           float v = 0.0f;
-          for (int c = 0; c < d; ++c) v = fmaf(s.Pcb[lane * d + c], xk[c] - s.xo[c], v);
+          for (int c = 0; c < d; ++c) v = fmaf(s.Pcb[lane * d + c], xk[c] - xo[c], v);
           Dkb[lane] = 2.0f * wk * v;
         }
         __syncthreads();
         for (int r = tid; r < d; r += TB) {
           float v = s.Xb[r];
-          for (int q = 0; q < K; ++q) v -= slot[(size_t)q * CL.size + CL.Dkb + r];
+#pragma unroll 4
+          for (int q = 0; q < K; ++q) v -= wbase[(size_t)q * WL.size + WL.Dkb + r];
           s.xt[r] = v;
         }
         __syncthreads();
         float wbp = (lane < d) ? xk[lane] * s.xt[lane] : 0.0f;
         for (int i = lane; i < d * d; i += 32) {
           const int r = i / d, c = i - r * d;
-          wbp = fmaf(s.Pcb[i], Pk[i] + (xk[r] - s.xo[r]) * (xk[c] - s.xo[c]), wbp);
+          wbp = fmaf(s.Pcb[i], Pk[i] + (xk[r] - xo[r]) * (xk[c] - xo[c]), wbp);
         }
         const float wbk = wsum(wbp);
         if (lane == 0) s.wb[k] = wbk;
@@ -581,31 +664,31 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
         }
         __syncthreads();
         const float lb = wk * (wbk - s.red[1]) + wk;
-        float* xb = cb + CL.xb;
-        float* Pb = cb + CL.Pb;
-        float* Xin = cb + CL.Xin;
-        float* Pin = cb + CL.Pin;
+        float* xb = wb + WL.xb;
+        float* Pb = wb + WL.Pb;
+        float* Xin = wb + WL.Xin;
+        float* Pinb = wb + WL.Pin;
         if (wk > 0.0f) {
           if (lane < d) xb[lane] = Dkb[lane] + wk * s.xt[lane];
           for (int i = lane; i < d * d; i += 32) Pb[i] = wk * s.Pcb[i];
           __syncwarp();
           for (int j = J - 1; j >= 0; --j)
-            joint_bwd(M, cb + CL.rec0 + j * rec_size(d), Bm + j * 3 * d, pd, kappa, xb, Pb, lb, cb + CL.tmp, sbl, lane);
-          // predict reverse: x = a*xh + (1-a)*mu ; P = A Ph A + Q
-          float* gmu = cb + CL.gmu;
-          float* ga = cb + CL.ga;
-          float* gL = cb + CL.gL;
+            joint_bwd<D>(M, cb + j * rec_size(d), Bm + j * 3 * d, pd, kappa, xb, Pb, lb, wb + WL.tmp, sbl, lane);
+          // predict reverse: x = a*xin + (1-a)*mu ; P = A Pin A + Q
+          float* gmu = wb + WL.gmu;
+          float* ga = wb + WL.ga;
+          float* gL = wb + WL.gL;
           if (lane < d) {
             Xin[lane] = a[lane] * xb[lane];
             gmu[lane] += (1.0f - a[lane]) * xb[lane];
-            float g = (s.xh[lane] - mu[lane]) * xb[lane];
+            float g = (xin[lane] - mu[lane]) * xb[lane];
             for (int c = 0; c < d; ++c)
-              g += (Pb[lane * d + c] * s.Ph[lane * d + c] + Pb[c * d + lane] * s.Ph[c * d + lane]) * a[c];
+              g += (Pb[lane * d + c] * Pin[lane * d + c] + Pb[c * d + lane] * Pin[c * d + lane]) * a[c];
             ga[lane] += g;
           }
           for (int i = lane; i < d * d; i += 32) {
             const int r = i / d, c = i - r * d;
-            Pin[i] = a[r] * a[c] * Pb[i];
+            Pinb[i] = a[r] * a[c] * Pb[i];
           }
           for (int i = lane; i < DD; i += 32) {
             int r = (int)((sqrtf(8.0f * i + 1.0f) - 1.0f) * 0.5f);
@@ -618,28 +701,30 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
           }
         } else {
           if (lane < d) Xin[lane] = 0.0f;
-          for (int i = lane; i < d * d; i += 32) Pin[i] = 0.0f;
+          for (int i = lane; i < d * d; i += 32) Pinb[i] = 0.0f;
         }
         __syncthreads();
         for (int r = tid; r < d; r += TB) {
           float v = 0.0f;
-          for (int q = 0; q < K; ++q) v += slot[(size_t)q * CL.size + CL.Xin + r];
+#pragma unroll 4
+          for (int q = 0; q < K; ++q) v += wbase[(size_t)q * WL.size + WL.Xin + r];
           s.Xb[r] = v;
         }
         for (int i = tid; i < d * d; i += TB) {
           float v = 0.0f;
-          for (int q = 0; q < K; ++q) v += slot[(size_t)q * CL.size + CL.Pin + i];
+#pragma unroll 4
+          for (int q = 0; q < K; ++q) v += wbase[(size_t)q * WL.size + WL.Pin + i];
           s.Pb[i] = v;
         }
         __syncthreads();
       }
       // flush this segment's FP32 parameter adjoints into the CTA's FP64 accumulators
       for (int i = lane; i < d; i += 32) {
-        gacc[k * d + i] += (double)cb[CL.gmu + i];
-        gacc[K * d + k * d + i] += (double)cb[CL.ga + i];
+        gacc[k * d + i] += (double)wb[WL.gmu + i];
+        gacc[K * d + k * d + i] += (double)wb[WL.ga + i];
       }
-      for (int i = lane; i < DD; i += 32) gacc[2 * K * d + k * DD + i] += (double)cb[CL.gL + i];
-      for (int i = lane; i < 2 * d + DD; i += 32) cb[CL.gmu + i] = 0.0f;
+      for (int i = lane; i < DD; i += 32) gacc[2 * K * d + k * DD + i] += (double)wb[WL.gL + i];
+      for (int i = lane; i < 2 * d + DD; i += 32) wb[WL.gmu + i] = 0.0f;
       __syncthreads();
     }
     // prior: x = sum pi mu, P = sum pi (S0 + D D^T)
@@ -652,16 +737,16 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
     if (lane < d) {
       float v = 0.0f;
       for (int c = 0; c < d; ++c) v = fmaf(s.Pb[lane * d + c] + s.Pb[c * d + lane], mu[c] - s.xh[c], v);
-      cb[CL.Dkb + lane] = M.pi[k] * v;
+      wb[WL.Dkb + lane] = M.pi[k] * v;
     }
     __syncthreads();
     for (int r = tid; r < d; r += TB) {
       float v = s.Xb[r];
-      for (int q = 0; q < K; ++q) v -= slot[(size_t)q * CL.size + CL.Dkb + r];
+      for (int q = 0; q < K; ++q) v -= wbase[(size_t)q * WL.size + WL.Dkb + r];
       s.xt[r] = v;
     }
     __syncthreads();
-    if (lane < d) gacc[k * d + lane] += (double)(cb[CL.Dkb + lane] + M.pi[k] * s.xt[lane]);
+    if (lane < d) gacc[k * d + lane] += (double)(wb[WL.Dkb + lane] + M.pi[k] * s.xt[lane]);
     __syncthreads();
   }
   // sigma: per-warp lane 0 partials, fixed-order sum
@@ -746,15 +831,44 @@ struct mkf_mixkf {
   int* status;
   double fx, fy, cx, cy;
   bool have_theta;
+  bool stage;
+  size_t smem_f, smem_b;
 };
 
+template <typename KF>
+static int mix_occ(KF kern, int tpb, size_t smem, int* occ) {
+  MKF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  MKF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, tpb, smem));
+  return MKF_OK;
+}
+
+// shared-memory sizes, STAGE choice and the persistent grid
 static int mix_grid(mkf_mixkf* h) {
-  const size_t smem = mix_smem_bytes(h->d);
-  int occ = 0;
-  MKF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, mix_backward_kernel, h->tpb, smem));
-  int occ2 = 0;
-  MKF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, mix_forward_kernel, h->tpb, smem));
-  occ = std::max(1, std::min(occ, occ2));
+  const int d = h->d, K = h->K;
+  const FrameLayout FL = frame_layout(d, K, h->J);
+  const WorkLayout WL = work_layout(d);
+  const size_t base = mix_smem_bytes(d);
+  const int SRf = fwd_scratch_floats(d);
+  h->smem_f = base + sizeof(float) * (size_t)K * SRf;
+  const size_t smem_stage = base + sizeof(float) * (size_t)K * (SRf + WL.size);
+  int dev = 0, optin = 0;
+  MKF_CUDA(cudaGetDevice(&dev));
+  MKF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  h->stage = smem_stage <= (size_t)optin;
+  h->smem_b = h->stage ? smem_stage : h->smem_f;
+  if (h->smem_f > (size_t)optin) { set_error("mkf_mixkf: model too large for shared memory"); return MKF_ERR_ARG; }
+  int of = 0, ob = 0, st;
+  if (d == 12) {
+    if ((st = mix_occ(mix_forward_kernel<12>, h->tpb, h->smem_f, &of))) return st;
+    st = h->stage ? mix_occ(mix_backward_kernel<12, true>, h->tpb, h->smem_b, &ob)
+                  : mix_occ(mix_backward_kernel<12, false>, h->tpb, h->smem_b, &ob);
+  } else {
+    if ((st = mix_occ(mix_forward_kernel<24>, h->tpb, h->smem_f, &of))) return st;
+    st = h->stage ? mix_occ(mix_backward_kernel<24, true>, h->tpb, h->smem_b, &ob)
+                  : mix_occ(mix_backward_kernel<24, false>, h->tpb, h->smem_b, &ob);
+  }
+  if (st) return st;
+  const int occ = std::max(1, std::min(of, ob));
   h->grid = std::min(h->n_tracks, num_sms() * occ);
   return MKF_OK;
 }
@@ -831,8 +945,9 @@ extern "C" int mkf_mixkf_create(const mkf_mix_model* model, int n_tracks, const 
   }
   int st = mix_grid(h);
   if (st) { mkf_mixkf_destroy(h); return st; }
-  const CompLayout CL = comp_layout(d, J);
-  h->slot_floats = ((long long)K * CL.size + (long long)h->C * (d + d * d) + 63) & ~63LL;
+  const FrameLayout FL = frame_layout(d, K, J);
+  const WorkLayout WL = work_layout(d);
+  h->slot_floats = ((long long)K * WL.size + (long long)h->C * FL.size + 63) & ~63LL;
   e = cudaMalloc(&h->slots, sizeof(float) * (size_t)h->slot_floats * h->grid);
   if (e == cudaSuccess) e = cudaMalloc(&h->gacc, sizeof(double) * (size_t)h->ng * h->grid);
   if (e != cudaSuccess) {
@@ -885,8 +1000,8 @@ extern "C" int mkf_mixkf_forward(mkf_mixkf_t h, const int* d_det_off, const floa
   if (!h->have_theta) { set_error("mkf_mixkf_forward: set theta first"); return MKF_ERR_STATE; }
   cudaStream_t s = (cudaStream_t)stream;
   MixArgs A = mix_args(h, d_det_off, d_det);
-  const size_t smem = mix_smem_bytes(h->d);
-  mix_forward_kernel<<<h->grid, h->tpb, smem, s>>>(A);
+  if (h->d == 12) mix_forward_kernel<12><<<h->grid, h->tpb, h->smem_f, s>>>(A);
+  else mix_forward_kernel<24><<<h->grid, h->tpb, h->smem_f, s>>>(A);
   MKF_CHECK_LAUNCH("mkf_mixkf_forward");
   if (d_loglik) MKF_CUDA(cudaMemcpyAsync(d_loglik, h->ll, sizeof(double) * h->n_tracks, cudaMemcpyDeviceToDevice, s));
   mix_total_kernel<<<1, 256, 0, s>>>(h->ll, h->n_tracks, d_total ? d_total : h->total);
@@ -901,8 +1016,13 @@ extern "C" int mkf_mixkf_backward(mkf_mixkf_t h, const int* d_det_off, const flo
   cudaStream_t s = (cudaStream_t)stream;
   MixArgs A = mix_args(h, d_det_off, d_det);
   MKF_CUDA(cudaMemsetAsync(h->gacc, 0, sizeof(double) * (size_t)h->ng * h->grid, s));
-  const size_t smem = mix_smem_bytes(h->d);
-  mix_backward_kernel<<<h->grid, h->tpb, smem, s>>>(A);
+  if (h->d == 12) {
+    if (h->stage) mix_backward_kernel<12, true><<<h->grid, h->tpb, h->smem_b, s>>>(A);
+    else mix_backward_kernel<12, false><<<h->grid, h->tpb, h->smem_b, s>>>(A);
+  } else {
+    if (h->stage) mix_backward_kernel<24, true><<<h->grid, h->tpb, h->smem_b, s>>>(A);
+    else mix_backward_kernel<24, false><<<h->grid, h->tpb, h->smem_b, s>>>(A);
+  }
   MKF_CHECK_LAUNCH("mkf_mixkf_backward");
   mix_reduce_kernel<<<(h->ng + 255) / 256, 256, 0, s>>>(h->gacc, h->grid, h->ng, d_grad);
   MKF_CHECK_LAUNCH("mkf_mixkf_backward: reduce");
