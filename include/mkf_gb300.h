@@ -88,6 +88,18 @@ int mkf_resample_f64(const double* d_w, int L, int N, uint32_t U, int* d_idx,
                      int* d_fallback, mkf_stream_t stream);
 int mkf_resample_f32(const float* d_w, int L, int N, uint32_t U, int* d_idx,
                      int* d_fallback, mkf_stream_t stream);
+/* Allocation-free variant of mkf_resample_f32 (no counterpart in the reference,
+ * whose resampler is host code).  For callers that must not allocate device
+ * memory, e.g. a per-frame loop that cannot afford cudaMalloc's implicit device
+ * synchronisation or an application that budgets its device memory up front:
+ * the scratch is a fixed array inside the library (about 2 KB per GPU, held
+ * until exit), so L must not exceed 1048576 weights (MKF_ERR_ARG otherwise).
+ * The first call on each device looks up the array's device address, so make
+ * that first call before any stream capture.  All calls share the one array:
+ * calls that can overlap on the GPU (different streams) race and must be
+ * serialised by the caller. */
+int mkf_resample_f32_noalloc(const float* d_w, int L, int N, uint32_t U, int* d_idx,
+                             int* d_fallback, mkf_stream_t stream);
 
 /* ------------------------------------------- A1/A13 mixture-of-MRRW motion model */
 /* Stacked per-model arrays (leading dimension n_models), all host pointers.

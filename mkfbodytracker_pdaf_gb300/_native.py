@@ -54,6 +54,7 @@ SIGNATURES = {
     "mkf_draw_particles": (I, [U64, U32, U32, I, I, P, P, P]),
     "mkf_resample_f64": (I, [P, I, I, U32, P, P, P]),
     "mkf_resample_f32": (I, [P, I, I, U32, P, P, P]),
+    "mkf_resample_f32_noalloc": (I, [P, I, I, U32, P, P, P]),
     "mkf_bpf_create": (I, [C.POINTER(BpfModels), C.POINTER(BpfTrack), C.POINTER(P)]),
     "mkf_bpf_reset": (I, [P, P]),
     "mkf_bpf_update": (I, [P, U32, P, P, P, P, P, P]),

@@ -274,3 +274,71 @@ extern "C" int mkf_resample_f32(const float* d_w, int L, int N, uint32_t U, int*
                                 mkf_stream_t stream) {
   return resample_impl<float>(d_w, L, N, U, d_idx, d_fallback, (cudaStream_t)stream);
 }
+
+// ------------------------------------------------------------------ allocation-free resampler
+// mkf_resample_f32_noalloc: the same exact systematic resampler as
+// mkf_resample_f32, for callers that must not allocate device memory -- for
+// example a per-frame tracking loop with a hard latency budget (cudaMalloc and
+// cudaFree can synchronise the whole device) or an application that budgets
+// all of its device memory up front.  Its scratch (per-block integer sums and
+// four control words) lives in the fixed file-scope array below, sized for at
+// most kNoAllocMaxWeights weights; every GPU that loads this library holds the
+// array until the process exits.
+namespace mkf {
+
+constexpr int kNoAllocMaxWeights = 1 << 20;
+constexpr int kNoAllocMaxBlocks = kNoAllocMaxWeights / kRsTile;      // 256 weight tiles
+// [0] max-weight bits, [1] +inf flag, [2] ticket (as two u32), [3] total, then block sums
+static __device__ __align__(256) unsigned long long g_resample_noalloc_scratch[4 + kNoAllocMaxBlocks];
+
+static std::mutex g_noalloc_mu;
+static unsigned long long* g_noalloc_ptr[64];
+
+// Host code cannot use the array's name as a device address, so the address is
+// looked up once per device (with that device current) on its first call.
+static int noalloc_scratch(unsigned long long** out) {
+  int dev = 0;
+  MKF_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) { set_error("mkf_resample_f32_noalloc: device index out of range"); return MKF_ERR_ARG; }
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_resample_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "mkf_resample_f32_noalloc: cudaGetSymbolAddress", __FILE__, __LINE__);
+    g_noalloc_ptr[dev] = static_cast<unsigned long long*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return MKF_OK;
+}
+
+}  // namespace mkf
+
+extern "C" int mkf_resample_f32_noalloc(const float* d_w, int L, int N, uint32_t U, int* d_idx,
+                                        int* d_fallback, mkf_stream_t stream) {
+  MKF_ARG(d_w && d_idx, "mkf_resample_f32_noalloc: null pointer");
+  if (L < 1 || L > kNoAllocMaxWeights) {
+    set_error("mkf_resample_f32_noalloc: L must be in [1, 1048576] (the fixed scratch holds 256 tiles "
+              "of 4096 weights); use mkf_resample_f32 for larger inputs");
+    return MKF_ERR_ARG;
+  }
+  MKF_ARG(N >= 1 && N <= (1 << 23), "mkf_resample_f32_noalloc: N must be in [1, 2^23]");
+  unsigned long long* sc = nullptr;
+  int st = noalloc_scratch(&sc);
+  if (st) return st;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nb = (L + kRsTile - 1) / kRsTile;
+  // the max bits, the +inf flag and the ticket must start at zero on every call
+  MKF_CUDA(cudaMemsetAsync(sc, 0, sizeof(unsigned long long) * 4, s));
+  unsigned long long* wm = sc;
+  unsigned int* ticket = reinterpret_cast<unsigned int*>(sc + 2);
+  unsigned long long* qt = sc + 3;
+  unsigned long long* bsum = sc + 4;
+  const int g1 = std::min(std::max(1, (L + kRsTB - 1) / kRsTB), 4 * num_sms());
+  rs_max<float><<<g1, kRsTB, 0, s>>>(d_w, L, wm);
+  MKF_CHECK_LAUNCH("mkf_resample_f32_noalloc: max kernel");
+  rs_sum<float><<<nb, kRsTB, 0, s>>>(d_w, L, wm, bsum, ticket, qt);
+  MKF_CHECK_LAUNCH("mkf_resample_f32_noalloc: sum kernel");
+  rs_search<float><<<nb, kRsTB, 0, s>>>(d_w, L, N, U, wm, bsum, qt, d_idx, d_fallback);
+  MKF_CHECK_LAUNCH("mkf_resample_f32_noalloc: search kernel");
+  return MKF_OK;
+}
