@@ -212,11 +212,12 @@ def run_gb300(args):
     from mkfbodytracker_pdaf_gb300.filters import BatchedBootstrapPF
 
     from mkfbodytracker_pdaf_gb300.autotune import load_tuning
-    tb, cps = load_tuning()
+    tb, cps, var = load_tuning()
     tb = args.block_threads or tb
     cps = cps if args.ctas_per_sm is None else args.ctas_per_sm
+    var = var if args.variant is None else args.variant
     batch = workload(rank, args.tracks)
-    runner = BatchedBootstrapPF(batch, block_threads=tb, ctas_per_sm=cps)
+    runner = BatchedBootstrapPF(batch, block_threads=tb, ctas_per_sm=cps, variant=var)
     det_off, det = runner.device_inputs()
     outs = runner.alloc_outputs()
     stream = torch.cuda.current_stream()
@@ -295,6 +296,7 @@ def run_gb300(args):
                        "particle_frames_per_gpu": PF,
                        "l2": "inputs larger than L2 (%.2f GB of detections per step)" % (h2d / 1e9),
                        "block_threads": runner.block_threads, "ctas_per_sm": runner.ctas_per_sm,
+                       "variant": runner.variant,
                        "parallelism": "one persistent kernel per GPU; tracks sharded by rank"},
             "e2e": {"value": G * ws / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
@@ -567,6 +569,7 @@ def main():
     ap.add_argument("--tracks", type=int, default=8192)
     ap.add_argument("--block-threads", type=int, default=None, help="default: autotuned choice")
     ap.add_argument("--ctas-per-sm", type=int, default=None)
+    ap.add_argument("--variant", type=int, default=None, help="bit 0 float4 loads, bit 1 binary-search resampling")
     ap.add_argument("--cpu-sample-tracks", type=int, default=24)
     ap.add_argument("--ref-sample-tracks", type=int, default=16)
     ap.add_argument("--plain-tracks", type=int, default=8)

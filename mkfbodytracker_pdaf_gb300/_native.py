@@ -64,6 +64,7 @@ SIGNATURES = {
     "mkf_bpf_destroy": (I, [P]),
     "mkf_bpf_batch_create": (I, [C.POINTER(BpfModels), I, P, I64, C.POINTER(P)]),
     "mkf_bpf_batch_set_tuning": (I, [P, I, I]),
+    "mkf_bpf_batch_set_variant": (I, [P, I]),
     "mkf_bpf_batch_run": (I, [P, P, P, P, P, P, P, P]),
     "mkf_bpf_batch_run_host": (I, [P, P, P, I64, P, P, P, P, P]),
     "mkf_bpf_batch_set_debug": (I, [P, I, P, P]),

@@ -1,12 +1,15 @@
 """Autotuner for the batched persistent kernel: block size (and so particles
-per thread, ceil(N / block)) and resident CTAs per SM.
+per thread, ceil(N / block)), resident CTAs per SM, and the kernel's code
+variants (float4 vs scalar model loads; ancestors by binary search vs the
+scatter walk).
 
 Run on the target GPU:
-    python -m mkfbodytracker_pdaf_gb300.autotune --tracks 2048 --out tuning.json
-It times every candidate on a seeded subset of the batched-uneven-tracks
-workload (same distributions as the full batch) with CUDA events and writes
-the ranking; ``load_tuning()`` returns the stored best choice (used by the
-benchmark and the runners when present).
+    python -m mkfbodytracker_pdaf_gb300.autotune --tracks 8192 --out tuning.json
+It times every candidate on the batched-uneven-tracks workload with CUDA
+events and writes the ranking; ``load_tuning()`` returns the stored best
+choice (used by the benchmark and the runners when present).  Tune at the
+full batch size: with few tracks per CTA the tail of the schedule dominates and
+the ranking changes.
 """
 from __future__ import annotations
 
@@ -19,18 +22,21 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 TUNING_FILE = os.path.join(HERE, "tuning_gb300.json")
 # (block_threads, ctas_per_sm): 512x1 and 256x2 compile with a 128-register
 # budget, 256x3 with an 80-register budget (3 CTAs of 71 KB shared memory each)
-CANDIDATES = [(256, 2), (256, 3), (512, 1), (128, 3)]
+SHAPES = [(256, 2), (256, 3), (512, 1)]
+VARIANTS = [0, 1, 2, 3]          # bit 0: float4 model loads, bit 1: binary-search resampling
+CANDIDATES = [(tb, cps, v) for (tb, cps) in SHAPES for v in VARIANTS]
 
 
 def load_tuning():
     if os.path.exists(TUNING_FILE):
         with open(TUNING_FILE) as f:
             d = json.load(f)
-        return int(d["best"]["block_threads"]), int(d["best"]["ctas_per_sm"])
-    return 256, 2
+        b = d["best"]
+        return int(b["block_threads"]), int(b["ctas_per_sm"]), int(b.get("variant", 1))
+    return 256, 3, 1
 
 
-def tune(n_tracks=2048, reps=3, seed=None):
+def tune(n_tracks=8192, reps=2, seed=None):
     import torch
     from . import build, synth
     from .filters import BatchedBootstrapPF
@@ -42,9 +48,9 @@ def tune(n_tracks=2048, reps=3, seed=None):
     outs = runner.alloc_outputs()
     G = batch.n_frames_total
     res = []
-    for tb, cps in CANDIDATES:
+    for tb, cps, var in CANDIDATES:
         try:
-            runner.set_tuning(tb, cps)
+            runner.set_tuning(tb, cps, var)
             runner.run(det_off, det, outs)
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -54,9 +60,10 @@ def tune(n_tracks=2048, reps=3, seed=None):
             e1.record()
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1) / reps
-            res.append({"block_threads": tb, "ctas_per_sm": cps, "ms": ms, "track_frames_per_s": G / ms * 1e3})
+            res.append({"block_threads": tb, "ctas_per_sm": cps, "variant": var, "ms": ms,
+                        "track_frames_per_s": G / ms * 1e3})
         except Exception as ex:  # a shape that does not fit is reported, not fatal
-            res.append({"block_threads": tb, "ctas_per_sm": cps, "error": str(ex)})
+            res.append({"block_threads": tb, "ctas_per_sm": cps, "variant": var, "error": str(ex)})
     ok = [r for r in res if "ms" in r]
     best = min(ok, key=lambda r: r["ms"])
     return {"workload": "batched uneven tracks subset: %d tracks, %d track-frames" % (n_tracks, G),
@@ -66,8 +73,8 @@ def tune(n_tracks=2048, reps=3, seed=None):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--tracks", type=int, default=2048)
-    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--tracks", type=int, default=8192)
+    ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--out", default=TUNING_FILE)
     a = ap.parse_args()
     r = tune(a.tracks, a.reps)

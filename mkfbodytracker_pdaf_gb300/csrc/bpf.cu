@@ -116,8 +116,9 @@ __device__ __forceinline__ void prior_sample(const PView& p, const float* eps, f
 
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 
-// x' = A_k x + (I - A_k) mu_k + L_k eps  (rows of a, mb, Ld, Bm are 16-byte aligned: D % 4 == 0)
-template <int D, bool DIAG>
+// x' = A_k x + (I - A_k) mu_k + L_k eps.  VEC: float4 parameter loads (rows of
+// a, mb, Ld, Bm are 16-byte aligned since D % 4 == 0); otherwise scalar loads.
+template <int D, bool DIAG, bool VEC = true>
 __device__ __forceinline__ void propagate(const PView& p, const float* eps, float uc, float* x) {
   constexpr int DD = D * (D + 1) / 2;
   int k = pick_component(p.cumpi, p.K, uc);
@@ -125,13 +126,18 @@ __device__ __forceinline__ void propagate(const PView& p, const float* eps, floa
   const float* mb = p.mb + k * D;
   if (DIAG) {
     const float* l = p.Ld + k * D;
+    if (VEC) {
 #pragma unroll
-    for (int r = 0; r < D; r += 4) {
-      float4 av = ld4(a + r), mv = ld4(mb + r), lv = ld4(l + r);
-      x[r + 0] = fmaf(lv.x, eps[r + 0], fmaf(av.x, x[r + 0], mv.x));
-      x[r + 1] = fmaf(lv.y, eps[r + 1], fmaf(av.y, x[r + 1], mv.y));
-      x[r + 2] = fmaf(lv.z, eps[r + 2], fmaf(av.z, x[r + 2], mv.z));
-      x[r + 3] = fmaf(lv.w, eps[r + 3], fmaf(av.w, x[r + 3], mv.w));
+      for (int r = 0; r < D; r += 4) {
+        float4 av = ld4(a + r), mv = ld4(mb + r), lv = ld4(l + r);
+        x[r + 0] = fmaf(lv.x, eps[r + 0], fmaf(av.x, x[r + 0], mv.x));
+        x[r + 1] = fmaf(lv.y, eps[r + 1], fmaf(av.y, x[r + 1], mv.y));
+        x[r + 2] = fmaf(lv.z, eps[r + 2], fmaf(av.z, x[r + 2], mv.z));
+        x[r + 3] = fmaf(lv.w, eps[r + 3], fmaf(av.w, x[r + 3], mv.w));
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < D; ++r) x[r] = fmaf(l[r], eps[r], fmaf(a[r], x[r], mb[r]));
     }
   } else {
     const float* L = p.Lq + k * DD;
@@ -149,7 +155,7 @@ __device__ __forceinline__ void propagate(const PView& p, const float* eps, floa
 }
 
 // log[(1-P_D) kappa + P_D sum_i N(z_i; pi(x), sigma^2 I)] summed over measured joints
-template <int D>
+template <int D, bool VEC = true>
 __device__ __forceinline__ float loglik(const PView& p, const float* x, const int* cnt,
                                         const float2* det, float kappa, float pd, float sigma) {
   const float inv2s2 = 0.5f / (sigma * sigma);
@@ -158,20 +164,31 @@ __device__ __forceinline__ float loglik(const PView& p, const float* x, const in
   float ll = 0.0f;
   for (int j = 0; j < p.J; ++j) {
     const float* B = p.Bm + j * 3 * D;
-    // two partial sums per row shorten the dependent FMA chains
-    float q0a = p.mm[j * 3 + 0], q1a = p.mm[j * 3 + 1], q2a = p.mm[j * 3 + 2];
-    float q0b = 0.0f, q1b = 0.0f, q2b = 0.0f;
+    float q0, q1, q2;
+    if (VEC) {
+      // two partial sums per row shorten the dependent FMA chains
+      float q0a = p.mm[j * 3 + 0], q1a = p.mm[j * 3 + 1], q2a = p.mm[j * 3 + 2];
+      float q0b = 0.0f, q1b = 0.0f, q2b = 0.0f;
 #pragma unroll
-    for (int c = 0; c < D; c += 4) {
-      float4 b0 = ld4(B + c), b1 = ld4(B + D + c), b2 = ld4(B + 2 * D + c);
-      q0a = fmaf(b0.x, x[c], q0a); q0b = fmaf(b0.y, x[c + 1], q0b);
-      q1a = fmaf(b1.x, x[c], q1a); q1b = fmaf(b1.y, x[c + 1], q1b);
-      q2a = fmaf(b2.x, x[c], q2a); q2b = fmaf(b2.y, x[c + 1], q2b);
-      q0a = fmaf(b0.z, x[c + 2], q0a); q0b = fmaf(b0.w, x[c + 3], q0b);
-      q1a = fmaf(b1.z, x[c + 2], q1a); q1b = fmaf(b1.w, x[c + 3], q1b);
-      q2a = fmaf(b2.z, x[c + 2], q2a); q2b = fmaf(b2.w, x[c + 3], q2b);
+      for (int c = 0; c < D; c += 4) {
+        float4 b0 = ld4(B + c), b1 = ld4(B + D + c), b2 = ld4(B + 2 * D + c);
+        q0a = fmaf(b0.x, x[c], q0a); q0b = fmaf(b0.y, x[c + 1], q0b);
+        q1a = fmaf(b1.x, x[c], q1a); q1b = fmaf(b1.y, x[c + 1], q1b);
+        q2a = fmaf(b2.x, x[c], q2a); q2b = fmaf(b2.y, x[c + 1], q2b);
+        q0a = fmaf(b0.z, x[c + 2], q0a); q0b = fmaf(b0.w, x[c + 3], q0b);
+        q1a = fmaf(b1.z, x[c + 2], q1a); q1b = fmaf(b1.w, x[c + 3], q1b);
+        q2a = fmaf(b2.z, x[c + 2], q2a); q2b = fmaf(b2.w, x[c + 3], q2b);
+      }
+      q0 = q0a + q0b; q1 = q1a + q1b; q2 = q2a + q2b;
+    } else {
+      q0 = p.mm[j * 3 + 0]; q1 = p.mm[j * 3 + 1]; q2 = p.mm[j * 3 + 2];
+#pragma unroll
+      for (int c = 0; c < D; ++c) {
+        q0 = fmaf(B[c], x[c], q0);
+        q1 = fmaf(B[D + c], x[c], q1);
+        q2 = fmaf(B[2 * D + c], x[c], q2);
+      }
     }
-    const float q0 = q0a + q0b, q1 = q1a + q1b, q2 = q2a + q2b;
     if (!(q2 > kZMin)) { ll += __logf(kappa); continue; }
     float iz = 1.0f / q2;
     float u = fmaf(p.fx * q0, iz, p.cx), v = fmaf(p.fy * q1, iz, p.cy);
@@ -222,15 +239,21 @@ __host__ __device__ constexpr int params_floats(int K, int J, bool diag) {
 // buffers of D x Nmax floats, L2-resident).  Per frame: propagate + score,
 // block max, weights/estimate/ESS, exact systematic resampling by a scatter
 // walk over each thread's contiguous chunk of integer weights.
-template <int D, bool DIAG, int TBMAX, int MINB>
+// Code variants chosen by the autotuner: VEC (float4 vs scalar parameter loads)
+// and SEARCH (ancestors by binary search over the shared prefix sums, 12 Nmax
+// bytes of shared memory, vs the scatter walk over each thread's chunk, 8 Nmax).
+template <int D, bool DIAG, int TBMAX, int MINB, bool VEC, bool SEARCH>
 __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int TB = blockDim.x, tid = threadIdx.x;
   constexpr int NV = D + 3;
   const int Nmax = A.Nmax;
-  float* sW = reinterpret_cast<float*>(smem);                            // 4 Nmax
-  int* sA = reinterpret_cast<int*>(smem + 4 * (size_t)Nmax);             // 4 Nmax
-  float* sP = reinterpret_cast<float*>(smem + 8 * (size_t)Nmax);         // params (Nmax % 32 == 0)
+  // SEARCH: sQ (u64) | sA (log-weights, weights, then ancestors, as int bits)
+  // scatter: sW (log-weights then weights) | sA (ancestors)
+  uint64_t* sQ = reinterpret_cast<uint64_t*>(smem);
+  float* sW = reinterpret_cast<float*>(smem);
+  int* sA = reinterpret_cast<int*>(smem + (SEARCH ? 8 : 4) * (size_t)Nmax);
+  float* sP = reinterpret_cast<float*>(smem + (SEARCH ? 12 : 8) * (size_t)Nmax);   // Nmax % 32 == 0
   const int K = A.K, J = A.J;
   const int Lsz = pad4(DIAG ? K * D : K * D * (D + 1) / 2);
   float* s_a = sP;
@@ -323,11 +346,11 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
 #pragma unroll
         for (int r = 0; r < D; ++r) x[r] = xa[(size_t)r * Nmax + an];
         float uc = particle_draws<D>(seed, trk, (uint32_t)t, (uint32_t)i, eps);
-        propagate<D, DIAG>(pv, eps, uc, x);
+        propagate<D, DIAG, VEC>(pv, eps, uc, x);
 #pragma unroll
         for (int r = 0; r < D; ++r) xb[(size_t)r * Nmax + i] = x[r];
-        float ll = loglik<D>(pv, x, s_cnt, s_det, ob.x, ob.y, ob.z);
-        sW[i] = ll;
+        float ll = loglik<D, VEC>(pv, x, s_cnt, s_det, ob.x, ob.y, ob.z);
+        if (SEARCH) sA[i] = __float_as_int(ll); else sW[i] = ll;
         lmax = fmaxf(lmax, ll);
       }
       const float M = block_max(lmax, s_red);
@@ -338,10 +361,10 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
 #pragma unroll
       for (int c = 0; c < NV; ++c) acc[c] = 0.0f;   // s, s2, wmax, v[D]
       for (int i = tid; i < N; i += TB) {
-        float ll = sW[i];
+        float ll = SEARCH ? __int_as_float(sA[i]) : sW[i];
         float w = fb ? 0.0f : (ll == M ? 1.0f : __expf(ll - M));
         if (!(w >= 0.0f)) w = 0.0f;
-        sW[i] = w;
+        if (SEARCH) sA[i] = __float_as_int(w); else sW[i] = w;
         if (dbg) A.dbg_w[(size_t)t * N + i] = w;
         acc[0] += w;
         acc[1] = fmaf(w, w, acc[1]);
@@ -375,13 +398,24 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       int e = 0;
       frexpf(Wmax, &e);
 
-      // ---- exact systematic resampling: chunk sums, block scan, scatter walk
+      // ---- exact systematic resampling: chunk sums and block scan, then either
+      // a binary search per target (SEARCH) or a scatter walk per chunk
       uint64_t cs = 0;
-      for (int j = j0; j < j1; ++j) cs += quantize_f32(sW[j], e);
+      for (int j = j0; j < j1; ++j) cs += quantize_f32(SEARCH ? __int_as_float(sA[j]) : sW[j], e);
       uint64_t Qt;
       uint64_t P = block_excl_scan_u64(cs, s_red64, &Qt);   // includes barriers
       const uint32_t U = resample_uniform(seed, trk, (uint32_t)t);
-      if (fb || Qt == 0) {
+      if (SEARCH) {
+        uint64_t pre = P;
+        for (int j = j0; j < j1; ++j) {
+          pre += quantize_f32(__int_as_float(sA[j]), e);
+          sQ[j] = pre;
+        }
+        __syncthreads();
+        const bool fb2 = fb || Qt == 0;
+        for (int i = tid; i < N; i += TB)
+          sA[i] = fb2 ? resample_fallback_index(U, i, N) : resample_search(sQ, N, N, resample_rhs(i, U, Qt));
+      } else if (fb || Qt == 0) {
         for (int i = tid; i < N; i += TB) sA[i] = resample_fallback_index(U, i, N);
       } else if (j0 < j1) {
         int i = (j0 == 0) ? 0 : count_targets_le(P, N, U, Qt);
@@ -402,9 +436,9 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
   }
 }
 
-static size_t batched_smem_bytes(int D, int Nmax, int K, int J, bool diag) {
+static size_t batched_smem_bytes(int D, int Nmax, int K, int J, bool diag, bool search) {
   size_t pf = (D == 12) ? params_floats<12>(K, J, diag) : params_floats<24>(K, J, diag);
-  size_t bytes = 8 * (size_t)Nmax + 4 * pf + 8 * MKF_MAX_J * MKF_MAX_DET + 32 +
+  size_t bytes = (search ? 12 : 8) * (size_t)Nmax + 4 * pf + 8 * MKF_MAX_J * MKF_MAX_DET + 32 +
                  4 * (32 * (D + 3) + 2) + 8 * 34 + 16;
   return (bytes + 15) & ~size_t(15);
 }
@@ -726,6 +760,7 @@ struct mkf_bpf_batch {
   float* scratch;
   size_t scratch_slots;
   int last_grid;
+  int variant;
   int dbg_track;
   float* dbg_w;
   int* dbg_anc;
@@ -911,7 +946,7 @@ extern "C" int mkf_bpf_batch_create(const mkf_bpf_models* models, int n_tracks, 
   if (st) { free_models(B->m); delete B; return st; }
   B->n_tracks = n_tracks; B->Nmax = (Nmax + 31) & ~31; B->d = models->d; B->K = models->K; B->J = models->J;
   B->G = n_frames_total;
-  B->tb = 256; B->ctas_per_sm = 0;
+  B->tb = 256; B->ctas_per_sm = 0; B->variant = MKF_BPF_VEC_LOADS;
   B->dbg_track = -1;
   std::vector<int4> meta(n_tracks);
   std::vector<long long> fb(n_tracks);
@@ -966,10 +1001,10 @@ extern "C" int mkf_bpf_batch_set_debug(mkf_bpf_batch_t B, int track, float* d_w,
   return MKF_OK;
 }
 
-template <int D, bool DIAG, int TBMAX, int MINB>
+template <int D, bool DIAG, int TBMAX, int MINB, bool VEC, bool SEARCH>
 static int launch_batched_v(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
-  auto kern = bpf_batched_kernel<D, DIAG, TBMAX, MINB>;
-  size_t smem = batched_smem_bytes(D, B->Nmax, B->K, B->J, DIAG);
+  auto kern = bpf_batched_kernel<D, DIAG, TBMAX, MINB, VEC, SEARCH>;
+  size_t smem = batched_smem_bytes(D, B->Nmax, B->K, B->J, DIAG, SEARCH);
   MKF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int occ = 0;
   MKF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, B->tb, smem));
@@ -993,12 +1028,32 @@ static int launch_batched_v(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
   return MKF_OK;
 }
 
-// launch-bound variant by block size and requested residency
+template <int D, bool DIAG, bool VEC, bool SEARCH>
+static int launch_shape(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
+  if (B->tb > 256) return launch_batched_v<D, DIAG, 512, 1, VEC, SEARCH>(B, a, s);
+  if (B->ctas_per_sm >= 3) return launch_batched_v<D, DIAG, 256, 3, VEC, SEARCH>(B, a, s);
+  return launch_batched_v<D, DIAG, 256, 2, VEC, SEARCH>(B, a, s);
+}
+
+// launch-bound variant by block size and requested residency; the load-width
+// and resampler variants are compiled for the diagonal-noise d = 12 model only
 template <int D, bool DIAG>
 static int launch_batched(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
-  if (B->tb > 256) return launch_batched_v<D, DIAG, 512, 1>(B, a, s);
-  if (B->ctas_per_sm >= 3) return launch_batched_v<D, DIAG, 256, 3>(B, a, s);
-  return launch_batched_v<D, DIAG, 256, 2>(B, a, s);
+  if (D == 12 && DIAG) {
+    const bool vec = (B->variant & MKF_BPF_VEC_LOADS) != 0, search = (B->variant & MKF_BPF_SEARCH) != 0;
+    if (vec && search) return launch_shape<D, DIAG, true, true>(B, a, s);
+    if (vec) return launch_shape<D, DIAG, true, false>(B, a, s);
+    if (search) return launch_shape<D, DIAG, false, true>(B, a, s);
+    return launch_shape<D, DIAG, false, false>(B, a, s);
+  }
+  return launch_shape<D, DIAG, true, false>(B, a, s);
+}
+
+extern "C" int mkf_bpf_batch_set_variant(mkf_bpf_batch_t B, int flags) {
+  MKF_ARG(B, "mkf_bpf_batch_set_variant: null handle");
+  MKF_ARG((flags & ~(MKF_BPF_VEC_LOADS | MKF_BPF_SEARCH)) == 0, "mkf_bpf_batch_set_variant: unknown flag");
+  B->variant = flags;
+  return MKF_OK;
 }
 
 extern "C" int mkf_bpf_batch_run(mkf_bpf_batch_t B, const int* d_det_off, const float* d_det,

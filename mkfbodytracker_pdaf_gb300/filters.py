@@ -120,7 +120,7 @@ class BootstrapParticleFilter:
 class BatchedBootstrapPF:
     """All tracks of a synth.BpfBatch (or equivalent) in one persistent launch."""
 
-    def __init__(self, batch, block_threads=256, ctas_per_sm=0):
+    def __init__(self, batch, block_threads=256, ctas_per_sm=0, variant=1):
         import torch
         self.torch = torch
         self.batch = batch
@@ -136,12 +136,15 @@ class BatchedBootstrapPF:
                                              C.cast(tr, C.c_void_p), batch.n_frames_total,
                                              C.byref(h)), "mkf_bpf_batch_create")
         self.h = h
-        self.set_tuning(block_threads, ctas_per_sm)
+        self.set_tuning(block_threads, ctas_per_sm, variant)
 
-    def set_tuning(self, block_threads, ctas_per_sm=0):
+    def set_tuning(self, block_threads, ctas_per_sm=0, variant=None):
         N.check(N.lib().mkf_bpf_batch_set_tuning(self.h, int(block_threads), int(ctas_per_sm)),
                 "mkf_bpf_batch_set_tuning")
         self.block_threads, self.ctas_per_sm = block_threads, ctas_per_sm
+        if variant is not None:
+            N.check(N.lib().mkf_bpf_batch_set_variant(self.h, int(variant)), "mkf_bpf_batch_set_variant")
+            self.variant = variant
 
     def device_inputs(self):
         torch = self.torch
