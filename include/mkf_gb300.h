@@ -163,8 +163,9 @@ int mkf_bpf_batch_set_tuning(mkf_bpf_batch_t h, int block_threads, int ctas_per_
 /* code variants (autotuned; applied to the d = 12 diagonal-noise model):
  * MKF_BPF_VEC_LOADS = float4 model loads, MKF_BPF_SEARCH = ancestors by binary
  * search over shared prefix sums (12 bytes/particle of shared memory) instead
- * of the scatter walk (8 bytes/particle).  Results are identical. */
-enum { MKF_BPF_VEC_LOADS = 1, MKF_BPF_SEARCH = 2 };
+ * of the scatter walk (8 bytes/particle), MKF_BPF_PAIR = two particles per
+ * loop iteration (implies the other two).  Results are identical. */
+enum { MKF_BPF_VEC_LOADS = 1, MKF_BPF_SEARCH = 2, MKF_BPF_PAIR = 4 };
 int mkf_bpf_batch_set_variant(mkf_bpf_batch_t h, int flags);
 /* device-resident run: outputs est (G*d), loglik (G), ess (G), status (n_tracks) */
 int mkf_bpf_batch_run(mkf_bpf_batch_t h, const int* d_det_off, const float* d_det,

@@ -23,7 +23,7 @@ TUNING_FILE = os.path.join(HERE, "tuning_gb300.json")
 # (block_threads, ctas_per_sm): 512x1 and 256x2 compile with a 128-register
 # budget, 256x3 with an 80-register budget (3 CTAs of 71 KB shared memory each)
 SHAPES = [(256, 2), (256, 3), (512, 1)]
-VARIANTS = [0, 1, 2, 3]          # bit 0: float4 model loads, bit 1: binary-search resampling
+VARIANTS = [0, 1, 2, 3, 7]       # bit 0: float4 loads, bit 1: binary-search resampling, bit 2: particle pairs
 CANDIDATES = [(tb, cps, v) for (tb, cps) in SHAPES for v in VARIANTS]
 
 

@@ -190,14 +190,30 @@ __device__ __forceinline__ float loglik(const PView& p, const float* x, const in
       }
     }
     if (!(q2 > kZMin)) { ll += __logf(kappa); continue; }
-    float iz = 1.0f / q2;
-    float u = fmaf(p.fx * q0, iz, p.cx), v = fmaf(p.fy * q1, iz, p.cy);
-    float acc = 0.0f;
+    const float iz = __fdividef(1.0f, q2);
+    const float u = fmaf(p.fx * q0, iz, p.cx), v = fmaf(p.fy * q1, iz, p.cy);
+    // four independent partial sums so the exponentials of a list overlap
+    float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, acc3 = 0.0f;
     const float2* dj = det + j * MKF_MAX_DET;
-    for (int i = 0; i < cnt[j]; ++i) {
-      float dx = dj[i].x - u, dy = dj[i].y - v;
-      acc += __expf(-(dx * dx + dy * dy) * inv2s2);
+    const int n = cnt[j];
+    int i = 0;
+    for (; i + 4 <= n; i += 4) {
+      const float4 d01 = *reinterpret_cast<const float4*>(dj + i);
+      const float4 d23 = *reinterpret_cast<const float4*>(dj + i + 2);
+      float dx = d01.x - u, dy = d01.y - v;
+      acc0 += __expf(-(dx * dx + dy * dy) * inv2s2);
+      dx = d01.z - u; dy = d01.w - v;
+      acc1 += __expf(-(dx * dx + dy * dy) * inv2s2);
+      dx = d23.x - u; dy = d23.y - v;
+      acc2 += __expf(-(dx * dx + dy * dy) * inv2s2);
+      dx = d23.z - u; dy = d23.w - v;
+      acc3 += __expf(-(dx * dx + dy * dy) * inv2s2);
     }
+    for (; i < n; ++i) {
+      const float dx = dj[i].x - u, dy = dj[i].y - v;
+      acc0 += __expf(-(dx * dx + dy * dy) * inv2s2);
+    }
+    const float acc = (acc0 + acc1) + (acc2 + acc3);
     ll += __logf(fmaf(norm, acc, floor_));
   }
   return ll;
@@ -242,7 +258,7 @@ __host__ __device__ constexpr int params_floats(int K, int J, bool diag) {
 // Code variants chosen by the autotuner: VEC (float4 vs scalar parameter loads)
 // and SEARCH (ancestors by binary search over the shared prefix sums, 12 Nmax
 // bytes of shared memory, vs the scatter walk over each thread's chunk, 8 Nmax).
-template <int D, bool DIAG, int TBMAX, int MINB, bool VEC, bool SEARCH>
+template <int D, bool DIAG, int TBMAX, int MINB, bool VEC, bool SEARCH, bool PAIR = false>
 __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int TB = blockDim.x, tid = threadIdx.x;
@@ -340,18 +356,50 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
 
       // ---- propagate from the resampled set and score
       float lmax = -INFINITY;
-      for (int i = tid; i < N; i += TB) {
-        const int an = sA[i];
-        float x[D], eps[D];
+      if (PAIR) {
+        // particles i and i + TB of this thread together: two independent
+        // dependency chains for the scheduler (same particles, same results)
+        for (int i = tid; i < N; i += 2 * TB) {
+          const int i2 = i + TB;
+          const bool two = i2 < N;
+          const int an = sA[i], an2 = two ? sA[i2] : an;
+          float x[D], eps[D], y[D], eps2[D];
 #pragma unroll
-        for (int r = 0; r < D; ++r) x[r] = xa[(size_t)r * Nmax + an];
-        float uc = particle_draws<D>(seed, trk, (uint32_t)t, (uint32_t)i, eps);
-        propagate<D, DIAG, VEC>(pv, eps, uc, x);
+          for (int r = 0; r < D; ++r) {
+            x[r] = xa[(size_t)r * Nmax + an];
+            y[r] = xa[(size_t)r * Nmax + an2];
+          }
+          const float uc = particle_draws<D>(seed, trk, (uint32_t)t, (uint32_t)i, eps);
+          const float uc2 = particle_draws<D>(seed, trk, (uint32_t)t, (uint32_t)i2, eps2);
+          propagate<D, DIAG, VEC>(pv, eps, uc, x);
+          propagate<D, DIAG, VEC>(pv, eps2, uc2, y);
 #pragma unroll
-        for (int r = 0; r < D; ++r) xb[(size_t)r * Nmax + i] = x[r];
-        float ll = loglik<D, VEC>(pv, x, s_cnt, s_det, ob.x, ob.y, ob.z);
-        if (SEARCH) sA[i] = __float_as_int(ll); else sW[i] = ll;
-        lmax = fmaxf(lmax, ll);
+          for (int r = 0; r < D; ++r) xb[(size_t)r * Nmax + i] = x[r];
+          const float ll = loglik<D, VEC>(pv, x, s_cnt, s_det, ob.x, ob.y, ob.z);
+          if (SEARCH) sA[i] = __float_as_int(ll); else sW[i] = ll;
+          lmax = fmaxf(lmax, ll);
+          if (two) {
+#pragma unroll
+            for (int r = 0; r < D; ++r) xb[(size_t)r * Nmax + i2] = y[r];
+            const float ll2 = loglik<D, VEC>(pv, y, s_cnt, s_det, ob.x, ob.y, ob.z);
+            if (SEARCH) sA[i2] = __float_as_int(ll2); else sW[i2] = ll2;
+            lmax = fmaxf(lmax, ll2);
+          }
+        }
+      } else {
+        for (int i = tid; i < N; i += TB) {
+          const int an = sA[i];
+          float x[D], eps[D];
+#pragma unroll
+          for (int r = 0; r < D; ++r) x[r] = xa[(size_t)r * Nmax + an];
+          float uc = particle_draws<D>(seed, trk, (uint32_t)t, (uint32_t)i, eps);
+          propagate<D, DIAG, VEC>(pv, eps, uc, x);
+#pragma unroll
+          for (int r = 0; r < D; ++r) xb[(size_t)r * Nmax + i] = x[r];
+          float ll = loglik<D, VEC>(pv, x, s_cnt, s_det, ob.x, ob.y, ob.z);
+          if (SEARCH) sA[i] = __float_as_int(ll); else sW[i] = ll;
+          lmax = fmaxf(lmax, ll);
+        }
       }
       const float M = block_max(lmax, s_red);
       const bool fb = !(M > -INFINITY) || !(M < INFINITY);
@@ -538,7 +586,7 @@ __device__ void block_merge(float& m, float& s, float& s2, float* v, float* red)
 
 template <int D, bool DIAG>
 __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
-  __shared__ float2 s_det[MKF_MAX_J * MKF_MAX_DET];
+  __shared__ __align__(16) float2 s_det[MKF_MAX_J * MKF_MAX_DET];
   __shared__ int s_cnt[MKF_MAX_J];
   __shared__ float s_red[32 * (D + 3)];
   __shared__ bool s_last;
@@ -1001,9 +1049,9 @@ extern "C" int mkf_bpf_batch_set_debug(mkf_bpf_batch_t B, int track, float* d_w,
   return MKF_OK;
 }
 
-template <int D, bool DIAG, int TBMAX, int MINB, bool VEC, bool SEARCH>
+template <int D, bool DIAG, int TBMAX, int MINB, bool VEC, bool SEARCH, bool PAIR>
 static int launch_batched_v(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
-  auto kern = bpf_batched_kernel<D, DIAG, TBMAX, MINB, VEC, SEARCH>;
+  auto kern = bpf_batched_kernel<D, DIAG, TBMAX, MINB, VEC, SEARCH, PAIR>;
   size_t smem = batched_smem_bytes(D, B->Nmax, B->K, B->J, DIAG, SEARCH);
   MKF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int occ = 0;
@@ -1028,11 +1076,11 @@ static int launch_batched_v(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
   return MKF_OK;
 }
 
-template <int D, bool DIAG, bool VEC, bool SEARCH>
+template <int D, bool DIAG, bool VEC, bool SEARCH, bool PAIR = false>
 static int launch_shape(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
-  if (B->tb > 256) return launch_batched_v<D, DIAG, 512, 1, VEC, SEARCH>(B, a, s);
-  if (B->ctas_per_sm >= 3) return launch_batched_v<D, DIAG, 256, 3, VEC, SEARCH>(B, a, s);
-  return launch_batched_v<D, DIAG, 256, 2, VEC, SEARCH>(B, a, s);
+  if (B->tb > 256) return launch_batched_v<D, DIAG, 512, 1, VEC, SEARCH, PAIR>(B, a, s);
+  if (B->ctas_per_sm >= 3) return launch_batched_v<D, DIAG, 256, 3, VEC, SEARCH, PAIR>(B, a, s);
+  return launch_batched_v<D, DIAG, 256, 2, VEC, SEARCH, PAIR>(B, a, s);
 }
 
 // launch-bound variant by block size and requested residency; the load-width
@@ -1041,6 +1089,7 @@ template <int D, bool DIAG>
 static int launch_batched(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
   if (D == 12 && DIAG) {
     const bool vec = (B->variant & MKF_BPF_VEC_LOADS) != 0, search = (B->variant & MKF_BPF_SEARCH) != 0;
+    if (B->variant & MKF_BPF_PAIR) return launch_shape<D, DIAG, true, true, true>(B, a, s);
     if (vec && search) return launch_shape<D, DIAG, true, true>(B, a, s);
     if (vec) return launch_shape<D, DIAG, true, false>(B, a, s);
     if (search) return launch_shape<D, DIAG, false, true>(B, a, s);
@@ -1051,7 +1100,8 @@ static int launch_batched(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
 
 extern "C" int mkf_bpf_batch_set_variant(mkf_bpf_batch_t B, int flags) {
   MKF_ARG(B, "mkf_bpf_batch_set_variant: null handle");
-  MKF_ARG((flags & ~(MKF_BPF_VEC_LOADS | MKF_BPF_SEARCH)) == 0, "mkf_bpf_batch_set_variant: unknown flag");
+  MKF_ARG((flags & ~(MKF_BPF_VEC_LOADS | MKF_BPF_SEARCH | MKF_BPF_PAIR)) == 0,
+          "mkf_bpf_batch_set_variant: unknown flag");
   B->variant = flags;
   return MKF_OK;
 }

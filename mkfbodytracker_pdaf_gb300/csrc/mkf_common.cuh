@@ -77,7 +77,8 @@ MKF_HD uint32_t resample_uniform(uint64_t seed, uint32_t track, uint32_t frame) 
 __device__ __forceinline__ void box_muller(uint32_t w0, uint32_t w1, float& z0, float& z1) {
   float u1 = (float)((w0 >> 8) + 1u) * (1.0f / 16777216.0f);
   float u2 = (float)(w1 >> 8) * (1.0f / 16777216.0f);
-  float r = sqrtf(-2.0f * __logf(u1));
+  const float y = -2.0f * __logf(u1);                 // >= 0; y * rsqrt(y) is the MUFU square root
+  float r = y * rsqrtf(fmaxf(y, 1e-30f));
   float s, c;
   __sincosf(3.14159265358979f * (2.0f * u2 - 1.0f), &s, &c);
   z0 = r * c;
