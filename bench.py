@@ -101,15 +101,14 @@ class ClockSampler:
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from mkfbodytracker_pdaf_gb300.replicas import dist_env as env
+    return env()
 
 
 def workload(rank, n_tracks):
     from mkfbodytracker_pdaf_gb300 import synth
-    return synth.config2_batch(n_tracks=n_tracks, seed=synth.MASTER_SEED + 2 + 1000 * rank)
+    from mkfbodytracker_pdaf_gb300.replicas import rank_seed
+    return synth.config2_batch(n_tracks=n_tracks, seed=rank_seed(synth.MASTER_SEED + 2, rank))
 
 
 def pf_count(batch, ids=None):
@@ -214,6 +213,7 @@ def run_gb300(args):
     from mkfbodytracker_pdaf_gb300.filters import BatchedBootstrapPF
 
     from mkfbodytracker_pdaf_gb300.autotune import load_tuning
+    from mkfbodytracker_pdaf_gb300.replicas import max_over_ranks, sum_over_ranks
     tb, cps, var = load_tuning()
     tb = args.block_threads or tb
     cps = cps if args.ctas_per_sm is None else args.ctas_per_sm
@@ -253,12 +253,9 @@ def run_gb300(args):
     barrier()
     clocks = sampler.stop()
     ms = e0.elapsed_time(e1) / args.steps
-    t_local = ms / 1000.0
-    if ws > 1:
-        t = torch.tensor([t_local], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_local = float(t.item())
-    value = G * ws / t_local
+    t_local = max_over_ranks(ms / 1000.0)
+    G_all = sum_over_ranks(G)
+    value = G_all / t_local
     st = outs[3].cpu().numpy()
     est_ok = bool(torch.isfinite(outs[0]).all().item())
 
@@ -277,21 +274,17 @@ def run_gb300(args):
     for _ in range(args.steps):
         runner.run_host(hbufs[0], hbufs[1], hbufs[2:])
     barrier()
-    t_e2e = (time.perf_counter() - t0) / args.steps
-    if ws > 1:
-        t = torch.tensor([t_e2e], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    t_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps)
     h2d = hbufs[0].nbytes + hbufs[1].nbytes
     d2h = sum(h.nbytes for h in hbufs[2:])
 
     if rank == 0:
         peak, peak_kind = load_peaks()
-        achieved = BYTES_PER_PF * PF / t_local / 1e9
+        achieved = BYTES_PER_PF * PF / (ms / 1000.0) / 1e9
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, no dataset)",
+            "warmup": args.warmup, "ms_per_step": t_local * 1000.0, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, no dataset)",
             "config": {"workload": "batched uneven tracks: B=%d, T~U{50..2000}, N log-uniform [128,8192], "
                                    "K=15, d=12, lambda~U[0,12], P_D~U[0.7,1]" % args.tracks,
                        "tracks_per_gpu": batch.n_tracks, "track_frames_per_gpu": G,
@@ -300,7 +293,7 @@ def run_gb300(args):
                        "block_threads": runner.block_threads, "ctas_per_sm": runner.ctas_per_sm,
                        "variant": runner.variant,
                        "parallelism": "one persistent kernel per GPU; tracks sharded by rank"},
-            "e2e": {"value": G * ws / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "e2e": {"value": G_all / t_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -562,7 +555,7 @@ def run_fit(args):
           flush=True)
 
 
-def main():
+def parse_args(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -588,9 +581,14 @@ def main():
     ap.add_argument("--fit-frames", type=int, default=500)
     ap.add_argument("--fit-steps", type=int, default=200)
     ap.add_argument("--fit-lr", type=float, default=0.02)
-    args = ap.parse_args()
+    args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
+    return args
+
+
+def main(argv=None):
+    args = parse_args(argv)
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "sweep":

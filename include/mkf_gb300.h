@@ -151,6 +151,21 @@ int mkf_bpf_read_debug(mkf_bpf_t h, float* d_x, float* d_logw, float* d_w, int* 
 int mkf_bpf_status(mkf_bpf_t h, int* status);
 int mkf_bpf_destroy(mkf_bpf_t h);
 
+/* Captured frame loop: n_frames consecutive mkf_bpf_update calls recorded once
+ * into a CUDA graph (three kernel nodes per frame).  Frame t of a launch is
+ * frame0 + t (frame0 given at launch, read on the device); its detections are
+ * d_det_off + t*J (J+1 offsets into d_det), its outputs d_est + t*d,
+ * d_loglik + t, d_ess + t (each may be NULL).  Buffers are bound at capture: a
+ * launch reads what they hold when it runs, so a caller stages each chunk of
+ * frames into the same buffers.  A launch is equivalent to the n_frames update
+ * calls, and launches chain with each other and with mkf_bpf_update.  The
+ * graph is valid while its filter exists. */
+typedef struct mkf_bpf_graph* mkf_bpf_graph_t;
+int mkf_bpf_graph_create(mkf_bpf_t h, int n_frames, const int* d_det_off, const float* d_det, float* d_est,
+                         float* d_loglik, float* d_ess, mkf_bpf_graph_t* out);
+int mkf_bpf_graph_launch(mkf_bpf_graph_t g, uint32_t frame0, mkf_stream_t stream);
+int mkf_bpf_graph_destroy(mkf_bpf_graph_t g);
+
 /* ---- batched uneven tracks: one persistent kernel over all tracks */
 typedef struct mkf_bpf_batch* mkf_bpf_batch_t;
 /* tracks: n_tracks descriptors; n_frames_total = sum of n_frames (global frame
@@ -181,6 +196,37 @@ int mkf_bpf_batch_run_host(mkf_bpf_batch_t h, const int* det_off, const float* d
 int mkf_bpf_batch_set_debug(mkf_bpf_batch_t h, int track, float* d_w, int* d_anc);
 int mkf_bpf_batch_destroy(mkf_bpf_batch_t h);
 
+
+/* ---------------------------------------------- A12 legacy bootstrap PF (pf2D) */
+/* pf2D's ParticleFilter(numParticles, numDims, side) with its my_gmm prior
+ * (pf2D.h:12-51), FP64, literal semantics: update(z) weights each particle by
+ * the GMM prior density (float expf, pf2D.cpp:157-164) times isotropic 2-D
+ * Gaussians (variance 15) of columns 6,7 against z[0..1] and columns 0,1 against
+ * z[2..3] (pf2D.cpp:168); normalises; resamples (exact systematic resampling
+ * of the normalised weights; when every weight is 0 all columns are redrawn
+ * uniformly over the constructor's ranges and the weights reset to 1/N,
+ * pf2D.cpp:225-250); leaves the weights as they were otherwise (as the
+ * reference does, so getEstimator weights the resampled particles with the
+ * pre-resampling weights); then predicts: columns 0..7 += N(0, 5^2)
+ * (pf2D.cpp:90-102; columns >= 8 get no noise).  Draws: column c uniform of
+ * particle i from word c%4 of block (frame, i, 0x200 + c/4) (w / 2^32); the 8
+ * normals from blocks (frame, i, 0x210..0x211) by Box-Muller; construction uses
+ * frame 0xFFFFFFFF.  mean (K*d), cov (K*d*d), w (K): host; 8 <= d <= 32. */
+typedef struct mkf_pf2d* mkf_pf2d_t;
+int mkf_pf2d_create(int n_particles, int d, int side, int K, const double* mean, const double* cov,
+                    const double* w, int width, int height, uint64_t seed, uint32_t track_id,
+                    mkf_pf2d_t* out);
+/* z: host, 4 doubles (head x, y; hand x, y) = the reference's 2x2 measurement */
+int mkf_pf2d_update(mkf_pf2d_t h, uint32_t frame, const double* z, mkf_stream_t stream);
+int mkf_pf2d_estimate(mkf_pf2d_t h, double* d_est, mkf_stream_t stream);
+/* particles (N*d), weights (N), ancestors (N, -1 after a re-initialisation),
+ * reinit (host int, optional: 1 if the last update re-initialised) */
+int mkf_pf2d_read(mkf_pf2d_t h, double* d_particles, double* d_weights, int* d_anc, int* reinit,
+                  mkf_stream_t stream);
+/* the filter's own draws of one frame: 8 normals and d uniforms per particle */
+int mkf_pf2d_draws(uint64_t seed, uint32_t track, uint32_t frame, int n, int d, double* d_eps,
+                   double* d_u, mkf_stream_t stream);
+int mkf_pf2d_destroy(mkf_pf2d_t h);
 
 /* --------------------------------------- A1-A5, A7, A8, A10 Rao-Blackwellised PF */
 /* pf2DRao ParticleFilter(int nParticles) + its my_gmm (pf2DRao.h:13-31,

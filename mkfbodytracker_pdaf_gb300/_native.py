@@ -62,6 +62,9 @@ SIGNATURES = {
     "mkf_bpf_read_debug": (I, [P, P, P, P, P, P]),
     "mkf_bpf_status": (I, [P, C.POINTER(I)]),
     "mkf_bpf_destroy": (I, [P]),
+    "mkf_bpf_graph_create": (I, [P, I, P, P, P, P, P, C.POINTER(P)]),
+    "mkf_bpf_graph_launch": (I, [P, U32, P]),
+    "mkf_bpf_graph_destroy": (I, [P]),
     "mkf_bpf_batch_create": (I, [C.POINTER(BpfModels), I, P, I64, C.POINTER(P)]),
     "mkf_bpf_batch_set_tuning": (I, [P, I, I]),
     "mkf_bpf_batch_set_variant": (I, [P, I]),
@@ -69,6 +72,12 @@ SIGNATURES = {
     "mkf_bpf_batch_run_host": (I, [P, P, P, I64, P, P, P, P, P]),
     "mkf_bpf_batch_set_debug": (I, [P, I, P, P]),
     "mkf_bpf_batch_destroy": (I, [P]),
+    "mkf_pf2d_create": (I, [I, I, I, I, P, P, P, I, I, U64, U32, C.POINTER(P)]),
+    "mkf_pf2d_update": (I, [P, U32, P, P]),
+    "mkf_pf2d_estimate": (I, [P, P, P]),
+    "mkf_pf2d_read": (I, [P, P, P, P, P, P]),
+    "mkf_pf2d_draws": (I, [U64, U32, U32, I, I, P, P, P]),
+    "mkf_pf2d_destroy": (I, [P]),
     "mkf_rbpf_create": (I, [I, I, I, I, I, U64, U32, C.POINTER(P)]),
     "mkf_rbpf_load_gaussian": (I, [P, I, P, P, P, P, I, C.c_double, C.c_double]),
     "mkf_rbpf_set_component": (I, [P, I, P, P, P, P, P, C.c_double, P, P]),

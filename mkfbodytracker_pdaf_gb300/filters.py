@@ -201,6 +201,62 @@ def _hp(a):
     return a.ctypes.data_as(C.c_void_p) if a is not None else None
 
 
+class LegacyParticleFilter:
+    """pf2D's ParticleFilter(numParticles, numDims, side) with its own my_gmm
+    prior (pf2D.h:12-51): update(measurement) = weight by prior x likelihood,
+    normalise, resample (uniform re-initialisation when every weight is 0),
+    predict; getEstimator = sum of weights x particles.  FP64 on the GPU."""
+
+    def __init__(self, n_particles, mean, cov, w, side=0, width=640, height=480, seed=0, track_id=0):
+        import torch
+        self.torch = torch
+        mean = _d(mean)
+        self.K, self.d = mean.shape
+        self.N = int(n_particles)
+        h = C.c_void_p()
+        N.check(N.lib().mkf_pf2d_create(self.N, self.d, int(side), self.K, _hp(mean), _hp(_d(cov)), _hp(_d(w)),
+                                        int(width), int(height), int(seed), int(track_id), C.byref(h)),
+                "mkf_pf2d_create")
+        self.h = h
+        self.est = torch.zeros(self.d, dtype=torch.float64, device="cuda")
+        self.seed, self.track_id = int(seed), int(track_id)
+
+    def update(self, measurement, frame, stream=None):
+        """measurement: 2x2 (head x, y; hand x, y) on the host."""
+        z = _d(measurement).ravel()
+        N.check(N.lib().mkf_pf2d_update(self.h, int(frame), _hp(z), _stream(self.torch, stream)), "mkf_pf2d_update")
+
+    def getEstimator(self, out=None, stream=None):
+        out = self.est if out is None else out
+        N.check(N.lib().mkf_pf2d_estimate(self.h, _ptr(out), _stream(self.torch, stream)), "mkf_pf2d_estimate")
+        return out
+
+    def read(self, stream=None):
+        t = self.torch
+        x = t.empty((self.N, self.d), dtype=t.float64, device="cuda")
+        w = t.empty(self.N, dtype=t.float64, device="cuda")
+        anc = t.empty(self.N, dtype=t.int32, device="cuda")
+        r = C.c_int(0)
+        N.check(N.lib().mkf_pf2d_read(self.h, _ptr(x), _ptr(w), _ptr(anc), C.byref(r), _stream(self.torch, stream)),
+                "mkf_pf2d_read")
+        return {"x": x, "w": w, "anc": anc, "reinit": bool(r.value)}
+
+    def draws(self, frame, stream=None):
+        """(eps (N, 8), u (N, d)): this filter's normals and uniforms of one frame."""
+        t = self.torch
+        eps = t.empty((self.N, 8), dtype=t.float64, device="cuda")
+        u = t.empty((self.N, self.d), dtype=t.float64, device="cuda")
+        N.check(N.lib().mkf_pf2d_draws(self.seed, self.track_id, int(frame) & 0xFFFFFFFF, self.N, self.d,
+                                       _ptr(eps), _ptr(u), _stream(self.torch, stream)), "mkf_pf2d_draws")
+        return eps, u
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value:
+            N.lib().mkf_pf2d_destroy(h)
+            self.h = None
+
+
 class RaoBlackwellisedPF:
     """pf2DRao ParticleFilter(nParticles) with its my_gmm (pf2DRao.h:13-31):
     loadGaussian / resetTracker / update(measurement) / getEstimator, FP64 on

@@ -78,6 +78,11 @@ class Track(C.Structure):
                 ("kappa", F), ("pd", F), ("sigma", F)]
 
 
+class Pf2dModel(C.Structure):
+    _fields_ = [("d", I), ("K", I), ("mean", P), ("sinv", P), ("det_s", P), ("w", P),
+                ("width", I), ("height", I), ("side", I)]
+
+
 class MixParams(C.Structure):
     _fields_ = [("d", I), ("K", I), ("J", I), ("mu", P), ("a", P), ("Lq", P), ("pi", P), ("S0", P),
                 ("sigma", D), ("fx", D), ("fy", D), ("cx", D), ("cy", D)]
@@ -119,6 +124,11 @@ def _declare(L):
     L.mko_bpf_run_tracks.argtypes = [I, P, I, I, I, P, P, P, P, P, P, P, P,
                                      F, F, F, F, P, P, P, P, P, I]
     L.mko_num_threads.restype = I
+    L.mko_pf2d_load.argtypes = [I, I, P, P, P, P]
+    L.mko_pf2d_init.argtypes = [C.POINTER(Pf2dModel), I, P, P, P]
+    L.mko_pf2d_update.argtypes = [C.POINTER(Pf2dModel), I, P, P, P, U32, P, P, P, P]
+    L.mko_pf2d_update.restype = I
+    L.mko_pf2d_estimate.argtypes = [I, I, P, P, P]
     L.mko_mix_forward.argtypes = [C.POINTER(MixParams), I, C.c_longlong, P, P, D, D, P, P]
     L.mko_mix_forward.restype = D
     L.mko_mix_adjoint.argtypes = [C.POINTER(MixParams), I, C.c_longlong, P, P, D, D, P, P, P, P, P, P]
@@ -471,3 +481,40 @@ def mix_batch(model, batch, grad=False, nthreads=0, tracks=None):
     if grad:
         return tot, ll, np.concatenate(g)
     return tot, ll
+
+
+# ---------------------------------------------------------------- A12 legacy pf2D
+class Pf2d:
+    """FP64 literal restatement of pf2D's ParticleFilter (injected draws)."""
+
+    def __init__(self, mean, cov, w, width=640, height=480, side=0):
+        self.mean = _c(mean, np.float64)
+        self.K, self.d = self.mean.shape
+        self.sinv = np.zeros((self.K, self.d, self.d))
+        self.det_s = np.zeros(self.K)
+        self.w = _c(w, np.float64)
+        lib().mko_pf2d_load(self.d, self.K, _p(self.mean), _p(_c(cov, np.float64)), _p(self.sinv), _p(self.det_s))
+        self.s = Pf2dModel(self.d, self.K, _p(self.mean), _p(self.sinv), _p(self.det_s), _p(self.w),
+                           width, height, side)
+
+    def init(self, u):
+        N = u.shape[0]
+        x = np.zeros((N, self.d))
+        wts = np.zeros(N)
+        lib().mko_pf2d_init(C.byref(self.s), N, _p(_c(u, np.float64)), _p(x), _p(wts))
+        return x, wts
+
+    def update(self, x, wts, z, U, reinit_u, eps):
+        x = _c(x, np.float64).copy()
+        wts = _c(wts, np.float64).copy()
+        N = x.shape[0]
+        wout = np.zeros(N)
+        anc = np.zeros(N, np.int32)
+        r = lib().mko_pf2d_update(C.byref(self.s), N, _p(x), _p(wts), _p(_c(z, np.float64)), U,
+                                  _p(_c(reinit_u, np.float64)), _p(_c(eps, np.float64)), _p(wout), _p(anc))
+        return x, wts, wout, anc, bool(r)
+
+    def estimate(self, x, wts):
+        est = np.zeros(self.d)
+        lib().mko_pf2d_estimate(x.shape[0], self.d, _p(_c(x, np.float64)), _p(_c(wts, np.float64)), _p(est))
+        return est

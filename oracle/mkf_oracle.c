@@ -665,3 +665,91 @@ void mko_bpf_run_tracks(int n_tracks, const mko_track* tracks, int d, int K, int
     free(xa); free(xb); free(lw); free(anc);
   }
 }
+
+/* ------------------------------------------------------------------------ */
+/* A12: legacy bootstrap PF pf2D (pf2D.cpp:13-268)                            */
+/* ------------------------------------------------------------------------ */
+void mko_pf2d_load(int d, int K, const double* mean, const double* cov, double* sinv, double* det_s) {
+  (void)mean;
+  for (int k = 0; k < K; ++k) {
+    const double* S = cov + (size_t)k * d * d;
+    double Lo[64 * 64];
+    chol_lower(d, S, Lo);
+    double ld = 0.0;
+    for (int i = 0; i < d; ++i) ld += 2.0 * log(Lo[i * d + i]);
+    det_s[k] = 1.0 / (pow(2.0 * M_PI, d / 2.0) * sqrt(exp(ld)));   /* pf2D.cpp:35 */
+    inv_lu(d, S, sinv + (size_t)k * d * d);                          /* invert(s, .., DECOMP_CHOLESKY) */
+  }
+}
+
+static void pf2d_uniform_row(const mko_pf2d_model* m, const double* u, double* x) {
+  for (int c = 0; c < m->d; ++c) {
+    double lo = 1.0, hi;
+    if (c == 6) { lo = m->width / 2.0 * m->side + 1.0; hi = m->width / 2.0 + m->width / 2.0 * m->side; }
+    else hi = ((c % 2) == 0) * (double)m->width + (((c + 1) % 2) == 0) * (double)m->height;
+    x[c] = lo + u[c] * (hi - lo);
+  }
+}
+
+void mko_pf2d_init(const mko_pf2d_model* m, int N, const double* u, double* particles, double* weights) {
+  for (int i = 0; i < N; ++i) {
+    pf2d_uniform_row(m, u + (size_t)i * m->d, particles + (size_t)i * m->d);
+    weights[i] = 1.0 / (double)N;
+  }
+}
+
+int mko_pf2d_update(const mko_pf2d_model* m, int N, double* particles, double* weights, const double* z,
+                    uint32_t U, const double* reinit_u, const double* eps, double* w_out, int* anc_out) {
+  const int d = m->d;
+  double sum = 0.0;
+  for (int i = 0; i < N; ++i) {
+    const double* x = particles + (size_t)i * d;
+    double prior = 0.0;
+    for (int k = 0; k < m->K; ++k) {
+      const double* mu = m->mean + (size_t)k * d;
+      const double* Si = m->sinv + (size_t)k * d * d;
+      double q = 0.0;
+      for (int r = 0; r < d; ++r) {
+        double t = 0.0;
+        for (int c = 0; c < d; ++c) t += Si[r * d + c] * (x[c] - mu[c]);
+        q += (x[r] - mu[r]) * t;
+      }
+      prior += m->w[k] * m->det_s[k] * (double)expf((float)(-0.5 * q));
+    }
+    double d0 = x[6] - z[0], d1 = x[7] - z[1], h0 = x[0] - z[2], h1 = x[1] - z[3];
+    double lik = (1.0 / (2.0 * M_PI * 15.0)) * exp(-0.5 * (d0 * d0 + d1 * d1) / 15.0) *
+                 (1.0 / (2.0 * M_PI * 15.0)) * exp(-0.5 * (h0 * h0 + h1 * h1) / 15.0);
+    weights[i] = prior * lik;
+    sum += weights[i];
+  }
+  for (int i = 0; i < N; ++i) weights[i] /= sum;
+  if (w_out) memcpy(w_out, weights, sizeof(double) * (size_t)N);
+  double mw = 0.0;
+  for (int i = 0; i < N; ++i) if (weights[i] > mw) mw = weights[i];
+  int reinit = !(mw > 0.0);
+  double* old = (double*)malloc(sizeof(double) * (size_t)N * d);
+  memcpy(old, particles, sizeof(double) * (size_t)N * d);
+  if (reinit) {
+    for (int i = 0; i < N; ++i) {
+      pf2d_uniform_row(m, reinit_u + (size_t)i * d, particles + (size_t)i * d);
+      weights[i] = 1.0 / (double)N;
+      if (anc_out) anc_out[i] = -1;
+    }
+  } else {
+    int* anc = (int*)malloc(sizeof(int) * (size_t)N);
+    mko_resample_f64(weights, N, N, U, anc);
+    for (int i = 0; i < N; ++i) memcpy(particles + (size_t)i * d, old + (size_t)anc[i] * d, sizeof(double) * (size_t)d);
+    if (anc_out) memcpy(anc_out, anc, sizeof(int) * (size_t)N);
+    free(anc);
+  }
+  for (int i = 0; i < N; ++i)
+    for (int c = 0; c < 8 && c < d; ++c) particles[(size_t)i * d + c] += 5.0 * eps[(size_t)i * 8 + c];
+  free(old);
+  return reinit;
+}
+
+void mko_pf2d_estimate(int N, int d, const double* particles, const double* weights, double* est) {
+  for (int c = 0; c < d; ++c) est[c] = 0.0;
+  for (int i = 0; i < N; ++i)
+    for (int c = 0; c < d; ++c) est[c] += weights[i] * particles[(size_t)i * d + c];
+}

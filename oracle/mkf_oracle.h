@@ -197,6 +197,34 @@ double mko_mix_batch(const mko_mix_params* p, int n_tracks, const int* n_frames,
                      const int* det_off, const float* det, int grad, double* ll, double* g_mu,
                      double* g_a, double* g_Lq, double* g_sigma, int nthreads);
 
+/* ---- A12: legacy bootstrap PF pf2D (pf2D.cpp:13-268), literal semantics.
+ * my_gmm::loadGaussian (pf2D.cpp:26-37): sigma_i = inv(s), det_s =
+ * 1/((2 pi)^(d/2) sqrt(det s)).  update (pf2D.cpp:148-210): prior_i =
+ * sum_k w_k det_k expf(float(-1/2 (x-mu_k) S_k^-1 (x-mu_k)^T)), likelihood_i =
+ * eyemvnpdf(x[6:8]-z0, 15) * eyemvnpdf(x[0:2]-z1, 15) (pf2D.cpp:124-128),
+ * w = prior*lik normalised by their sum; resample (pf2D.cpp:225-268): if the
+ * max weight is 0 every column is redrawn uniformly (ctor ranges,
+ * pf2D.cpp:44-71; reinit_u: N*d uniforms) and the weights reset to 1/N,
+ * otherwise particles <- old[anc] with anc the exact systematic resampling of
+ * the normalised weights and the weights left unchanged (the reference never
+ * resets them, so getEstimator uses stale weights); predict (pf2D.cpp:90-102):
+ * columns 0..7 += N(0, 5^2) (eps: N*8 normals; columns >= 8 get no noise --
+ * the reference adds an uninitialised temporary there).
+ * particles: N*d, weights: N.  Returns 1 if the re-initialisation ran. */
+typedef struct {
+  int d, K;
+  const double* mean;    /* K*d */
+  const double* sinv;    /* K*d*d */
+  const double* det_s;   /* K */
+  const double* w;       /* K */
+  int width, height, side;
+} mko_pf2d_model;
+void mko_pf2d_load(int d, int K, const double* mean, const double* cov, double* sinv, double* det_s);
+void mko_pf2d_init(const mko_pf2d_model* m, int N, const double* u, double* particles, double* weights);
+int mko_pf2d_update(const mko_pf2d_model* m, int N, double* particles, double* weights, const double* z,
+                    uint32_t U, const double* reinit_u, const double* eps, double* w_out, int* anc_out);
+void mko_pf2d_estimate(int N, int d, const double* particles, const double* weights, double* est);
+
 #ifdef __cplusplus
 }
 #endif

@@ -313,3 +313,50 @@ def test_rbpf_alias_quirk_changes_duplicates_only(olib):
     np.testing.assert_allclose(a["logw"][first], b["logw"][first], rtol=1e-12)
     if (~first).any():
         assert not np.allclose(a["logw"][~first], b["logw"][~first])
+
+
+def test_pf2d_oracle_pieces(olib):
+    """Legacy pf2D restatement: constructor ranges, GMM prior density against a
+    direct evaluation, re-initialisation when every weight vanishes, and the
+    estimator as the weighted particle sum."""
+    rng = np.random.default_rng(2)
+    d, K, N = 8, 2, 64
+    mean = rng.uniform(100, 400, (K, d))
+    cov = np.stack([np.diag(rng.uniform(100, 160, d) ** 2) for _ in range(K)])
+    w = np.array([0.3, 0.7])
+    for side in (0, 1):
+        om = olib.Pf2d(mean, cov, w, width=640, height=480, side=side)
+        u = rng.uniform(0, 1, (N, d))
+        x, wt = om.init(u)
+        assert (x[:, 6] >= 320 * side + 1).all() and (x[:, 6] < 320 + 320 * side).all()
+        assert (x[:, 1] < 480).all() and (x[:, 0] < 640).all() and (x[:, 0] >= 1).all()
+        np.testing.assert_array_equal(wt, np.full(N, 1.0 / N))
+    om = olib.Pf2d(mean, cov, w)
+    x, wt = om.init(rng.uniform(0, 1, (N, d)))
+    z = np.array([300.0, 120.0, 260.0, 300.0])
+    eps = rng.normal(0, 1, (N, 8))
+    xn, wn, wout, anc, reinit = om.update(x, wt, z, 12345, rng.uniform(0, 1, (N, d)), eps)
+    assert not reinit
+    prior = np.zeros(N)
+    for k in range(K):
+        dx = x - mean[k]
+        q = np.einsum("ni,ij,nj->n", dx, np.linalg.inv(cov[k]), dx)
+        prior += w[k] * np.exp(-0.5 * q) / np.sqrt((2 * np.pi) ** d * np.linalg.det(cov[k]))
+    c = 1.0 / (2 * np.pi * 15.0)
+    lik = c * np.exp(-0.5 * ((x[:, 6] - z[0]) ** 2 + (x[:, 7] - z[1]) ** 2) / 15.0) * \
+        c * np.exp(-0.5 * ((x[:, 0] - z[2]) ** 2 + (x[:, 1] - z[3]) ** 2) / 15.0)
+    ref = prior * lik / (prior * lik).sum()
+    np.testing.assert_allclose(wout, ref, rtol=1e-5, atol=1e-300)
+    np.testing.assert_array_equal(wn, wout)        # weights stay as normalised (not reset after resampling)
+    a2, _ = olib.resample(wout, N, 12345)
+    np.testing.assert_array_equal(anc, a2)
+    np.testing.assert_array_equal(xn[:, :8], x[anc][:, :8] + 5.0 * eps)
+    np.testing.assert_array_equal(xn[:, 8:], x[anc][:, 8:])
+    np.testing.assert_allclose(om.estimate(xn, wn), (wn[:, None] * xn).sum(0), rtol=1e-13)
+    ru = rng.uniform(0, 1, (N, d))
+    xr, wr, _, ar, reinit = om.update(x, wt, np.array([-1e4, -1e4, -1e4, -1e4]), 1, ru, eps)
+    assert reinit and (ar == -1).all()
+    np.testing.assert_array_equal(wr, np.full(N, 1.0 / N))
+    x2, _ = om.init(ru)
+    x2[:, :8] += 5.0 * eps
+    np.testing.assert_array_equal(xr, x2)
