@@ -348,27 +348,38 @@ def run_sweep(args):
         ll = torch.empty(T, dtype=torch.float32, device="cuda")
         ess = torch.empty(T, dtype=torch.float32, device="cuda")
 
-        def run_all():
-            pf.reset()
+        def timed(frames_fn):
+            tot = 0.0
+            for rep in range(args.warmup + args.steps):
+                pf.reset()
+                e0, e1 = _events(torch)
+                e0.record()
+                frames_fn()
+                e1.record()
+                torch.cuda.synchronize()
+                if rep >= args.warmup:
+                    tot += e0.elapsed_time(e1) / 1000
+            return tot / args.steps
+
+        def loop():
             for f in range(T):
                 pf.update(f, offs[f * J:], det, est=est[f], loglik=ll[f], ess=ess[f])
 
-        for _ in range(args.warmup):
-            run_all()
-        torch.cuda.synchronize()
-        e0, e1 = _events(torch)
-        e0.record()
-        for _ in range(args.steps):
-            run_all()
-        e1.record()
-        torch.cuda.synchronize()
-        sec = e0.elapsed_time(e1) / 1000 / args.steps
+        sec = timed(loop)
+        pf.reset()
+        graph = pf.capture(T, offs, det, est, ll, ess)
+        sec_g = timed(lambda: graph.launch(0))
+        del graph
         pfs = N * T / sec
         ach = BYTES_PER_PF * N * T / sec / 1e9
+        ach_g = BYTES_PER_PF * N * T / sec_g / 1e9
         rows.append({"N": N, "T": T, "ms_per_track": sec * 1e3, "particle_frames_per_s": pfs,
                      "track_frames_per_s": T / sec, "achieved_GBps": ach, "frac_of_" + peak_kind + "_hbm": ach / peak,
+                     "graph_ms_per_track": sec_g * 1e3, "graph_particle_frames_per_s": N * T / sec_g,
+                     "graph_us_per_frame": sec_g / T * 1e6, "graph_frac_of_" + peak_kind + "_hbm": ach_g / peak,
                      "l2_resident": N <= (1 << 18)})
-    print(json.dumps({"workload": "particle-count sweep, one track, T=%d, plain per-track path" % T,
+    print(json.dumps({"workload": "particle-count sweep, one track, T=%d, plain per-track path: "
+                                  "one C-ABI call per frame, and the frame loop captured as one CUDA graph" % T,
                       "unit": "particle-frames/s", "peak_hbm_GBps": peak, "rows": rows}), flush=True)
 
 

@@ -307,6 +307,25 @@ int mkf_pdaf_associate(mkf_rbpf_t arm0, mkf_rbpf_t arm1, uint32_t frame, const d
                        const double* d_cand, int M, double Pa, double clutter, double* d_meas0,
                        double* d_meas1, int* d_bins0, int* d_bins1, mkf_stream_t stream);
 
+/* ------------------------------------- f2 pose decode and 3-D back-projection */
+/* For B estimates x (B*d, device): e = Hpca^T x + mpca (pfPose.cpp:347-348;
+ * Hpca d*F row-major and mpca F, device) into d_e (B*F, optional), and the
+ * get3Dpose back-projection (pfPose.cpp:93-127) into d_pos3d (B*15: per
+ * estimate a 3x5 row-major matrix, columns hand, elbow, shoulder, head, neck;
+ * optional, needs F >= 21): full state (u, v, Z) per joint at 0..14, yaw 15,
+ * roll 16, pitch 17, t 18..20; R = R3(yaw) R2(pitch) R1(roll); P = Kc [R | t];
+ * point = inv(P[:, 0:3]) ((u Z, v Z, Z) - P[:, 3]).  Kc: host 3x3 camera
+ * matrix.  A singular P[:, 0:3] gives NaN points and sets MKF_ST_NONPD in
+ * *d_status (device int).  1 <= d <= 24, 1 <= F <= 64. */
+int mkf_pose_decode(const double* d_x, int B, int d, int F, const double* d_Hpca, const double* d_mpca,
+                    const double* Kc, double* d_e, double* d_pos3d, int* d_status, mkf_stream_t stream);
+/* publish2Dpos point record (pfPose.cpp:173-208) for B frames from both arms'
+ * decoded vectors e1, e2 (B*F each, device): 8 (x, y) points per frame into
+ * d_pts (B*16): hand1, hand2, head and neck (means of both arms), elbow1,
+ * elbow2, shoulder1, shoulder2.  F >= 14. */
+int mkf_pose2d_record(const double* d_e1, const double* d_e2, int B, int F, double* d_pts,
+                      mkf_stream_t stream);
+
 /* ------------------------------------------- A11 mixture KF forward / adjoint */
 /* Deterministic counterpart of ParticleFilter::update (pf2DRao.cpp:125-158):
  * per frame every component k predicts from the collapsed posterior

@@ -76,5 +76,39 @@ def build(force: bool = False, verbose: bool = False, ptxas_v: bool = False) -> 
     return LIB
 
 
+HARNESS_DIR = os.path.join(HERE, "harness")
+HARNESS = os.path.join(HARNESS_DIR, "mkf_harness")
+INCLUDE = os.path.join(HERE, "..", "include")
+
+
+def cuda_home() -> str:
+    return os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+
+
+def build_harness(force: bool = False) -> str:
+    """The standalone C++ harness (host code only, g++), linked against
+    libmkf_gb300.so (found next to the package through its rpath) and the
+    static CUDA runtime."""
+    lib = build()
+    src = os.path.join(HARNESS_DIR, "mkf_harness.cpp")
+    deps = [src, lib, os.path.join(HARNESS_DIR, "mkf_yaml.hpp"), os.path.join(INCLUDE, "mkf_gb300.hpp"),
+            os.path.join(INCLUDE, "mkf_gb300.h")]
+    if not force and not _stale(HARNESS, deps):
+        return HARNESS
+    cxx = shutil.which("g++") or "g++"
+    cuda = cuda_home()
+    tmp = HARNESS + ".tmp%d" % os.getpid()
+    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I", INCLUDE, "-I", os.path.join(cuda, "include"), src, "-o", tmp,
+           "-L", HERE, "-lmkf_gb300", "-Wl,-rpath,$ORIGIN/..", "-L", os.path.join(cuda, "lib64"),
+           "-lcudart_static", "-ldl", "-lpthread", "-lrt"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode:
+        sys.stderr.write(r.stdout + r.stderr)
+        raise RuntimeError("g++ failed on the harness")
+    os.replace(tmp, HARNESS)
+    return HARNESS
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True, ptxas_v="--ptxas-v" in sys.argv))
+    print(build_harness(force="--force" in sys.argv))

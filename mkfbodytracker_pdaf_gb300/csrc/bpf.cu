@@ -521,8 +521,17 @@ struct StreamArgs {
   float* out_ess;
   float* dbg_w;
   int* anc_out;
+  const uint32_t* frame_base;   // device frame offset (graph replays), or null
   bool prior;
 };
+
+// frame index of this step: a.frame, plus the device offset when replayed from a graph
+__device__ __forceinline__ uint32_t step_frame(const StreamArgs& A) {
+  return A.frame_base ? A.frame + *A.frame_base : A.frame;
+}
+__device__ __forceinline__ uint32_t step_uniform(const StreamArgs& A) {
+  return A.frame_base ? resample_uniform(A.seed, A.track, step_frame(A)) : A.U;
+}
 
 // online merge of (m, s, s2, v) accumulators
 template <int D>
@@ -610,6 +619,7 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
   for (int r = 0; r < D; ++r) v[r] = 0.0f;
   const int base = blockIdx.x * A.tile_a;
   const int end = min(A.N, base + A.tile_a);
+  const uint32_t frame = step_frame(A);
   for (int i = base + tid; i < end; i += TB) {
     float x[D], eps[D];
     if (A.prior) {
@@ -622,7 +632,7 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
     const int an = A.anc[i];
 #pragma unroll
     for (int r = 0; r < D; ++r) x[r] = A.xa[(size_t)r * A.N + an];
-    float uc = particle_draws<D>(A.seed, A.track, A.frame, (uint32_t)i, eps);
+    float uc = particle_draws<D>(A.seed, A.track, frame, (uint32_t)i, eps);
     propagate<D, DIAG>(A.pv, eps, uc, x);
 #pragma unroll
     for (int r = 0; r < D; ++r) A.xb[(size_t)r * A.N + i] = x[r];
@@ -747,8 +757,9 @@ __global__ void __launch_bounds__(256) bpf_stream_c(StreamArgs A, int tile_c) {
   const int fb = A.fs->fb;
   const uint64_t Qt = A.fs->Qt;
   const int base = blockIdx.x * tile_c, end = min(A.N, base + tile_c), n = end - base;
+  const uint32_t U = step_uniform(A);
   if (fb) {
-    for (int i = base + tid; i < end; i += TB) A.anc_out[i] = resample_fallback_index(A.U, i, A.N);
+    for (int i = base + tid; i < end; i += TB) A.anc_out[i] = resample_fallback_index(U, i, A.N);
     return;
   }
   const int E = (tile_c + TB - 1) / TB;
@@ -763,12 +774,12 @@ __global__ void __launch_bounds__(256) bpf_stream_c(StreamArgs A, int tile_c) {
   }
   if (tid == 0) {
     uint64_t Xprev = A.bsum[blockIdx.x];
-    s_lo = (blockIdx.x == 0) ? 0 : count_targets_le(Xprev, A.N, A.U, Qt);
-    s_hi = (blockIdx.x == gridDim.x - 1) ? A.N : count_targets_le(Xprev + tot, A.N, A.U, Qt);
+    s_lo = (blockIdx.x == 0) ? 0 : count_targets_le(Xprev, A.N, U, Qt);
+    s_hi = (blockIdx.x == gridDim.x - 1) ? A.N : count_targets_le(Xprev + tot, A.N, U, Qt);
   }
   __syncthreads();
   for (int i = s_lo + tid; i < s_hi; i += TB)
-    A.anc_out[i] = base + resample_search(sQ, n, A.N, resample_rhs(i, A.U, Qt));
+    A.anc_out[i] = base + resample_search(sQ, n, A.N, resample_rhs(i, U, Qt));
 }
 
 // ------------------------------------------------------------------ handles
@@ -846,9 +857,18 @@ extern "C" int mkf_bpf_create(const mkf_bpf_models* models, const mkf_bpf_track*
   h.tr = *track;
   h.N = track->n_particles;
   h.d = models->d;
-  h.tile_a = kTileA; h.tile_b = kTileB;
-  h.nb_a = (h.N + kTileA - 1) / kTileA;
-  h.nb_b = (h.N + kTileB - 1) / kTileB;
+  // tiles: at most kTileA / kTileB particles per block, fewer when N is small so
+  // that a frame spreads over about 4 (propagate) / 2 (sums, search) blocks per SM
+  const int sms = num_sms();
+  auto tile_for = [&](int cap, int per_sm) {
+    int t = (h.N + per_sm * sms - 1) / (per_sm * sms);
+    t = (t + kStreamTB - 1) / kStreamTB * kStreamTB;
+    return std::min(cap, std::max(kStreamTB, t));
+  };
+  h.tile_a = tile_for(kTileA, 4);
+  h.tile_b = tile_for(kTileB, 2);
+  h.nb_a = (h.N + h.tile_a - 1) / h.tile_a;
+  h.nb_b = (h.N + h.tile_b - 1) / h.tile_b;
   const size_t N = h.N, d = h.d;
   cudaError_t e = cudaSuccess;
   if (e == cudaSuccess) e = cudaMalloc(&h.xa, N * d * sizeof(float));
@@ -908,15 +928,13 @@ extern "C" int mkf_bpf_reset(mkf_bpf_t H, mkf_stream_t stream) {
   return MKF_OK;
 }
 
-extern "C" int mkf_bpf_update(mkf_bpf_t H, uint32_t frame, const int* d_det_off, const float* d_det,
-                              float* d_est, float* d_loglik, float* d_ess, mkf_stream_t stream) {
-  MKF_ARG(H && d_det_off, "mkf_bpf_update: null argument");
-  BpfHandle& h = H->h;
-  if (!h.ready) { set_error("mkf_bpf_update: call mkf_bpf_reset first"); return MKF_ERR_STATE; }
-  cudaStream_t s = (cudaStream_t)stream;
+// one frame: propagate+score, block sums, ancestor search (three launches on s)
+static int enqueue_update(BpfHandle& h, uint32_t frame, const uint32_t* frame_base, const int* d_det_off,
+                          const float* d_det, float* d_est, float* d_loglik, float* d_ess, cudaStream_t s) {
   StreamArgs a = stream_args(h);
   a.frame = frame;
-  a.U = resample_uniform(h.tr.seed, h.tr.track_id, frame);
+  a.frame_base = frame_base;
+  a.U = frame_base ? 0u : resample_uniform(h.tr.seed, h.tr.track_id, frame);
   a.det_off = d_det_off;
   a.det = reinterpret_cast<const float2*>(d_det);
   a.anc = h.anc; a.xa = h.xa; a.xb = h.xb; a.logw = h.logw;
@@ -930,6 +948,92 @@ extern "C" int mkf_bpf_update(mkf_bpf_t H, uint32_t frame, const int* d_det_off,
   bpf_stream_c<<<h.nb_b, kStreamTB, (size_t)h.tile_b * sizeof(uint64_t), s>>>(a, h.tile_b);
   MKF_CHECK_LAUNCH("mkf_bpf_update: search kernel");
   std::swap(h.xa, h.xb);
+  return MKF_OK;
+}
+
+extern "C" int mkf_bpf_update(mkf_bpf_t H, uint32_t frame, const int* d_det_off, const float* d_det,
+                              float* d_est, float* d_loglik, float* d_ess, mkf_stream_t stream) {
+  MKF_ARG(H && d_det_off, "mkf_bpf_update: null argument");
+  BpfHandle& h = H->h;
+  if (!h.ready) { set_error("mkf_bpf_update: call mkf_bpf_reset first"); return MKF_ERR_STATE; }
+  return enqueue_update(h, frame, nullptr, d_det_off, d_det, d_est, d_loglik, d_ess, (cudaStream_t)stream);
+}
+
+// ------------------------------------------------------------- captured frame loops
+struct mkf_bpf_graph {
+  mkf_bpf_t owner;
+  int n_frames;
+  uint32_t* frame_base;          // device
+  cudaGraphExec_t exec;
+};
+
+__global__ void set_frame_base_kernel(uint32_t* p, uint32_t v) { *p = v; }
+
+extern "C" int mkf_bpf_graph_create(mkf_bpf_t H, int n_frames, const int* d_det_off, const float* d_det,
+                                    float* d_est, float* d_loglik, float* d_ess, mkf_bpf_graph_t* out) {
+  MKF_ARG(H && out && d_det_off && n_frames >= 1, "mkf_bpf_graph_create: bad argument");
+  BpfHandle& h = H->h;
+  if (!h.ready) { set_error("mkf_bpf_graph_create: call mkf_bpf_reset first"); return MKF_ERR_STATE; }
+  mkf_bpf_graph* g = new (std::nothrow) mkf_bpf_graph();
+  if (!g) return MKF_ERR_NOMEM;
+  g->owner = H; g->n_frames = n_frames; g->frame_base = nullptr; g->exec = nullptr;
+  cudaError_t e = cudaMalloc(&g->frame_base, sizeof(uint32_t));
+  if (e != cudaSuccess) { delete g; return cuda_fail(e, "mkf_bpf_graph_create: allocation", __FILE__, __LINE__); }
+  cudaStream_t cs = nullptr;
+  e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    if (cs) cudaStreamDestroy(cs);
+    cudaFree(g->frame_base); delete g;
+    return cuda_fail(e, "mkf_bpf_graph_create: capture start", __FILE__, __LINE__);
+  }
+  float* const x0 = h.xa;
+  const int J = h.m.J;
+  int rc = MKF_OK;
+  for (int t = 0; t < n_frames && rc == MKF_OK; ++t)
+    rc = enqueue_update(h, (uint32_t)t, g->frame_base, d_det_off + (size_t)t * J, d_det,
+                        d_est ? d_est + (size_t)t * h.d : nullptr, d_loglik ? d_loglik + t : nullptr,
+                        d_ess ? d_ess + t : nullptr, cs);
+  // an odd number of frames ends in the other buffer: copy back so that launches chain
+  if (h.xa != x0) {
+    if (rc == MKF_OK) {
+      cudaError_t ce = cudaMemcpyAsync(x0, h.xa, sizeof(float) * (size_t)h.N * h.d, cudaMemcpyDeviceToDevice, cs);
+      if (ce != cudaSuccess) rc = cuda_fail(ce, "mkf_bpf_graph_create: copy-back", __FILE__, __LINE__);
+    }
+    std::swap(h.xa, h.xb);
+  }
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(cs, &graph);
+  if (rc == MKF_OK && e != cudaSuccess) rc = cuda_fail(e, "mkf_bpf_graph_create: capture end", __FILE__, __LINE__);
+  if (rc == MKF_OK) {
+    e = cudaGraphInstantiate(&g->exec, graph, 0);
+    if (e != cudaSuccess) rc = cuda_fail(e, "mkf_bpf_graph_create: instantiate", __FILE__, __LINE__);
+  }
+  if (graph) cudaGraphDestroy(graph);
+  cudaStreamDestroy(cs);
+  if (rc != MKF_OK) {
+    cudaGetLastError();
+    cudaFree(g->frame_base); delete g;
+    return rc;
+  }
+  *out = g;
+  return MKF_OK;
+}
+
+extern "C" int mkf_bpf_graph_launch(mkf_bpf_graph_t g, uint32_t frame0, mkf_stream_t stream) {
+  MKF_ARG(g && g->exec, "mkf_bpf_graph_launch: null graph");
+  cudaStream_t s = (cudaStream_t)stream;
+  set_frame_base_kernel<<<1, 1, 0, s>>>(g->frame_base, frame0);
+  MKF_CHECK_LAUNCH("mkf_bpf_graph_launch: frame offset");
+  MKF_CUDA(cudaGraphLaunch(g->exec, s));
+  return MKF_OK;
+}
+
+extern "C" int mkf_bpf_graph_destroy(mkf_bpf_graph_t g) {
+  if (!g) return MKF_OK;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->frame_base) cudaFree(g->frame_base);
+  delete g;
   return MKF_OK;
 }
 

@@ -102,3 +102,46 @@ def load_reference_models(left_path: str, right_path: str, gamma_from_right: boo
     if gamma_from_right:
         arms[0]["gamma"] = arms[1]["gamma"].copy()
     return arms
+
+
+def dump(doc: dict) -> str:
+    """OpenCV FileStorage YAML text for a dict of numpy matrices (written as
+    ``!!opencv-matrix``; float32 arrays get dt f, everything else dt d, 1-D
+    arrays become 1 x n) and scalars.  ``parse(dump(doc))`` returns the same
+    values: 17 significant digits for doubles, 9 for floats."""
+    out = ["%YAML:1.0"]
+    for key, v in doc.items():
+        if isinstance(v, (int, float, str)) and not isinstance(v, bool):
+            out.append("%s: %s" % (key, v if not isinstance(v, float) else repr(v)))
+            continue
+        a = np.asarray(v)
+        if a.ndim == 1:
+            a = a.reshape(1, -1)
+        if a.ndim != 2:
+            raise ValueError("%s: only 2-D matrices are written" % key)
+        dt = "f" if a.dtype == np.float32 else "d"
+        fmt = "%.9g" if dt == "f" else "%.17g"
+        vals = [fmt % x for x in a.astype(np.float64).ravel()]
+        lines = [", ".join(vals[i:i + 2]) for i in range(0, len(vals), 2)]
+        out.append("%s: !!opencv-matrix\n   rows: %d\n   cols: %d\n   dt: %s\n   data: [ %s ]"
+                   % (key, a.shape[0], a.shape[1], dt, ",\n       ".join(lines)))
+    return "\n".join(out) + "\n"
+
+
+def save(path: str, doc: dict) -> None:
+    with open(path, "w") as f:
+        f.write(dump(doc))
+
+
+def save_arm_model(path: str, means, covs, weights, pca_proj, pca_mean, gamma) -> None:
+    """One arm's model file in the layout the tracker reads (pfPose.cpp:37-53):
+    means K x d, covs (K*d) x d, weights 1 x K, pca_proj d x F (float, as
+    shipped), pca_mean 1 x F, gamma K x 1."""
+    means = np.asarray(means, np.float64)
+    K, d = means.shape
+    save(path, {"means": means,
+                "covs": np.asarray(covs, np.float64).reshape(K * d, d),
+                "weights": np.asarray(weights, np.float64).reshape(1, K),
+                "pca_proj": np.asarray(pca_proj, np.float32),
+                "pca_mean": np.asarray(pca_mean, np.float64).reshape(1, -1),
+                "gamma": np.asarray(gamma, np.float64).reshape(K, 1)})

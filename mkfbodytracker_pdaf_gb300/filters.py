@@ -108,11 +108,43 @@ class BootstrapParticleFilter:
         N.check(N.lib().mkf_bpf_status(self.h, C.byref(s)), "mkf_bpf_status")
         return s.value
 
+    def capture(self, n_frames, det_off, det, est=None, loglik=None, ess=None):
+        """Record n_frames consecutive updates into a CUDA graph (FrameGraph).
+        det_off: int32 CUDA tensor (n_frames*J + 1) of offsets into det; est
+        (n_frames, d), loglik, ess (n_frames): CUDA tensors or None."""
+        return FrameGraph(self, n_frames, det_off, det, est, loglik, ess)
+
     def __del__(self):
         try:
             if getattr(self, "h", None):
                 N.lib().mkf_bpf_destroy(self.h)
                 self.h = None
+        except Exception:
+            pass
+
+
+class FrameGraph:
+    """A captured frame loop of one BootstrapParticleFilter; launch(frame0) runs
+    frames frame0 .. frame0 + n_frames - 1 from the buffers bound at capture."""
+
+    def __init__(self, pf, n_frames, det_off, det, est, loglik, ess):
+        self.pf = pf                      # keeps the filter (and its buffers) alive
+        self.n_frames = int(n_frames)
+        self.buffers = (det_off, det, est, loglik, ess)
+        g = C.c_void_p()
+        N.check(N.lib().mkf_bpf_graph_create(pf.h, self.n_frames, _ptr(det_off), _ptr(det), _ptr(est),
+                                             _ptr(loglik), _ptr(ess), C.byref(g)), "mkf_bpf_graph_create")
+        self.g = g
+
+    def launch(self, frame0=0, stream=None):
+        N.check(N.lib().mkf_bpf_graph_launch(self.g, int(frame0) & 0xFFFFFFFF, _stream(self.pf.torch, stream)),
+                "mkf_bpf_graph_launch")
+
+    def __del__(self):
+        try:
+            if getattr(self, "g", None):
+                N.lib().mkf_bpf_graph_destroy(self.g)
+                self.g = None
         except Exception:
             pass
 

@@ -422,3 +422,40 @@ def config3_batch(n_tracks=1024, T=1000, seed=MASTER_SEED + 3):
 def config4_batch(n_tracks=16384, T=500, seed=MASTER_SEED + 4):
     """Fitting workload: ground-truth GMM K=32, d=24 (8 joints x 3D), lambda=5."""
     return make_mix_batch(seed, n_tracks, T, K=32, d=24, lam=5.0, pd=0.9, layout="body8")
+
+
+# ------------------------------------------------- reference-model (LINEAR) scene
+def make_reference_scene(arms, T=60, seed=MASTER_SEED + 7, clutter_rate=3.0, sigma_px=4.0, roi_w=40.0,
+                         no_face_every=0):
+    """A synthetic sequence for the shipped (u, v, Z)-state models: each arm's
+    latent state follows the AR(1) of one of its components; per frame the head
+    ROI is placed so that its centre and the 1.65-height neck point match the
+    decoded head and neck (as PFTracker reads them, pfPose.cpp:303-323); hand
+    candidates are both decoded hands + N(0, sigma_px^2) plus Poisson clutter
+    over the 640 x 480 image.  arms: dicts of means, covs, weights, pca_proj,
+    pca_mean, gamma (cvyaml.load_reference_models)."""
+    rng = np.random.default_rng(seed)
+    d = arms[0]["means"].shape[1]
+    xs = np.zeros((2, T, d))
+    for a, arm in enumerate(arms):
+        k = int(rng.integers(0, arm["means"].shape[0]))
+        g = float(arm["gamma"][k])
+        mu = arm["means"][k]
+        L = np.linalg.cholesky(arm["covs"][k * d:(k + 1) * d] + 1e-9 * np.eye(d))
+        x = mu.copy()
+        for t in range(T):
+            x = g * x + (1 - g) * mu + np.sqrt(max(1 - g * g, 0.0)) * (L @ rng.normal(0, 1, d))
+            xs[a, t] = x
+    e = np.stack([xs[a] @ arms[a]["pca_proj"] + arms[a]["pca_mean"] for a in range(2)])
+    rois, cands = [], []
+    for t in range(T):
+        head = 0.5 * (e[0, t, 9:11] + e[1, t, 9:11])
+        neck = 0.5 * (e[0, t, 12:14] + e[1, t, 12:14])
+        h = max(abs(neck[1] - head[1]) / 1.15, 10.0)
+        roi = np.array([head[0] - roi_w / 2, head[1] - h / 2, roi_w, h])
+        rois.append(None if (no_face_every and t % no_face_every == no_face_every - 1) else np.stack([roi, roi]))
+        c = [e[a, t, 0:2] + rng.normal(0, sigma_px, 2) for a in range(2)]
+        nc = rng.poisson(clutter_rate)
+        c += [rng.uniform([0, 0], [640, 480]) for _ in range(nc)]
+        cands.append(np.array(c))
+    return xs, e, rois, cands

@@ -124,6 +124,9 @@ def _declare(L):
     L.mko_bpf_run_tracks.argtypes = [I, P, I, I, I, P, P, P, P, P, P, P, P,
                                      F, F, F, F, P, P, P, P, P, I]
     L.mko_num_threads.restype = I
+    L.mko_pose_decode.argtypes = [I, I, P, P, P, P]
+    L.mko_pose3d.argtypes = [P, P, P]
+    L.mko_pose2d_record.argtypes = [P, P, P]
     L.mko_pf2d_load.argtypes = [I, I, P, P, P, P]
     L.mko_pf2d_init.argtypes = [C.POINTER(Pf2dModel), I, P, P, P]
     L.mko_pf2d_update.argtypes = [C.POINTER(Pf2dModel), I, P, P, P, U32, P, P, P, P]
@@ -518,3 +521,27 @@ class Pf2d:
         est = np.zeros(self.d)
         lib().mko_pf2d_estimate(x.shape[0], self.d, _p(_c(x, np.float64)), _p(_c(wts, np.float64)), _p(est))
         return est
+
+
+# ---------------------------------------------------------------- f2 pose decode
+KINECT_K = np.array([[525.0, 0.0, 319.5], [0.0, 525.0, 239.5], [0.0, 0.0, 1.0]])
+
+
+def pose_decode(Hpca, mpca, x):
+    Hpca = _c(Hpca, np.float64)
+    d, F = Hpca.shape
+    e = np.zeros(F)
+    lib().mko_pose_decode(d, F, _p(Hpca), _p(_c(mpca, np.float64)), _p(_c(x, np.float64)), _p(e))
+    return e
+
+
+def pose3d(e, Kc=KINECT_K):
+    out = np.zeros((3, 5))
+    lib().mko_pose3d(_p(_c(e, np.float64)), _p(_c(Kc, np.float64)), _p(out))
+    return out
+
+
+def pose2d_record(e1, e2):
+    out = np.zeros(16)
+    lib().mko_pose2d_record(_p(_c(e1, np.float64)), _p(_c(e2, np.float64)), _p(out))
+    return out.reshape(8, 2)

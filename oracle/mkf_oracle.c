@@ -753,3 +753,54 @@ void mko_pf2d_estimate(int N, int d, const double* particles, const double* weig
   for (int i = 0; i < N; ++i)
     for (int c = 0; c < d; ++c) est[c] += weights[i] * particles[(size_t)i * d + c];
 }
+
+/* ------------------------------------------------------------------------ */
+/* f2: pose decode and 3-D back-projection (pfPose.cpp:84-127, 173-208)      */
+/* ------------------------------------------------------------------------ */
+void mko_pose_decode(int d, int F, const double* Hpca, const double* mpca, const double* x, double* e) {
+  for (int f = 0; f < F; ++f) {          /* pfPose.cpp:347-348: e = (H_pca^T x + m_pca^T)^T */
+    double s = 0.0;
+    for (int r = 0; r < d; ++r) s += Hpca[(size_t)r * F + f] * x[r];
+    e[f] = s + mpca[f];
+  }
+}
+
+static void mat3_mul(const double* A, const double* B, double* C) {
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double s = 0.0;
+      for (int k = 0; k < 3; ++k) s += A[i * 3 + k] * B[k * 3 + j];
+      C[i * 3 + j] = s;
+    }
+}
+
+void mko_pose3d(const double* e, const double* Kc, double* pos3d) {
+  const double roll = e[16], pitch = e[17], yaw = e[15];       /* pfPose.cpp:104 */
+  const double R1[9] = {1, 0, 0, 0, cos(roll), -sin(roll), 0, sin(roll), cos(roll)};
+  const double R2[9] = {cos(pitch), 0, sin(pitch), 0, 1, 0, -sin(pitch), 0, cos(pitch)};
+  const double R3[9] = {cos(yaw), -sin(yaw), 0, sin(yaw), cos(yaw), 0, 0, 0, 1};
+  double T1[9], R[9], P3[9], Pi[9];
+  mat3_mul(R3, R2, T1);
+  mat3_mul(T1, R1, R);                                          /* rpy: R3 R2 R1 (pfPose.cpp:91) */
+  mat3_mul(Kc, R, P3);
+  double p4[3];
+  for (int i = 0; i < 3; ++i) p4[i] = Kc[i * 3 + 0] * e[18] + Kc[i * 3 + 1] * e[19] + Kc[i * 3 + 2] * e[20];
+  inv_lu(3, P3, Pi);                                            /* invert(.., DECOMP_LU) */
+  for (int k = 0; k < 5; ++k) {
+    const double Z = e[3 * k + 2];
+    const double ip[3] = {e[3 * k] * Z - p4[0], e[3 * k + 1] * Z - p4[1], Z - p4[2]};
+    for (int i = 0; i < 3; ++i)
+      pos3d[i * 5 + k] = Pi[i * 3 + 0] * ip[0] + Pi[i * 3 + 1] * ip[1] + Pi[i * 3 + 2] * ip[2];
+  }
+}
+
+void mko_pose2d_record(const double* e1, const double* e2, double* p) {
+  p[0] = e1[0]; p[1] = e1[1];                                   /* hand1 */
+  p[2] = e2[0]; p[3] = e2[1];                                   /* hand2 */
+  p[4] = 0.5 * (e1[9] + e2[9]); p[5] = 0.5 * (e1[10] + e2[10]); /* head */
+  p[6] = 0.5 * (e1[12] + e2[12]); p[7] = 0.5 * (e1[13] + e2[13]); /* neck */
+  p[8] = e1[3]; p[9] = e1[4];                                   /* elbow1 */
+  p[10] = e2[3]; p[11] = e2[4];                                 /* elbow2 */
+  p[12] = e1[6]; p[13] = e1[7];                                 /* shoulder1 */
+  p[14] = e2[6]; p[15] = e2[7];                                 /* shoulder2 */
+}

@@ -225,6 +225,18 @@ int mko_pf2d_update(const mko_pf2d_model* m, int N, double* particles, double* w
                     uint32_t U, const double* reinit_u, const double* eps, double* w_out, int* anc_out);
 void mko_pf2d_estimate(int N, int d, const double* particles, const double* weights, double* est);
 
+/* ---- f2: pose decode and 3-D back-projection (pfPose.cpp:84-127, 173-208, 347-348)
+ * e = Hpca^T x + mpca (F values, Hpca is d x F row-major), then get3Dpose: full
+ * state (u, v, Z) for joints hand, elbow, shoulder, head, neck at 0..14, roll,
+ * pitch, yaw at 16, 17, 15 and t at 18..20; R = R3(yaw) R2(pitch) R1(roll);
+ * P = Kc [R | t]; point k = inv(P[:, 0:3]) ((u Z, v Z, Z) - P[:, 3]) with a
+ * 3x3 LU inverse (DECOMP_LU).  pos3d: 3 x 5 row-major (x; y; z rows). */
+void mko_pose_decode(int d, int F, const double* Hpca, const double* mpca, const double* x, double* e);
+void mko_pose3d(const double* e, const double* Kc, double* pos3d);
+/* publish2Dpos record (pfPose.cpp:173-208): 8 (x, y) points: hand1, hand2, head
+ * (mean of both arms), neck (mean), elbow1, elbow2, shoulder1, shoulder2 */
+void mko_pose2d_record(const double* e1, const double* e2, double* pts16);
+
 #ifdef __cplusplus
 }
 #endif

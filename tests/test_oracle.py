@@ -360,3 +360,33 @@ def test_pf2d_oracle_pieces(olib):
     x2, _ = om.init(ru)
     x2[:, :8] += 5.0 * eps
     np.testing.assert_array_equal(xr, x2)
+
+
+def test_pose3d_oracle_against_closed_form(olib):
+    """get3Dpose restatement: the back-projected points re-project through
+    K [R | t] onto (u, v) with depth scale Z, and R is a rotation."""
+    rng = np.random.default_rng(4)
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_models.npz"))
+    for a in range(2):
+        H, m = z["arm%d_pca_proj" % a], z["arm%d_pca_mean" % a]
+        x = z["arm%d_means" % a][rng.integers(0, 15)] + rng.normal(0, 0.5, 12)
+        e = olib.pose_decode(H, m, x)
+        np.testing.assert_allclose(e, H.T @ x + m, rtol=1e-13, atol=1e-12)
+        p = olib.pose3d(e)
+        r, pi, y = e[16], e[17], e[15]
+        R1 = np.array([[1, 0, 0], [0, np.cos(r), -np.sin(r)], [0, np.sin(r), np.cos(r)]])
+        R2 = np.array([[np.cos(pi), 0, np.sin(pi)], [0, 1, 0], [-np.sin(pi), 0, np.cos(pi)]])
+        R3 = np.array([[np.cos(y), -np.sin(y), 0], [np.sin(y), np.cos(y), 0], [0, 0, 1]])
+        R = R3 @ R2 @ R1
+        P = olib.KINECT_K @ np.hstack([R, e[18:21, None]])
+        proj = P @ np.vstack([p, np.ones((1, 5))])
+        for k in range(5):
+            Zk = e[3 * k + 2]
+            np.testing.assert_allclose(proj[:, k], [e[3 * k] * Zk, e[3 * k + 1] * Zk, Zk], rtol=1e-9, atol=1e-9)
+    e1, e2 = rng.normal(0, 100, 22), rng.normal(0, 100, 22)
+    rec = olib.pose2d_record(e1, e2)
+    np.testing.assert_array_equal(rec[0], e1[0:2])
+    np.testing.assert_array_equal(rec[1], e2[0:2])
+    np.testing.assert_array_equal(rec[2], 0.5 * (e1[9:11] + e2[9:11]))
+    np.testing.assert_array_equal(rec[3], 0.5 * (e1[12:14] + e2[12:14]))
+    np.testing.assert_array_equal(rec[4:], np.stack([e1[3:5], e2[3:5], e1[6:8], e2[6:8]]))
