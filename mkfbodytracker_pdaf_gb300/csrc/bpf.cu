@@ -94,9 +94,12 @@ struct PView {
   float fx, fy, cx, cy;
 };
 
+// first k with u < cumpi[k] (the last component if none): with cumpi
+// nondecreasing that is the number of c < K-1 with cumpi[c] <= u, counted with
+// independent loads instead of a dependent walk
 __device__ __forceinline__ int pick_component(const float* cumpi, int K, float u) {
   int k = 0;
-  while (k < K - 1 && !(u < cumpi[k])) ++k;
+  for (int c = 0; c < K - 1; ++c) k += (u >= cumpi[c]) ? 1 : 0;
   return k;
 }
 
@@ -337,7 +340,10 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
     }
     __syncthreads();
 
-    const int E = (N + TB - 1) / TB;                 // contiguous chunk per thread
+    // contiguous chunk per thread, an odd number of elements so that a warp's
+    // chunk-wise shared-memory accesses fall in distinct banks
+    int E = (N + TB - 1) / TB;
+    if (E > 1 && !(E & 1)) ++E;
     const int j0 = min(N, tid * E), j1 = min(N, j0 + E);
     for (int t = 0; t < T; ++t) {
       const long long g = g0 + t;
@@ -412,7 +418,10 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
         float ll = SEARCH ? __int_as_float(sA[i]) : sW[i];
         float w = fb ? 0.0f : (ll == M ? 1.0f : __expf(ll - M));
         if (!(w >= 0.0f)) w = 0.0f;
-        if (SEARCH) sA[i] = __float_as_int(w); else sW[i] = w;
+        // SEARCH: the integer weight straight into the prefix array; the max
+        // weight is exactly 1 (or every weight is 0), so the quantisation
+        // exponent is 1
+        if (SEARCH) sQ[i] = quantize_f32(w, 1); else sW[i] = w;
         if (dbg) A.dbg_w[(size_t)t * N + i] = w;
         acc[0] += w;
         acc[1] = fmaf(w, w, acc[1]);
@@ -449,20 +458,23 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       // ---- exact systematic resampling: chunk sums and block scan, then either
       // a binary search per target (SEARCH) or a scatter walk per chunk
       uint64_t cs = 0;
-      for (int j = j0; j < j1; ++j) cs += quantize_f32(SEARCH ? __int_as_float(sA[j]) : sW[j], e);
+      for (int j = j0; j < j1; ++j) cs += SEARCH ? sQ[j] : quantize_f32(sW[j], e);
       uint64_t Qt;
       uint64_t P = block_excl_scan_u64(cs, s_red64, &Qt);   // includes barriers
       const uint32_t U = resample_uniform(seed, trk, (uint32_t)t);
       if (SEARCH) {
         uint64_t pre = P;
         for (int j = j0; j < j1; ++j) {
-          pre += quantize_f32(__int_as_float(sA[j]), e);
+          pre += sQ[j];
           sQ[j] = pre;
         }
         __syncthreads();
-        const bool fb2 = fb || Qt == 0;
-        for (int i = tid; i < N; i += TB)
-          sA[i] = fb2 ? resample_fallback_index(U, i, N) : resample_search(sQ, N, N, resample_rhs(i, U, Qt));
+        if (fb || Qt == 0) {
+          for (int i = tid; i < N; i += TB) sA[i] = resample_fallback_index(U, i, N);
+        } else {
+          const RsThresh th = rs_thresh_setup(Qt, N, U);
+          for (int i = tid; i < N; i += TB) sA[i] = search_u64(sQ, N, rs_threshold(th, (uint32_t)i));
+        }
       } else if (fb || Qt == 0) {
         for (int i = tid; i < N; i += TB) sA[i] = resample_fallback_index(U, i, N);
       } else if (j0 < j1) {

@@ -186,6 +186,43 @@ __device__ __forceinline__ int resample_fallback_index(uint32_t U, int i, int L)
   u32x4 o = philox4x32_10(u32x4{(uint32_t)i, 0u, 0u, 0u}, U, 0x5EEDu);
   return (int)(((uint64_t)o.x * (uint64_t)L) >> 32);
 }
+// The same rule with 64-bit thresholds: target i takes the first j whose
+// inclusive prefix Q_j >= T_i = ceil((i 2^32 + U) Qt / (N 2^32)), the 128-bit
+// comparison N Q_j 2^32 >= (i 2^32 + U) Qt restated exactly.  With
+// Qt = A N + r and floor(U Qt / 2^32) = C N + s, and V_i = i r + s:
+//   T_i = i A + C + floor(V_i / N) + [V_i mod N > 0 or (U Qt mod 2^32) > 0].
+// Needs N <= 65536 (V_i < N^2 fits 32 bits) and i A + C < 2^64.
+struct RsThresh {
+  uint64_t A, C;
+  uint32_t r, s, N, low;
+};
+MKF_HD RsThresh rs_thresh_setup(uint64_t Qt, int N, uint32_t U) {
+  RsThresh t;
+  t.N = (uint32_t)N;
+  t.A = Qt / t.N;
+  t.r = (uint32_t)(Qt - t.A * t.N);
+  const unsigned __int128 UQ = (unsigned __int128)U * Qt;
+  const uint64_t UQh = (uint64_t)(UQ >> 32);
+  t.low = (uint32_t)UQ;
+  t.C = UQh / t.N;
+  t.s = (uint32_t)(UQh - t.C * t.N);
+  return t;
+}
+MKF_HD uint64_t rs_threshold(const RsThresh& t, uint32_t i) {
+  const uint32_t V = i * t.r + t.s;
+  const uint32_t g = V / t.N, h = V - g * t.N;
+  return (uint64_t)i * t.A + t.C + g + (((h | t.low) != 0u) ? 1u : 0u);
+}
+// first j in [0, n) with Q[j] >= T (Q nondecreasing, T <= Q[n-1])
+__device__ __forceinline__ int search_u64(const uint64_t* Q, int n, uint64_t T) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (Q[mid] < T) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
 // number of targets i in [0, N) with (i 2^32 + U) Qt <= N X 2^32
 __device__ __forceinline__ int count_targets_le(uint64_t X, int N, uint32_t U, uint64_t Qt) {
   const unsigned __int128 lim = ((unsigned __int128)(uint64_t)N * (unsigned __int128)X) << 32;
