@@ -157,13 +157,37 @@ __device__ __forceinline__ void propagate(const PView& p, const float* eps, floa
   }
 }
 
-// log[(1-P_D) kappa + P_D sum_i N(z_i; pi(x), sigma^2 I)] summed over measured joints
+// Per-track constants of the likelihood.  Detections and the projected joint
+// are both scaled by k = sqrt(log2(e) / (2 sigma^2)), so that a detection's
+// Gaussian kernel exp(-|z - pi|^2 / (2 sigma^2)) is the single exponential
+// 2^(-|k z - k pi|^2).
+struct LikConst {
+  float k;                          // detection scale
+  float fxk, fyk, cxk, cyk;         // camera scaled by k
+  float norm, floor_, log_kappa;    // P_D / (2 pi sigma^2), (1 - P_D) kappa, log kappa
+};
+
+__device__ __forceinline__ LikConst lik_const(const PView& p, float kappa, float pd, float sigma) {
+  LikConst L;
+  L.k = sqrtf(0.72134752044448170f / (sigma * sigma));
+  L.fxk = p.fx * L.k; L.fyk = p.fy * L.k; L.cxk = p.cx * L.k; L.cyk = p.cy * L.k;
+  L.norm = pd / (kTwoPi * sigma * sigma);
+  L.floor_ = (1.0f - pd) * kappa;
+  L.log_kappa = __logf(kappa);
+  return L;
+}
+
+__device__ __forceinline__ float ex2_neg(float s) {   // 2^(-s), MUFU.EX2
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(-s));
+  return r;
+}
+
+// log[(1-P_D) kappa + P_D sum_i N(z_i; pi(x), sigma^2 I)] summed over measured
+// joints; det holds the detections already scaled by L.k
 template <int D, bool VEC = true>
-__device__ __forceinline__ float loglik(const PView& p, const float* x, const int* cnt,
-                                        const float2* det, float kappa, float pd, float sigma) {
-  const float inv2s2 = 0.5f / (sigma * sigma);
-  const float norm = pd / (kTwoPi * sigma * sigma);
-  const float floor_ = (1.0f - pd) * kappa;
+__device__ __forceinline__ float loglik(const PView& p, const float* x, const int* cnt, const float2* det,
+                                        const LikConst& L) {
   float ll = 0.0f;
   for (int j = 0; j < p.J; ++j) {
     const float* B = p.Bm + j * 3 * D;
@@ -192,9 +216,9 @@ __device__ __forceinline__ float loglik(const PView& p, const float* x, const in
         q2 = fmaf(B[2 * D + c], x[c], q2);
       }
     }
-    if (!(q2 > kZMin)) { ll += __logf(kappa); continue; }
+    if (!(q2 > kZMin)) { ll += L.log_kappa; continue; }
     const float iz = __fdividef(1.0f, q2);
-    const float u = fmaf(p.fx * q0, iz, p.cx), v = fmaf(p.fy * q1, iz, p.cy);
+    const float u = fmaf(L.fxk * q0, iz, L.cxk), v = fmaf(L.fyk * q1, iz, L.cyk);
     // four independent partial sums so the exponentials of a list overlap
     float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, acc3 = 0.0f;
     const float2* dj = det + j * MKF_MAX_DET;
@@ -204,20 +228,20 @@ __device__ __forceinline__ float loglik(const PView& p, const float* x, const in
       const float4 d01 = *reinterpret_cast<const float4*>(dj + i);
       const float4 d23 = *reinterpret_cast<const float4*>(dj + i + 2);
       float dx = d01.x - u, dy = d01.y - v;
-      acc0 += __expf(-(dx * dx + dy * dy) * inv2s2);
+      acc0 += ex2_neg(fmaf(dy, dy, dx * dx));
       dx = d01.z - u; dy = d01.w - v;
-      acc1 += __expf(-(dx * dx + dy * dy) * inv2s2);
+      acc1 += ex2_neg(fmaf(dy, dy, dx * dx));
       dx = d23.x - u; dy = d23.y - v;
-      acc2 += __expf(-(dx * dx + dy * dy) * inv2s2);
+      acc2 += ex2_neg(fmaf(dy, dy, dx * dx));
       dx = d23.z - u; dy = d23.w - v;
-      acc3 += __expf(-(dx * dx + dy * dy) * inv2s2);
+      acc3 += ex2_neg(fmaf(dy, dy, dx * dx));
     }
     for (; i < n; ++i) {
       const float dx = dj[i].x - u, dy = dj[i].y - v;
-      acc0 += __expf(-(dx * dx + dy * dy) * inv2s2);
+      acc0 += ex2_neg(fmaf(dy, dy, dx * dx));
     }
     const float acc = (acc0 + acc1) + (acc2 + acc3);
-    ll += __logf(fmaf(norm, acc, floor_));
+    ll += __logf(fmaf(L.norm, acc, L.floor_));
   }
   return ll;
 }
@@ -245,6 +269,24 @@ struct BatchArgs {
 };
 
 __host__ __device__ constexpr int pad4(int n) { return (n + 3) & ~3; }
+
+// batched per-CTA state slot: D/4 planes of Nmax float4, particle i's
+// dimensions 4g..4g+3 in plane g (a warp's 32 particles read 512 contiguous bytes)
+template <int D>
+__device__ __forceinline__ void load_state(const float* slot, int Nmax, int i, float* x) {
+  const float4* p = reinterpret_cast<const float4*>(slot);
+#pragma unroll
+  for (int g = 0; g < D / 4; ++g) {
+    const float4 v = p[(size_t)g * Nmax + i];
+    x[4 * g] = v.x; x[4 * g + 1] = v.y; x[4 * g + 2] = v.z; x[4 * g + 3] = v.w;
+  }
+}
+template <int D>
+__device__ __forceinline__ void store_state(float* slot, int Nmax, int i, const float* x) {
+  float4* p = reinterpret_cast<float4*>(slot);
+#pragma unroll
+  for (int g = 0; g < D / 4; ++g) p[(size_t)g * Nmax + i] = make_float4(x[4 * g], x[4 * g + 1], x[4 * g + 2], x[4 * g + 3]);
+}
 
 // shared-memory parameter block: a | mb | L | Bm | mm | cumpi, every section 16-byte aligned
 template <int D>
@@ -326,6 +368,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
     pv.S0c = A.m.S0c + (size_t)mi * K * D * (D + 1) / 2;
     pv.K = K; pv.J = J; pv.fx = A.m.fx; pv.fy = A.m.fy; pv.cx = A.m.cx; pv.cy = A.m.cy;
     const bool dbg = (A.dbg_w != nullptr) && (b == A.dbg_track);
+    const LikConst LK = lik_const(pv, ob.x, ob.y, ob.z);
 
     float* xa = xa0;
     float* xb = xb0;
@@ -335,7 +378,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       float uc = particle_draws<D>(seed, trk, kFramePrior, (uint32_t)i, eps);
       prior_sample<D>(pv, eps, uc, x);
 #pragma unroll
-      for (int r = 0; r < D; ++r) xa[(size_t)r * Nmax + i] = x[r];
+      store_state<D>(xa, Nmax, i, x);
       sA[i] = i;
     }
     __syncthreads();
@@ -356,7 +399,10 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       __syncthreads();
       for (int q = tid; q < J * MKF_MAX_DET; q += TB) {
         int j = q / MKF_MAX_DET, i = q - j * MKF_MAX_DET;
-        if (i < s_cnt[j]) s_det[j * MKF_MAX_DET + i] = A.det[A.det_off[g * J + j] + i];
+        if (i < s_cnt[j]) {
+          const float2 z = A.det[A.det_off[g * J + j] + i];
+          s_det[j * MKF_MAX_DET + i] = make_float2(z.x * LK.k, z.y * LK.k);
+        }
       }
       __syncthreads();
 
@@ -370,24 +416,19 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
           const bool two = i2 < N;
           const int an = sA[i], an2 = two ? sA[i2] : an;
           float x[D], eps[D], y[D], eps2[D];
-#pragma unroll
-          for (int r = 0; r < D; ++r) {
-            x[r] = xa[(size_t)r * Nmax + an];
-            y[r] = xa[(size_t)r * Nmax + an2];
-          }
+          load_state<D>(xa, Nmax, an, x);
+          load_state<D>(xa, Nmax, an2, y);
           const float uc = particle_draws<D>(seed, trk, (uint32_t)t, (uint32_t)i, eps);
           const float uc2 = particle_draws<D>(seed, trk, (uint32_t)t, (uint32_t)i2, eps2);
           propagate<D, DIAG, VEC>(pv, eps, uc, x);
           propagate<D, DIAG, VEC>(pv, eps2, uc2, y);
-#pragma unroll
-          for (int r = 0; r < D; ++r) xb[(size_t)r * Nmax + i] = x[r];
-          const float ll = loglik<D, VEC>(pv, x, s_cnt, s_det, ob.x, ob.y, ob.z);
+          store_state<D>(xb, Nmax, i, x);
+          const float ll = loglik<D, VEC>(pv, x, s_cnt, s_det, LK);
           if (SEARCH) sA[i] = __float_as_int(ll); else sW[i] = ll;
           lmax = fmaxf(lmax, ll);
           if (two) {
-#pragma unroll
-            for (int r = 0; r < D; ++r) xb[(size_t)r * Nmax + i2] = y[r];
-            const float ll2 = loglik<D, VEC>(pv, y, s_cnt, s_det, ob.x, ob.y, ob.z);
+            store_state<D>(xb, Nmax, i2, y);
+            const float ll2 = loglik<D, VEC>(pv, y, s_cnt, s_det, LK);
             if (SEARCH) sA[i2] = __float_as_int(ll2); else sW[i2] = ll2;
             lmax = fmaxf(lmax, ll2);
           }
@@ -396,13 +437,11 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
         for (int i = tid; i < N; i += TB) {
           const int an = sA[i];
           float x[D], eps[D];
-#pragma unroll
-          for (int r = 0; r < D; ++r) x[r] = xa[(size_t)r * Nmax + an];
+          load_state<D>(xa, Nmax, an, x);
           float uc = particle_draws<D>(seed, trk, (uint32_t)t, (uint32_t)i, eps);
           propagate<D, DIAG, VEC>(pv, eps, uc, x);
-#pragma unroll
-          for (int r = 0; r < D; ++r) xb[(size_t)r * Nmax + i] = x[r];
-          float ll = loglik<D, VEC>(pv, x, s_cnt, s_det, ob.x, ob.y, ob.z);
+          store_state<D>(xb, Nmax, i, x);
+          float ll = loglik<D, VEC>(pv, x, s_cnt, s_det, LK);
           if (SEARCH) sA[i] = __float_as_int(ll); else sW[i] = ll;
           lmax = fmaxf(lmax, ll);
         }
@@ -426,8 +465,10 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
         acc[0] += w;
         acc[1] = fmaf(w, w, acc[1]);
         acc[2] = fmaxf(acc[2], w);
+        float xi[D];
+        load_state<D>(xb, Nmax, i, xi);
 #pragma unroll
-        for (int r = 0; r < D; ++r) acc[3 + r] = fmaf(w, xb[(size_t)r * Nmax + i], acc[3 + r]);
+        for (int r = 0; r < D; ++r) acc[3 + r] = fmaf(w, xi[r], acc[3 + r]);
       }
       {
         const int lane = tid & 31, w = tid >> 5, nw = (TB + 31) >> 5;
@@ -613,6 +654,7 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
   __shared__ bool s_last;
   const int tid = threadIdx.x, TB = blockDim.x;
   const int J = A.pv.J;
+  const LikConst LK = lik_const(A.pv, A.kappa, A.pd, A.sigma);
   if (!A.prior) {
     if (tid < J) {
       int n = A.det_off[tid + 1] - A.det_off[tid];
@@ -622,7 +664,10 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
     __syncthreads();
     for (int q = tid; q < J * MKF_MAX_DET; q += TB) {
       int j = q / MKF_MAX_DET, i = q - j * MKF_MAX_DET;
-      if (i < s_cnt[j]) s_det[j * MKF_MAX_DET + i] = A.det[A.det_off[j] + i];
+      if (i < s_cnt[j]) {
+        const float2 z = A.det[A.det_off[j] + i];
+        s_det[j * MKF_MAX_DET + i] = make_float2(z.x * LK.k, z.y * LK.k);
+      }
     }
     __syncthreads();
   }
@@ -648,7 +693,7 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
     propagate<D, DIAG>(A.pv, eps, uc, x);
 #pragma unroll
     for (int r = 0; r < D; ++r) A.xb[(size_t)r * A.N + i] = x[r];
-    float ll = loglik<D>(A.pv, x, s_cnt, s_det, A.kappa, A.pd, A.sigma);
+    float ll = loglik<D>(A.pv, x, s_cnt, s_det, LK);
     A.logw[i] = ll;
     // online accumulation
     if (ll > m) {
