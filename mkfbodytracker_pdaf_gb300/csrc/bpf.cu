@@ -513,8 +513,18 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
         if (fb || Qt == 0) {
           for (int i = tid; i < N; i += TB) sA[i] = resample_fallback_index(U, i, N);
         } else {
+          // four targets per thread at a time (i, i + TB, i + 2 TB, i + 3 TB)
           const RsThresh th = rs_thresh_setup(Qt, N, U);
-          for (int i = tid; i < N; i += TB) sA[i] = search_u64(sQ, N, rs_threshold(th, (uint32_t)i));
+          for (int i0 = tid; i0 < N; i0 += 4 * TB) {
+            uint64_t T4[4];
+            int r4[4];
+#pragma unroll
+            for (int g = 0; g < 4; ++g) T4[g] = rs_threshold(th, (uint32_t)min(i0 + g * TB, N - 1));
+            search_u64_multi<4>(sQ, N, T4, r4);
+#pragma unroll
+            for (int g = 0; g < 4; ++g)
+              if (i0 + g * TB < N) sA[i0 + g * TB] = r4[g];
+          }
         }
       } else if (fb || Qt == 0) {
         for (int i = tid; i < N; i += TB) sA[i] = resample_fallback_index(U, i, N);

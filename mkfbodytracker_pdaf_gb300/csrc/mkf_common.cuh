@@ -223,6 +223,25 @@ __device__ __forceinline__ int search_u64(const uint64_t* Q, int n, uint64_t T) 
   return lo;
 }
 
+// The same search for G targets at once: a branch-free lower bound whose
+// halving steps depend on n only, so the G searches run interleaved.  Needs
+// T[g] <= Q[n-1].
+template <int G>
+__device__ __forceinline__ void search_u64_multi(const uint64_t* Q, int n, const uint64_t* T, int* out) {
+  int base[G];
+#pragma unroll
+  for (int g = 0; g < G; ++g) base[g] = 0;
+  int len = n;
+  while (len > 1) {
+    const int half = len >> 1;
+#pragma unroll
+    for (int g = 0; g < G; ++g) base[g] = (Q[base[g] + half] < T[g]) ? base[g] + half : base[g];
+    len -= half;
+  }
+#pragma unroll
+  for (int g = 0; g < G; ++g) out[g] = base[g] + ((Q[base[g]] < T[g]) ? 1 : 0);
+}
+
 // number of targets i in [0, N) with (i 2^32 + U) Qt <= N X 2^32
 __device__ __forceinline__ int count_targets_le(uint64_t X, int N, uint32_t U, uint64_t Qt) {
   const unsigned __int128 lim = ((unsigned __int128)(uint64_t)N * (unsigned __int128)X) << 32;
