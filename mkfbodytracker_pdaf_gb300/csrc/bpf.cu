@@ -90,6 +90,7 @@ static int build_models(const mkf_bpf_models* M, DevModels& out) {
 // parameters of one model as seen by one particle (pointers into shared or global)
 struct PView {
   const float *a, *mb, *mu, *Lq, *Ld, *S0c, *cumpi, *Bm, *mm;
+  const uint8_t* ktab;     // optional component table (kPickBins entries), or null
   int K, J;
   float fx, fy, cx, cy;
 };
@@ -103,10 +104,36 @@ __device__ __forceinline__ int pick_component(const float* cumpi, int K, float u
   return k;
 }
 
+// The same count from a table over kPickBins equal bins of [0, 1): entry b holds
+// #{c < K-1 : cumpi[c] <= b / kPickBins} in its low 7 bits and, in bit 7,
+// whether some cumpi[c] falls strictly inside the bin; only then does the count
+// continue past the bin's lower edge.  u is a multiple of 2^-24, so u * kPickBins
+// and its floor are exact.
+constexpr int kPickBins = 1024;
+__device__ __forceinline__ void build_pick_table(const float* cumpi, int K, uint8_t* tab, int tid, int TB) {
+  for (int b = tid; b < kPickBins; b += TB) {
+    const float lo = (float)b * (1.0f / kPickBins), hi = (float)(b + 1) * (1.0f / kPickBins);
+    int s = 0, s2 = 0;
+    for (int c = 0; c < K - 1; ++c) {
+      s += (cumpi[c] <= lo) ? 1 : 0;
+      s2 += (cumpi[c] < hi) ? 1 : 0;
+    }
+    tab[b] = (uint8_t)(s | ((s2 > s) ? 0x80 : 0));
+  }
+}
+__device__ __forceinline__ int pick_component(const PView& p, float u) {
+  if (!p.ktab) return pick_component(p.cumpi, p.K, u);
+  const int e = p.ktab[__float2int_rz(u * (float)kPickBins)];
+  int k = e & 0x7F;
+  if (e & 0x80)
+    while (k < p.K - 1 && u >= p.cumpi[k]) ++k;
+  return k;
+}
+
 template <int D>
 __device__ __forceinline__ void prior_sample(const PView& p, const float* eps, float uc, float* x) {
   constexpr int DD = D * (D + 1) / 2;
-  int k = pick_component(p.cumpi, p.K, uc);
+  int k = pick_component(p, uc);
   const float* L = p.S0c + k * DD;
 #pragma unroll
   for (int r = 0; r < D; ++r) {
@@ -124,7 +151,7 @@ __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast
 template <int D, bool DIAG, bool VEC = true>
 __device__ __forceinline__ void propagate(const PView& p, const float* eps, float uc, float* x) {
   constexpr int DD = D * (D + 1) / 2;
-  int k = pick_component(p.cumpi, p.K, uc);
+  int k = pick_component(p, uc);
   const float* a = p.a + k * D;
   const float* mb = p.mb + k * D;
   if (DIAG) {
@@ -328,6 +355,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
   float* s_red = reinterpret_cast<float*>(s_cnt + 8);                    // 32*NV floats
   uint64_t* s_red64 = reinterpret_cast<uint64_t*>(s_red + 32 * NV + 2);
   s_red64 = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(s_red64) + 7) & ~uintptr_t(7));
+  uint8_t* s_ktab = reinterpret_cast<uint8_t*>(s_red64 + 34);
   __shared__ int s_item;
   __shared__ int s_flag;
 
@@ -360,10 +388,13 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       for (int i = tid; i < J * 3 * D; i += TB) s_Bm[i] = gB[i];
       for (int i = tid; i < J * 3; i += TB) s_mm[i] = gm[i];
       if (tid == 0) s_flag = 0;
+      __syncthreads();
+      build_pick_table(s_cum, K, s_ktab, tid, TB);
     }
     __syncthreads();
     PView pv;
     pv.a = s_a; pv.mb = s_mb; pv.Lq = s_L; pv.Ld = s_L; pv.cumpi = s_cum; pv.Bm = s_Bm; pv.mm = s_mm;
+    pv.ktab = s_ktab;
     pv.mu = A.m.mu + (size_t)mi * K * D;
     pv.S0c = A.m.S0c + (size_t)mi * K * D * (D + 1) / 2;
     pv.K = K; pv.J = J; pv.fx = A.m.fx; pv.fy = A.m.fy; pv.cx = A.m.cx; pv.cy = A.m.cy;
@@ -550,7 +581,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
 static size_t batched_smem_bytes(int D, int Nmax, int K, int J, bool diag, bool search) {
   size_t pf = (D == 12) ? params_floats<12>(K, J, diag) : params_floats<24>(K, J, diag);
   size_t bytes = (search ? 12 : 8) * (size_t)Nmax + 4 * pf + 8 * MKF_MAX_J * MKF_MAX_DET + 32 +
-                 4 * (32 * (D + 3) + 2) + 8 * 34 + 16;
+                 4 * (32 * (D + 3) + 2) + 8 * 34 + 16 + kPickBins;
   return (bytes + 15) & ~size_t(15);
 }
 
@@ -905,6 +936,7 @@ static PView make_view(const DevModels& m, int mi) {
   p.Lq = m.Lq + (size_t)mi * K * DD; p.Ld = m.Ld + (size_t)mi * K * d;
   p.S0c = m.S0c + (size_t)mi * K * DD; p.cumpi = m.cumpi + (size_t)mi * K;
   p.Bm = m.Bm + (size_t)mi * J * 3 * d; p.mm = m.mm + (size_t)mi * J * 3;
+  p.ktab = nullptr;
   p.K = K; p.J = J; p.fx = m.fx; p.fy = m.fy; p.cx = m.cx; p.cy = m.cy;
   return p;
 }
