@@ -243,7 +243,7 @@ __device__ __forceinline__ float loglik(const PView& p, const float* x, const in
         q2 = fmaf(B[2 * D + c], x[c], q2);
       }
     }
-    if (!(q2 > kZMin)) { ll += L.log_kappa; continue; }
+    if (!(q2 > kZMin)) { ll = __fadd_rn(ll, L.log_kappa); continue; }
     const float iz = __fdividef(1.0f, q2);
     const float u = fmaf(L.fxk * q0, iz, L.cxk), v = fmaf(L.fyk * q1, iz, L.cyk);
     // four independent partial sums so the exponentials of a list overlap
@@ -268,7 +268,9 @@ __device__ __forceinline__ float loglik(const PView& p, const float* x, const in
       acc0 += ex2_neg(fmaf(dy, dy, dx * dx));
     }
     const float acc = (acc0 + acc1) + (acc2 + acc3);
-    ll += __logf(fmaf(L.norm, acc, L.floor_));
+    // __fadd_rn: never merged with the multiply inside __logf, so every kernel
+    // that inlines this function rounds the log-likelihood the same way
+    ll = __fadd_rn(ll, __logf(fmaf(L.norm, acc, L.floor_)));
   }
   return ll;
 }
@@ -437,8 +439,18 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       }
       __syncthreads();
 
-      // ---- propagate from the resampled set and score
+      // ---- propagate from the resampled set and score.  Besides the
+      // log-weights, the non-pair loop accumulates the estimate sums with the
+      // frame's upper bound Lub of any log-likelihood (every Gaussian kernel is
+      // <= 1) as the shift; they are used when the frame's max M is within 60
+      // of Lub (no weight that matters can underflow), else the sums are
+      // formed again below with M as the shift.
       float lmax = -INFINITY;
+      float Lub = 0.0f;
+      for (int j = 0; j < J; ++j) Lub += fmaxf(LK.log_kappa, __logf(fmaf(LK.norm, (float)s_cnt[j], LK.floor_)));
+      float fs = 0.0f, fs2 = 0.0f, fv[D];
+#pragma unroll
+      for (int r = 0; r < D; ++r) fv[r] = 0.0f;
       if (PAIR) {
         // particles i and i + TB of this thread together: two independent
         // dependency chains for the scheduler (same particles, same results)
@@ -475,10 +487,16 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
           float ll = loglik<D, VEC>(pv, x, s_cnt, s_det, LK);
           if (SEARCH) sA[i] = __float_as_int(ll); else sW[i] = ll;
           lmax = fmaxf(lmax, ll);
+          const float wl = __expf(ll - Lub);
+          fs += wl;
+          fs2 = fmaf(wl, wl, fs2);
+#pragma unroll
+          for (int r = 0; r < D; ++r) fv[r] = fmaf(wl, x[r], fv[r]);
         }
       }
       const float M = block_max(lmax, s_red);
       const bool fb = !(M > -INFINITY) || !(M < INFINITY);
+      const bool fused = !PAIR && (M - Lub >= -60.0f);
 
       // ---- weights normalised to the max, weighted-mean estimate, ESS
       float acc[NV];
@@ -493,13 +511,21 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
         // exponent is 1
         if (SEARCH) sQ[i] = quantize_f32(w, 1); else sW[i] = w;
         if (dbg) A.dbg_w[(size_t)t * N + i] = w;
-        acc[0] += w;
-        acc[1] = fmaf(w, w, acc[1]);
         acc[2] = fmaxf(acc[2], w);
-        float xi[D];
-        load_state<D>(xb, Nmax, i, xi);
+        if (!fused) {
+          acc[0] += w;
+          acc[1] = fmaf(w, w, acc[1]);
+          float xi[D];
+          load_state<D>(xb, Nmax, i, xi);
 #pragma unroll
-        for (int r = 0; r < D; ++r) acc[3 + r] = fmaf(w, xi[r], acc[3 + r]);
+          for (int r = 0; r < D; ++r) acc[3 + r] = fmaf(w, xi[r], acc[3 + r]);
+        }
+      }
+      if (fused) {
+        acc[0] = fs;
+        acc[1] = fs2;
+#pragma unroll
+        for (int r = 0; r < D; ++r) acc[3 + r] = fv[r];
       }
       {
         const int lane = tid & 31, w = tid >> 5, nw = (TB + 31) >> 5;
@@ -520,7 +546,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       const float S = s_red[0], S2 = s_red[1], Wmax = s_red[2];
       if (tid < D) A.est[(size_t)g * D + tid] = s_red[3 + tid] / S;
       if (tid == 0) {
-        A.loglik[g] = M + __logf(S) - __logf((float)N);
+        A.loglik[g] = (fused ? Lub : M) + __logf(S) - __logf((float)N);
         A.ess[g] = S * S / S2;
         if (fb) s_flag |= MKF_ST_FALLBACK | MKF_ST_NAN;
       }
