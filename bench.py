@@ -505,7 +505,7 @@ def run_adjoint(args):
         "forward_ms": tf, "backward_ms": tb, "backward_over_forward": tb / tf,
         "track_frames_per_s_forward": b.n_frames_total / tf * 1e3,
         "gradient_evals_per_s": 1e3 / (tf + tb), "logL": L_gpu,
-        "checkpoint_stride": int(np.ceil(np.sqrt(args.adj_frames))),
+        "checkpoint_stride": g.checkpoint_stride,
         "check_subset_tracks": len(sub), "logL_rel_err_subset": abs(L_sub_gpu - L_c) / abs(L_c),
         "fd_directions": args.fd_dirs,
         "grad_rel_err_vs_fd": {"median": float(np.median(rel_fd)), "max": float(np.max(rel_fd))},

@@ -363,9 +363,16 @@ int mkf_mixkf_theta_size(mkf_mixkf_t h);
  * device pointers; stores the checkpoints the backward pass needs */
 int mkf_mixkf_forward(mkf_mixkf_t h, const int* d_det_off, const float* d_det, double* d_loglik,
                       double* d_total, mkf_stream_t stream);
-/* backward: d logL_total / d theta into d_grad (theta-sized, device) */
+/* backward: d logL_total / d theta into d_grad (theta-sized, device); needs the
+ * checkpoints of a forward run with the current stride (MKF_ERR_STATE otherwise) */
 int mkf_mixkf_backward(mkf_mixkf_t h, const int* d_det_off, const float* d_det, double* d_grad,
                        mkf_stream_t stream);
+/* checkpoint stride C (frames per backward segment; C >= 1, or 0 for the
+ * default: ceil(sqrt(T_max)), lowered when one segment's records of all
+ * resident CTAs would not fit in 60 % of L2).  Gradients do not depend on C.
+ * Run mkf_mixkf_forward again before the next backward. */
+int mkf_mixkf_set_checkpoint_stride(mkf_mixkf_t h, int C);
+int mkf_mixkf_checkpoint_stride(mkf_mixkf_t h);
 int mkf_mixkf_status(mkf_mixkf_t h, int* status);
 int mkf_mixkf_destroy(mkf_mixkf_t h);
 /* one Adam step on device (maximising when maximize != 0):

@@ -100,6 +100,8 @@ SIGNATURES = {
     "mkf_mixkf_theta_size": (I, [P]),
     "mkf_mixkf_forward": (I, [P, P, P, P, P, P]),
     "mkf_mixkf_backward": (I, [P, P, P, P, P]),
+    "mkf_mixkf_set_checkpoint_stride": (I, [P, I]),
+    "mkf_mixkf_checkpoint_stride": (I, [P]),
     "mkf_mixkf_status": (I, [P, C.POINTER(I)]),
     "mkf_mixkf_destroy": (I, [P]),
     "mkf_adam_step": (I, [P, P, P, P, P, I, I, C.c_double, C.c_double, C.c_double, C.c_double, I, P]),

@@ -833,7 +833,47 @@ struct mkf_mixkf {
   bool have_theta;
   bool stage;
   size_t smem_f, smem_b;
+  int* h_nf;          // host copy of the tracks' frame counts
+  int maxT;
+  int fwd_C;          // checkpoint stride of the last forward (0: none yet)
 };
+
+// Checkpoint stride C and the buffers that depend on it: the checkpoints
+// (every C-th collapsed state of every track) and the per-CTA slot, which holds
+// the work arrays and one backward segment of C frames of records.
+static int mix_set_stride(mkf_mixkf* h, int C) {
+  const FrameLayout FL = frame_layout(h->d, h->K, h->J);
+  const WorkLayout WL = work_layout(h->d);
+  std::vector<long long> ckoff(h->n_tracks);
+  long long ck_total = 0;
+  for (int b = 0; b < h->n_tracks; ++b) {
+    ckoff[b] = ck_total;
+    ck_total += (long long)((h->h_nf[b] + C - 1) / C) * (h->d + h->d * h->d);
+  }
+  if (h->ck) { cudaFree(h->ck); h->ck = nullptr; }
+  if (h->slots) { cudaFree(h->slots); h->slots = nullptr; }
+  h->C = C;
+  h->fwd_C = 0;
+  h->slot_floats = ((long long)h->K * WL.size + (long long)C * FL.size + 63) & ~63LL;
+  MKF_CUDA(cudaMalloc(&h->ck, sizeof(float) * (size_t)std::max<long long>(1, ck_total)));
+  MKF_CUDA(cudaMemcpy(h->ck_off, ckoff.data(), sizeof(long long) * h->n_tracks, cudaMemcpyHostToDevice));
+  MKF_CUDA(cudaMalloc(&h->slots, sizeof(float) * (size_t)h->slot_floats * h->grid));
+  return MKF_OK;
+}
+
+// ceil(sqrt(T_max)) frames per segment, unless one segment's records of all
+// resident CTAs would exceed 60 % of L2; then the longest segment that fits
+static int mix_auto_stride(mkf_mixkf* h) {
+  const FrameLayout FL = frame_layout(h->d, h->K, h->J);
+  int dev = 0, l2 = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess)
+    l2 = 0;
+  const int c_sqrt = std::max(1, (int)std::ceil(std::sqrt((double)std::max(1, h->maxT))));
+  if (l2 <= 0) return c_sqrt;
+  const double per_frame = 4.0 * (double)FL.size * h->grid;
+  const int c_fit = std::max(1, (int)(0.6 * l2 / per_frame));
+  return std::min(c_sqrt, c_fit);
+}
 
 template <typename KF>
 static int mix_occ(KF kern, int tpb, size_t smem, int* occ) {
@@ -894,16 +934,13 @@ extern "C" int mkf_mixkf_create(const mkf_mix_model* model, int n_tracks, const 
   if (!h) return MKF_ERR_NOMEM;
   memset(h, 0, sizeof(*h));
   h->d = d; h->K = K; h->J = J; h->DD = DD; h->n_tracks = n_tracks; h->G = n_frames_total;
-  h->C = std::max(1, (int)std::ceil(std::sqrt((double)std::max(1, maxT))));
+  h->maxT = maxT;
   h->ng = 2 * K * d + K * DD + 1;
   h->tpb = 32 * K;
   h->fx = model->fx; h->fy = model->fy; h->cx = model->cx; h->cy = model->cy;
-  std::vector<long long> ckoff(n_tracks);
-  long long ck_total = 0;
-  for (int b = 0; b < n_tracks; ++b) {
-    ckoff[b] = ck_total;
-    ck_total += (long long)((n_frames[b] + h->C - 1) / h->C) * (d + d * d);
-  }
+  h->h_nf = static_cast<int*>(malloc(sizeof(int) * n_tracks));
+  if (!h->h_nf) { delete h; return MKF_ERR_NOMEM; }
+  memcpy(h->h_nf, n_frames, sizeof(int) * n_tracks);
   std::vector<float> f_Bm((size_t)n_tracks * J * 3 * d), f_mm((size_t)n_tracks * J * 3), f_pd(n_tracks), f_k(n_tracks);
   for (size_t i = 0; i < f_Bm.size(); ++i) f_Bm[i] = (float)Bm[i];
   for (size_t i = 0; i < f_mm.size(); ++i) f_mm[i] = (float)mm[i];
@@ -929,13 +966,11 @@ extern "C" int mkf_mixkf_create(const mkf_mix_model* model, int n_tracks, const 
   al((void**)&h->ck_off, sizeof(long long) * n_tracks);
   al((void**)&h->Bm, sizeof(float) * f_Bm.size()); al((void**)&h->mm, sizeof(float) * f_mm.size());
   al((void**)&h->pd, sizeof(float) * n_tracks); al((void**)&h->kappa, sizeof(float) * n_tracks);
-  al((void**)&h->ck, sizeof(float) * std::max<long long>(1, ck_total));
   al((void**)&h->ll, sizeof(double) * n_tracks); al((void**)&h->total, sizeof(double));
   al((void**)&h->status, sizeof(int));
   cp(h->pi, f_pi.data(), sizeof(float) * K); cp(h->logpi, f_lpi.data(), sizeof(float) * K);
   cp(h->S0, f_S0.data(), sizeof(float) * f_S0.size());
   cp(h->n_frames, n_frames, sizeof(int) * n_tracks); cp(h->frame_base, fb.data(), sizeof(long long) * n_tracks);
-  cp(h->ck_off, ckoff.data(), sizeof(long long) * n_tracks);
   cp(h->Bm, f_Bm.data(), sizeof(float) * f_Bm.size()); cp(h->mm, f_mm.data(), sizeof(float) * f_mm.size());
   cp(h->pd, f_pd.data(), sizeof(float) * n_tracks); cp(h->kappa, f_k.data(), sizeof(float) * n_tracks);
   if (e == cudaSuccess) e = cudaMemset(h->status, 0, sizeof(int));
@@ -945,11 +980,9 @@ extern "C" int mkf_mixkf_create(const mkf_mix_model* model, int n_tracks, const 
   }
   int st = mix_grid(h);
   if (st) { mkf_mixkf_destroy(h); return st; }
-  const FrameLayout FL = frame_layout(d, K, J);
-  const WorkLayout WL = work_layout(d);
-  h->slot_floats = ((long long)K * WL.size + (long long)h->C * FL.size + 63) & ~63LL;
-  e = cudaMalloc(&h->slots, sizeof(float) * (size_t)h->slot_floats * h->grid);
-  if (e == cudaSuccess) e = cudaMalloc(&h->gacc, sizeof(double) * (size_t)h->ng * h->grid);
+  st = mix_set_stride(h, mix_auto_stride(h));
+  if (st) { mkf_mixkf_destroy(h); return st; }
+  e = cudaMalloc(&h->gacc, sizeof(double) * (size_t)h->ng * h->grid);
   if (e != cudaSuccess) {
     mkf_mixkf_destroy(h);
     return cuda_fail(e, "mkf_mixkf_create: scratch allocation", __FILE__, __LINE__);
@@ -957,6 +990,13 @@ extern "C" int mkf_mixkf_create(const mkf_mix_model* model, int n_tracks, const 
   *out = h;
   return MKF_OK;
 }
+
+extern "C" int mkf_mixkf_set_checkpoint_stride(mkf_mixkf_t h, int C) {
+  MKF_ARG(h && C >= 0, "mkf_mixkf_set_checkpoint_stride: bad argument");
+  return mix_set_stride(h, C == 0 ? mix_auto_stride(h) : std::min(C, std::max(1, h->maxT)));
+}
+
+extern "C" int mkf_mixkf_checkpoint_stride(mkf_mixkf_t h) { return h ? h->C : 0; }
 
 extern "C" int mkf_mixkf_theta_size(mkf_mixkf_t h) { return h ? h->ng : 0; }
 
@@ -1003,6 +1043,7 @@ extern "C" int mkf_mixkf_forward(mkf_mixkf_t h, const int* d_det_off, const floa
   if (h->d == 12) mix_forward_kernel<12><<<h->grid, h->tpb, h->smem_f, s>>>(A);
   else mix_forward_kernel<24><<<h->grid, h->tpb, h->smem_f, s>>>(A);
   MKF_CHECK_LAUNCH("mkf_mixkf_forward");
+  h->fwd_C = h->C;
   if (d_loglik) MKF_CUDA(cudaMemcpyAsync(d_loglik, h->ll, sizeof(double) * h->n_tracks, cudaMemcpyDeviceToDevice, s));
   mix_total_kernel<<<1, 256, 0, s>>>(h->ll, h->n_tracks, d_total ? d_total : h->total);
   MKF_CHECK_LAUNCH("mkf_mixkf_forward: total");
@@ -1013,6 +1054,10 @@ extern "C" int mkf_mixkf_backward(mkf_mixkf_t h, const int* d_det_off, const flo
                                   mkf_stream_t stream) {
   MKF_ARG(h && d_det_off && d_det && d_grad, "mkf_mixkf_backward: null argument");
   if (!h->have_theta) { set_error("mkf_mixkf_backward: set theta first"); return MKF_ERR_STATE; }
+  if (h->fwd_C != h->C) {
+    set_error("mkf_mixkf_backward: run mkf_mixkf_forward first (its checkpoints are the backward's input)");
+    return MKF_ERR_STATE;
+  }
   cudaStream_t s = (cudaStream_t)stream;
   MixArgs A = mix_args(h, d_det_off, d_det);
   MKF_CUDA(cudaMemsetAsync(h->gacc, 0, sizeof(double) * (size_t)h->ng * h->grid, s));
@@ -1041,6 +1086,7 @@ extern "C" int mkf_mixkf_destroy(mkf_mixkf_t h) {
                 h->frame_base, h->ck_off, h->Bm, h->mm, h->pd, h->kappa, h->ck, h->ll, h->total, h->status,
                 h->slots, h->gacc};
   for (void* p : ps) if (p) cudaFree(p);
+  free(h->h_nf);
   delete h;
   return MKF_OK;
 }

@@ -75,6 +75,13 @@ class MixtureKF:
                                            _stream(self.torch, stream)), "mkf_mixkf_backward")
         return self.grad
 
+    def set_checkpoint_stride(self, C_=0):
+        N.check(N.lib().mkf_mixkf_set_checkpoint_stride(self.h, int(C_)), "mkf_mixkf_set_checkpoint_stride")
+
+    @property
+    def checkpoint_stride(self):
+        return N.lib().mkf_mixkf_checkpoint_stride(self.h)
+
     def status(self):
         s = C.c_int()
         N.check(N.lib().mkf_mixkf_status(self.h, C.byref(s)), "mkf_mixkf_status")

@@ -65,3 +65,25 @@ def test_gradient_deterministic(cuda, olib):
     g.forward()
     g2 = g.backward().cpu().numpy()
     np.testing.assert_array_equal(g1, g2)
+
+
+def test_checkpoint_stride_does_not_change_the_gradient(cuda, olib):
+    b, om, th, g = _setup(olib, n_tracks=5, T=29)
+    g.set_theta(th)
+    ref = None
+    for C in (0, 1, 3, 29):
+        g.set_checkpoint_stride(C)
+        if C:
+            assert g.checkpoint_stride == C
+        L = g.forward().item()
+        grad = g.backward().cpu().numpy().copy()
+        if ref is None:
+            ref = (L, grad)
+            continue
+        assert L == ref[0]                                  # the forward does not depend on C
+        np.testing.assert_allclose(grad, ref[1], rtol=1e-5, atol=1e-6 * np.abs(ref[1]).max())
+    # the backward needs the checkpoints of a forward at the current stride
+    g.set_checkpoint_stride(4)
+    from mkfbodytracker_pdaf_gb300._native import MkfError
+    with pytest.raises(MkfError):
+        g.backward()
