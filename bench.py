@@ -36,9 +36,9 @@ UNIT = "track-frames/s"
 BYTES_PER_PF = 112          # algorithmic bytes per particle-frame (state in/out 4d+4d, logw 8, anc 8)
 # DRAM bytes per particle-frame of bpf_batched_kernel: dram__bytes_read.sum +
 # dram__bytes_write.sum of one ncu capture on 2048 tracks of the same workload
-# (242.2 GB over 4.148e9 particle-frames), scaled to a full launch by
+# (210.1 GB over 4.148e9 particle-frames), scaled to a full launch by
 # particle-frames (profiles/bpf_batched_kernel_config2.md)
-TRAFFIC_BYTES_PER_PF = 58.4
+TRAFFIC_BYTES_PER_PF = 50.65
 
 
 def load_peaks():
@@ -554,6 +554,16 @@ def run_fit(args):
     Qt = np.einsum("kij,klj->kil", synth.unpack_lower(tt["Lq"], d), synth.unpack_lower(tt["Lq"], d))
     Qf = np.einsum("kij,klj->kil", synth.unpack_lower(L_f, d), synth.unpack_lower(L_f, d))
     Q0 = np.einsum("kij,klj->kil", synth.unpack_lower(Lq0, d), synth.unpack_lower(Lq0, d))
+    # components matched to the truth by their means (Hungarian assignment), then compared
+    cost = ((mu_f[:, None, :] - tt["mu"][None, :, :]) ** 2).sum(-1)
+    try:
+        from scipy.optimize import linear_sum_assignment
+        _, perm = linear_sum_assignment(cost)
+    except ImportError:
+        perm = np.argmin(cost, axis=1)
+    matched = {"mu_mae": err(mu_f, tt["mu"][perm]),
+               "a_mae": err(a_f, tt["a"][perm]), "Q_mae": err(Qf, Qt[perm]),
+               "components_relabelled": int((perm != np.arange(K)).sum())}
     print(json.dumps({
         "workload": "config 4: fit K=32, d=24 from B=%d x T=%d, %d Adam steps (lr %g) on the device"
                     % (b.n_tracks, args.fit_frames, args.fit_steps, args.fit_lr),
@@ -562,7 +572,8 @@ def run_fit(args):
         "recovery": {"mu_mae_init": err(mu_0, tt["mu"]), "mu_mae_final": err(mu_f, tt["mu"]),
                      "a_mae_init": 0.0, "a_mae_final": err(a_f, tt["a"]),
                      "Q_mae_init": err(Q0, Qt), "Q_mae_final": err(Qf, Qt),
-                     "sigma_init": float(th0[-1]), "sigma_final": s_f, "sigma_true": float(tt["sigma"])}}),
+                     "sigma_init": float(th0[-1]), "sigma_final": s_f, "sigma_true": float(tt["sigma"]),
+                     "after_matching_components": matched}}),
           flush=True)
 
 

@@ -326,6 +326,32 @@ int mkf_pose_decode(const double* d_x, int B, int d, int F, const double* d_Hpca
 int mkf_pose2d_record(const double* d_e1, const double* d_e2, int B, int F, double* d_pts,
                       mkf_stream_t stream);
 
+/* ------------------------------------ f1 likelihood-image measurement front end */
+/* GaussianBlur(likelihood, 15 x 15, sigma 3, BORDER_DEFAULT) (pfPose.cpp:213)
+ * of an 8-bit image (device, row pitch in bytes): separable, each pass the
+ * fmaf chain over the taps w_k = exp(-(k-7)^2/18) / sum (double, rounded to
+ * float) in tap order, reflect-101 border, then round-to-nearest-even and
+ * saturate to 8 bits.  width, height >= 8; d_out must not alias d_in. */
+int mkf_likelihood_blur(const uint8_t* d_in, int width, int height, int pitch_in, uint8_t* d_out,
+                        int pitch_out, mkf_stream_t stream);
+/* PFTracker::getMeasurementProposal over a (blurred) likelihood image
+ * (pfPose.cpp:210-329) for both arms.  Per arm a, M candidates (10 N in the
+ * reference): with init != 0 uniform in the box x in [max(x-4w, 0),
+ * min(x+5w, W)), y in [min(y+h, H), min(y+7h, H)) of the arm's ROI (integer
+ * bounds, pfPose.cpp:228-235), else hand_a + 0.8 w (n0, n1) (getSamples:
+ * randn with the matrix 0.8 w I as its standard deviation, pf2DRao.cpp:85-103);
+ * draws from Philox block (frame, j, 0x104) of the arm's key (words 0, 1:
+ * uniforms w / 2^32, or a Box-Muller pair).  Weight of candidate c inside the
+ * image (0 < x < W, 0 < y < H): L = like[int(y)][int(x)] / 255, w = 0 if
+ * L == 0 else L / (Pa p_a(c) + Pa p_o(c) + clutter (1 - 2 Pa)) with
+ * p = N(c; hand, 0.8 w I) (pfPose.cpp:250-289); outside: 0.  Then as
+ * mkf_pdaf_associate: normalise, resample N bins, measurement rows.
+ * d_cand_a (optional, M x 2 doubles) receive the candidates. */
+int mkf_pdaf_propose_image(mkf_rbpf_t arm0, mkf_rbpf_t arm1, uint32_t frame, const double* roi,
+                           const uint8_t* d_like, int width, int height, int pitch, int M, int init,
+                           double Pa, double clutter, double* d_meas0, double* d_meas1, int* d_bins0,
+                           int* d_bins1, double* d_cand0, double* d_cand1, mkf_stream_t stream);
+
 /* ------------------------------------------- A11 mixture KF forward / adjoint */
 /* Deterministic counterpart of ParticleFilter::update (pf2DRao.cpp:125-158):
  * per frame every component k predicts from the collapsed posterior

@@ -410,7 +410,6 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       float eps[D], x[D];
       float uc = particle_draws<D>(seed, trk, kFramePrior, (uint32_t)i, eps);
       prior_sample<D>(pv, eps, uc, x);
-#pragma unroll
       store_state<D>(xa, Nmax, i, x);
       sA[i] = i;
     }

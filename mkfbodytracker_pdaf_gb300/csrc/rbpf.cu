@@ -362,6 +362,8 @@ struct PdafArm {
   double* meas;
   int* bins;
   double* w;                // M scratch
+  uint64_t p_seed;          // the arm's Philox key
+  uint32_t p_track;
 };
 struct PdafArgs {
   PdafArm arm[2];
@@ -391,60 +393,42 @@ __device__ void decode_hand(const RbpfParams& p, const double* est, double* hat)
   }
 }
 
-__global__ void __launch_bounds__(256) pdaf_kernel(PdafArgs A) {
-  __shared__ double red[32];
-  __shared__ uint64_t red64[34];
-  __shared__ double s_est[2][MKF_MAX_D];
-  __shared__ double s_hat[2][2];
-  const int a = blockIdx.x, o = 1 - a;
+// both arms' estimates (getEstimator inside getSampleProb, pf2DRao.cpp:111) and
+// their decoded hand pixels
+__device__ void pdaf_hats(const PdafArm* arm, double (*s_est)[MKF_MAX_D], double (*s_hat)[2], double* red) {
   const int tid = threadIdx.x, TB = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = TB >> 5;
-  // both arms' estimates (getEstimator inside getSampleProb, pf2DRao.cpp:111)
-  for (int arm = 0; arm < 2; ++arm) {
-    const RbpfParams& p = A.arm[arm].p;
+  for (int a = 0; a < 2; ++a) {
+    const RbpfParams& p = arm[a].p;
     for (int r = 0; r < p.d; ++r) {
       double s = 0.0;
-      for (int j = tid; j < p.N; j += TB) s += A.arm[arm].x[(size_t)j * p.d + r];
+      for (int j = tid; j < p.N; j += TB) s += arm[a].x[(size_t)j * p.d + r];
       s = warp_sum_d(s);
       if (lane == 0) red[wid] = s;
       __syncthreads();
       if (tid == 0) {
         double t = 0.0;
         for (int q = 0; q < nw; ++q) t += red[q];
-        s_est[arm][r] = t / (double)p.N;
+        s_est[a][r] = t / (double)p.N;
       }
       __syncthreads();
     }
   }
-  if (tid < 2) decode_hand(A.arm[tid].p, s_est[tid], s_hat[tid]);
+  if (tid < 2) decode_hand(arm[tid].p, s_est[tid], s_hat[tid]);
   __syncthreads();
-  const PdafArm& me = A.arm[a];
-  const int N = me.p.N, m = me.p.m, M = A.M;
+}
+
+// weights[j] / sum (pfPose.cpp:294-298), N bins by exact systematic resampling
+// of the M candidate weights (the reference's uniform fallback when no weight
+// is positive), and the measurement columns [head; candidate; neck]
+// (pfPose.cpp:303-323)
+__device__ void pdaf_finish(const PdafArm& me, const double* cand, int M, double* red, uint64_t* red64) {
+  const int tid = threadIdx.x, TB = blockDim.x, lane = tid & 31, wid = tid >> 5, nw = TB >> 5;
+  const int N = me.p.N, m = me.p.m;
   const double* roi = me.roi;
   const double hx = roi[0] + roi[2] / 2.0, hy = roi[1] + 0.5 * roi[3];
   const double nx = roi[0] + roi[2] / 2.0, ny = roi[1] + 1.65 * roi[3];
-  if (M <= 0) {
-    for (int i = tid; i < N; i += TB) {
-      double* z = me.meas + (size_t)i * m;
-      z[0] = hx; z[1] = hy;
-      if (m >= 6) { z[4] = nx; z[5] = ny; }
-      if (me.bins) me.bins[i] = -1;
-    }
-    return;
-  }
-  const double var = 0.8 * roi[2];               // getSampleProb covariance 0.8 w I
-  const double nrm = 1.0 / (2.0 * 3.14159265358979323846 * var);
   double s = 0.0;
-  for (int j = tid; j < M; j += TB) {
-    const double cx = A.cand[2 * j], cy = A.cand[2 * j + 1];
-    double dx = cx - s_hat[a][0], dy = cy - s_hat[a][1];
-    const double po = exp(-0.5 * (dx * dx + dy * dy) / var) * nrm;
-    dx = cx - s_hat[o][0]; dy = cy - s_hat[o][1];
-    const double pt = exp(-0.5 * (dx * dx + dy * dy) / var) * nrm;
-    const double Z = po * A.Pa + pt * A.Pa + A.clutter * (1.0 - 2.0 * A.Pa);
-    const double w = A.Pa * po / Z;
-    me.w[j] = w;
-    s += w;
-  }
+  for (int j = tid; j < M; j += TB) s += me.w[j];
   s = warp_sum_d(s);
   if (lane == 0) red[wid] = s;
   __syncthreads();
@@ -459,7 +443,7 @@ __global__ void __launch_bounds__(256) pdaf_kernel(PdafArgs A) {
   double wmax = 0.0;
   int inf = 0;
   for (int j = tid; j < M; j += TB) {
-    double v = me.w[j] / sum;                   // weights1[j] / sum1 (pfPose.cpp:294-298)
+    double v = me.w[j] / sum;
     me.w[j] = v;
     if (isinf(v) && v > 0) inf = 1;
     if (v > 0.0) wmax = fmax(wmax, v);
@@ -497,12 +481,158 @@ __global__ void __launch_bounds__(256) pdaf_kernel(PdafArgs A) {
     scatter_walk(j0, j1, P, N, me.U, Qt, [&](int j) { return quantize_f64(me.w[j], e); }, bins);
   }
   __syncthreads();
-  for (int i = tid; i < N; i += TB) {          // measurement columns (pfPose.cpp:306-323)
+  for (int i = tid; i < N; i += TB) {
     const int bi = bins[i];
     double* z = me.meas + (size_t)i * m;
     z[0] = hx; z[1] = hy;
-    z[2] = A.cand[2 * bi]; z[3] = A.cand[2 * bi + 1];
+    z[2] = cand[2 * bi]; z[3] = cand[2 * bi + 1];
     if (m >= 6) { z[4] = nx; z[5] = ny; }
+  }
+}
+
+__device__ __forceinline__ double gauss2_pdf(double x, double y, const double* hat, double var) {
+  const double dx = x - hat[0], dy = y - hat[1];
+  return exp(-0.5 * (dx * dx + dy * dy) / var) / (2.0 * 3.14159265358979323846 * var);
+}
+
+__global__ void __launch_bounds__(256) pdaf_kernel(PdafArgs A) {
+  __shared__ double red[32];
+  __shared__ uint64_t red64[34];
+  __shared__ double s_est[2][MKF_MAX_D];
+  __shared__ double s_hat[2][2];
+  const int a = blockIdx.x, o = 1 - a;
+  const int tid = threadIdx.x, TB = blockDim.x;
+  pdaf_hats(A.arm, s_est, s_hat, red);
+  const PdafArm& me = A.arm[a];
+  const int N = me.p.N, m = me.p.m, M = A.M;
+  const double* roi = me.roi;
+  if (M <= 0) {
+    const double hx = roi[0] + roi[2] / 2.0, hy = roi[1] + 0.5 * roi[3];
+    const double nx = roi[0] + roi[2] / 2.0, ny = roi[1] + 1.65 * roi[3];
+    for (int i = tid; i < N; i += TB) {
+      double* z = me.meas + (size_t)i * m;
+      z[0] = hx; z[1] = hy;
+      if (m >= 6) { z[4] = nx; z[5] = ny; }
+      if (me.bins) me.bins[i] = -1;
+    }
+    return;
+  }
+  const double var = 0.8 * roi[2];               // getSampleProb covariance 0.8 w I
+  for (int j = tid; j < M; j += TB) {
+    const double cx = A.cand[2 * j], cy = A.cand[2 * j + 1];
+    const double po = gauss2_pdf(cx, cy, s_hat[a], var), pt = gauss2_pdf(cx, cy, s_hat[o], var);
+    const double Z = po * A.Pa + pt * A.Pa + A.clutter * (1.0 - 2.0 * A.Pa);
+    me.w[j] = A.Pa * po / Z;
+  }
+  __syncthreads();
+  pdaf_finish(me, A.cand, M, red, red64);
+}
+
+// Likelihood-image proposal (pfPose.cpp:210-301): per arm, M candidates drawn
+// uniformly in the box below the face on the first frame after (re)start
+// (pfPose.cpp:228-235) or from N(hand, (0.8 w)^2 I) otherwise (getSamples,
+// pf2DRao.cpp:85-103), scored by the blurred likelihood L = image / 255 at the
+// candidate's pixel over Z = Pa p_own + Pa p_other + clutter (1 - 2 Pa)
+// (pfPose.cpp:250-289), then normalised and resampled as above.
+struct PdafImageArgs {
+  PdafArm arm[2];
+  double* cand[2];          // M x 2 per arm (device, written)
+  const uint8_t* img;
+  int width, height, pitch, M, init;
+  double Pa, clutter;
+  uint32_t frame;
+};
+constexpr uint32_t kStreamPropose = 0x104u;
+
+__global__ void __launch_bounds__(256) pdaf_image_kernel(PdafImageArgs A) {
+  __shared__ double red[32];
+  __shared__ uint64_t red64[34];
+  __shared__ double s_est[2][MKF_MAX_D];
+  __shared__ double s_hat[2][2];
+  const int a = blockIdx.x, o = 1 - a;
+  const int tid = threadIdx.x, TB = blockDim.x;
+  pdaf_hats(A.arm, s_est, s_hat, red);
+  const PdafArm& me = A.arm[a];
+  const double* roi = me.roi;
+  const double var = 0.8 * roi[2];
+  const double sd = 0.8 * roi[2];                // randn with the matrix 0.8 w I as its "stddev"
+  const int xo = (int)roi[0], yo = (int)roi[1], wi = (int)roi[2], hi = (int)roi[3];
+  const int xmin = max(xo - 4 * wi, 0), xmax = min(xo + 5 * wi, A.width);
+  const int ymin = min(yo + hi, A.height), ymax = min(yo + 7 * hi, A.height);
+  double* cand = A.cand[a];
+  for (int j = tid; j < A.M; j += TB) {
+    const u32x4 w = draw_block(me.p_seed, me.p_track, A.frame, (uint32_t)j, kStreamPropose);
+    double cx, cy;
+    if (A.init) {
+      cx = xmin + (double)w.x * (1.0 / 4294967296.0) * (double)(xmax - xmin);
+      cy = ymin + (double)w.y * (1.0 / 4294967296.0) * (double)(ymax - ymin);
+    } else {
+      float n0, n1;
+      box_muller(w.x, w.y, n0, n1);
+      cx = s_hat[a][0] + sd * (double)n0;
+      cy = s_hat[a][1] + sd * (double)n1;
+    }
+    cand[2 * j] = cx;
+    cand[2 * j + 1] = cy;
+    double wt = 0.0;
+    if (cy > 0.0 && cy < A.height && cx > 0.0 && cx < A.width) {
+      const double L = (double)A.img[(size_t)(int)cy * A.pitch + (int)cx] / 255.0;
+      if (L != 0.0) {
+        const double po = gauss2_pdf(cx, cy, s_hat[a], var), pt = gauss2_pdf(cx, cy, s_hat[o], var);
+        wt = L / (po * A.Pa + pt * A.Pa + A.clutter * (1.0 - 2.0 * A.Pa));
+      }
+    }
+    me.w[j] = wt;
+  }
+  __syncthreads();
+  pdaf_finish(me, cand, A.M, red, red64);
+}
+
+// GaussianBlur(likelihood, 15x15, sigma 3, BORDER_DEFAULT) (pfPose.cpp:213) as a
+// separable float filter: each pass is the fmaf chain over the 15 taps in tap
+// order, the border reflects without repeating the edge pixel, and the result
+// is rounded to nearest-even and saturated to 8 bits.
+constexpr int kBlurR = 7, kBlurTile = 32;
+struct BlurArgs {
+  const uint8_t* in;
+  uint8_t* out;
+  int width, height, pitch_in, pitch_out;
+  float w[2 * kBlurR + 1];
+};
+__device__ __forceinline__ int reflect101(int i, int n) {
+  if (i < 0) i = -i;
+  if (i >= n) i = 2 * n - 2 - i;
+  return i;
+}
+__global__ void __launch_bounds__(256) blur_kernel(BlurArgs A) {
+  constexpr int T = kBlurTile, R = kBlurR, S = T + 2 * R;
+  __shared__ float s_in[S][S + 1];
+  __shared__ float s_h[S][T + 1];
+  const int x0 = blockIdx.x * T, y0 = blockIdx.y * T;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x, nt = blockDim.x * blockDim.y;
+  for (int q = tid; q < S * S; q += nt) {
+    const int r = q / S, c = q - r * S;
+    const int y = reflect101(y0 + r - R, A.height), x = reflect101(x0 + c - R, A.width);
+    s_in[r][c] = (float)A.in[(size_t)y * A.pitch_in + x];
+  }
+  __syncthreads();
+  for (int q = tid; q < S * T; q += nt) {          // horizontal pass over every staged row
+    const int r = q / T, c = q - r * T;
+    float acc = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 2 * R + 1; ++k) acc = fmaf(A.w[k], s_in[r][c + k], acc);
+    s_h[r][c] = acc;
+  }
+  __syncthreads();
+  for (int q = tid; q < T * T; q += nt) {          // vertical pass
+    const int r = q / T, c = q - r * T;
+    const int y = y0 + r, x = x0 + c;
+    if (y >= A.height || x >= A.width) continue;
+    float acc = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 2 * R + 1; ++k) acc = fmaf(A.w[k], s_h[r + k][c], acc);
+    const float v = fminf(fmaxf(rintf(acc), 0.0f), 255.0f);
+    A.out[(size_t)y * A.pitch_out + x] = (uint8_t)v;
   }
 }
 
@@ -519,10 +649,30 @@ struct mkf_rbpf {
   int hand_joint;
   bool dirty, ready;
   double *d_f, *d_B, *d_Q, *d_H, *d_BH, *d_R, *d_w, *d_mu, *d_Sigma, *d_Bm, *d_mm, *d_Hd, *d_hb;
-  double *x, *P, *tx, *tP, *logw, *wn, *pw;
+  double *x, *P, *tx, *tP, *logw, *wn, *pw, *pc;
   int *ind, *anc, *bins, *status;
-  int pw_cap;
+  int pw_cap, pc_cap;
 };
+
+// per-arm candidate-weight (M) and candidate (2 M) scratch
+static int rbpf_pdaf_scratch(mkf_rbpf* h, int M, bool cand) {
+  M = std::max(M, 1);
+  if (h->pw_cap < M) {
+    if (h->pw) cudaFree(h->pw);
+    h->pw = nullptr;
+    h->pw_cap = 0;
+    MKF_CUDA(cudaMalloc(&h->pw, sizeof(double) * M));
+    h->pw_cap = M;
+  }
+  if (cand && h->pc_cap < M) {
+    if (h->pc) cudaFree(h->pc);
+    h->pc = nullptr;
+    h->pc_cap = 0;
+    MKF_CUDA(cudaMalloc(&h->pc, sizeof(double) * 2 * (size_t)M));
+    h->pc_cap = M;
+  }
+  return MKF_OK;
+}
 
 static void rbpf_free_params(mkf_rbpf* h) {
   double* ps[] = {h->d_f, h->d_B, h->d_Q, h->d_H, h->d_BH, h->d_R, h->d_w, h->d_mu, h->d_Sigma,
@@ -784,7 +934,7 @@ extern "C" int mkf_rbpf_status(mkf_rbpf_t h, int* status) {
 extern "C" int mkf_rbpf_destroy(mkf_rbpf_t h) {
   if (!h) return MKF_OK;
   rbpf_free_params(h);
-  void* ps[] = {h->x, h->P, h->tx, h->tP, h->logw, h->wn, h->pw, h->ind, h->anc, h->bins, h->status};
+  void* ps[] = {h->x, h->P, h->tx, h->tP, h->logw, h->wn, h->pw, h->pc, h->ind, h->anc, h->bins, h->status};
   for (void* p : ps) if (p) cudaFree(p);
   delete h;
   return MKF_OK;
@@ -807,14 +957,9 @@ extern "C" int mkf_pdaf_associate(mkf_rbpf_t arm0, mkf_rbpf_t arm1, uint32_t fra
     mkf_rbpf_t h = arms[i];
     int st = rbpf_sync_params(h);
     if (st) return st;
-    if (h->pw_cap < std::max(M, 1)) {
-      if (h->pw) cudaFree(h->pw);
-      h->pw = nullptr;
-      h->pw_cap = 0;
-      MKF_CUDA(cudaMalloc(&h->pw, sizeof(double) * std::max(M, 1)));
-      h->pw_cap = std::max(M, 1);
-    }
+    if ((st = rbpf_pdaf_scratch(h, M, false))) return st;
     a.arm[i].p = rbpf_params(h);
+    a.arm[i].p_seed = h->seed; a.arm[i].p_track = h->track;
     a.arm[i].x = h->x;
     for (int q = 0; q < 4; ++q) a.arm[i].roi[q] = roi[4 * i + q];
     a.arm[i].U = draw_block(h->seed, h->track, frame, kItemFrame, kStreamPdaf).x;
@@ -825,5 +970,63 @@ extern "C" int mkf_pdaf_associate(mkf_rbpf_t arm0, mkf_rbpf_t arm1, uint32_t fra
   a.cand = d_cand; a.M = M; a.Pa = Pa; a.clutter = clutter;
   pdaf_kernel<<<2, 256, 0, s>>>(a);
   MKF_CHECK_LAUNCH("mkf_pdaf_associate");
+  return MKF_OK;
+}
+
+extern "C" int mkf_pdaf_propose_image(mkf_rbpf_t arm0, mkf_rbpf_t arm1, uint32_t frame, const double* roi,
+                                      const uint8_t* d_like, int width, int height, int pitch, int M, int init,
+                                      double Pa, double clutter, double* d_meas0, double* d_meas1, int* d_bins0,
+                                      int* d_bins1, double* d_cand0, double* d_cand1, mkf_stream_t stream) {
+  MKF_ARG(arm0 && arm1 && roi && d_like && d_meas0 && d_meas1, "mkf_pdaf_propose_image: null argument");
+  MKF_ARG(width >= 1 && height >= 1 && pitch >= width, "mkf_pdaf_propose_image: bad image size");
+  MKF_ARG(M >= 1 && M <= (1 << 20), "mkf_pdaf_propose_image: M must be in [1, 1048576]");
+  MKF_ARG(arm0->m >= 4 && arm1->m >= 4, "mkf_pdaf_propose_image: measurement needs head and hand rows");
+  MKF_ARG(roi[2] > 0.0 && roi[6] > 0.0, "mkf_pdaf_propose_image: ROI width must be positive");
+  cudaStream_t s = (cudaStream_t)stream;
+  mkf_rbpf_t arms[2] = {arm0, arm1};
+  double* meas[2] = {d_meas0, d_meas1};
+  int* bins[2] = {d_bins0, d_bins1};
+  double* cands[2] = {d_cand0, d_cand1};
+  PdafImageArgs a;
+  memset(&a, 0, sizeof(a));
+  for (int i = 0; i < 2; ++i) {
+    mkf_rbpf_t h = arms[i];
+    int st = rbpf_sync_params(h);
+    if (st) return st;
+    if ((st = rbpf_pdaf_scratch(h, M, cands[i] == nullptr))) return st;
+    a.arm[i].p = rbpf_params(h);
+    a.arm[i].p_seed = h->seed; a.arm[i].p_track = h->track;
+    a.arm[i].x = h->x;
+    for (int q = 0; q < 4; ++q) a.arm[i].roi[q] = roi[4 * i + q];
+    a.arm[i].U = draw_block(h->seed, h->track, frame, kItemFrame, kStreamPdaf).x;
+    a.arm[i].meas = meas[i];
+    a.arm[i].bins = bins[i] ? bins[i] : h->bins;
+    a.arm[i].w = h->pw;
+    a.cand[i] = cands[i] ? cands[i] : h->pc;
+  }
+  a.img = d_like; a.width = width; a.height = height; a.pitch = pitch; a.M = M; a.init = init ? 1 : 0;
+  a.Pa = Pa; a.clutter = clutter; a.frame = frame;
+  pdaf_image_kernel<<<2, 256, 0, s>>>(a);
+  MKF_CHECK_LAUNCH("mkf_pdaf_propose_image");
+  return MKF_OK;
+}
+
+extern "C" int mkf_likelihood_blur(const uint8_t* d_in, int width, int height, int pitch_in, uint8_t* d_out,
+                                   int pitch_out, mkf_stream_t stream) {
+  MKF_ARG(d_in && d_out && d_in != d_out, "mkf_likelihood_blur: null or aliased buffers");
+  MKF_ARG(width >= 8 && height >= 8 && pitch_in >= width && pitch_out >= width,
+          "mkf_likelihood_blur: image must be at least 8 x 8 with pitches >= width");
+  BlurArgs a;
+  a.in = d_in; a.out = d_out; a.width = width; a.height = height; a.pitch_in = pitch_in; a.pitch_out = pitch_out;
+  double e[2 * kBlurR + 1], sum = 0.0;
+  for (int k = 0; k <= 2 * kBlurR; ++k) {
+    const double x = (double)(k - kBlurR);
+    e[k] = std::exp(-x * x / (2.0 * 3.0 * 3.0));
+    sum += e[k];
+  }
+  for (int k = 0; k <= 2 * kBlurR; ++k) a.w[k] = (float)(e[k] / sum);
+  dim3 grid((width + kBlurTile - 1) / kBlurTile, (height + kBlurTile - 1) / kBlurTile), block(32, 8);
+  blur_kernel<<<grid, block, 0, (cudaStream_t)stream>>>(a);
+  MKF_CHECK_LAUNCH("mkf_likelihood_blur");
   return MKF_OK;
 }

@@ -395,6 +395,42 @@ def pdaf_associate(arm0, arm1, frame, roi, cand, Pa=0.05, clutter=1e-4, meas=Non
     return meas[0], meas[1], bins[0], bins[1]
 
 
+def likelihood_blur(img, out=None, stream=None):
+    """GaussianBlur 15x15, sigma 3 of an (H, W) uint8 CUDA tensor (pfPose.cpp:213)."""
+    import torch
+    img = img.contiguous()
+    H, W = img.shape
+    out = torch.empty_like(img) if out is None else out
+    N.check(N.lib().mkf_likelihood_blur(_ptr(img), W, H, W, _ptr(out), out.stride(0), _stream(torch, stream)),
+            "mkf_likelihood_blur")
+    return out
+
+
+def pdaf_propose_image(arm0, arm1, frame, roi, like, M, init, Pa=0.05, clutter=1e-4, meas=None, bins=None,
+                       cands=None, stream=None):
+    """getMeasurementProposal over a blurred likelihood image (pfPose.cpp:210-329):
+    M candidates per arm (uniform box when init, else around the decoded hand),
+    weights L / Z, N bins, measurement rows.  like: (H, W) uint8 CUDA tensor.
+    Returns (meas0, meas1, bins0, bins1, cand0, cand1)."""
+    torch = arm0.torch
+    roi = _d(roi).reshape(8)
+    H, W = like.shape
+    if meas is None:
+        meas = (torch.zeros((arm0.N, arm0.m), dtype=torch.float64, device="cuda"),
+                torch.zeros((arm1.N, arm1.m), dtype=torch.float64, device="cuda"))
+    if bins is None:
+        bins = (torch.zeros(arm0.N, dtype=torch.int32, device="cuda"),
+                torch.zeros(arm1.N, dtype=torch.int32, device="cuda"))
+    if cands is None:
+        cands = (torch.zeros((M, 2), dtype=torch.float64, device="cuda"),
+                 torch.zeros((M, 2), dtype=torch.float64, device="cuda"))
+    N.check(N.lib().mkf_pdaf_propose_image(arm0.h, arm1.h, int(frame), _hp(roi), _ptr(like), W, H, like.stride(0),
+                                           int(M), int(bool(init)), float(Pa), float(clutter), _ptr(meas[0]),
+                                           _ptr(meas[1]), _ptr(bins[0]), _ptr(bins[1]), _ptr(cands[0]),
+                                           _ptr(cands[1]), _stream(torch, stream)), "mkf_pdaf_propose_image")
+    return meas[0], meas[1], bins[0], bins[1], cands[0], cands[1]
+
+
 class PoseTracker:
     """ROS-free replacement of PFTracker's per-frame flow (pfPose.cpp:332-385):
     with a head ROI present, associate hand candidates (PDAF) and update both
@@ -412,6 +448,28 @@ class PoseTracker:
                      torch.zeros(arm1.N, dtype=torch.int32, device="cuda"))
         self.est = (torch.zeros(arm0.d, dtype=torch.float64, device="cuda"),
                     torch.zeros(arm1.d, dtype=torch.float64, device="cuda"))
+
+    def step_image(self, frame, roi, likelihood, n_cand=None):
+        """The reference's own frame (pfPose.cpp:332-385): blur the MONO8
+        likelihood, propose 10 N candidates per arm (uniform box on the first
+        frame after a start or a no-face frame), weight, resample, update.
+        roi: (2, 4) or None (no face: skip and restart the proposals)."""
+        if roi is None:
+            self.init = False
+            return None
+        torch = self.torch
+        if getattr(self, "_blur", None) is None or self._blur.shape != likelihood.shape:
+            self._blur = torch.empty_like(likelihood)
+        likelihood_blur(likelihood, out=self._blur)
+        M = 10 * self.arms[0].N if n_cand is None else int(n_cand)
+        pdaf_propose_image(self.arms[0], self.arms[1], frame, roi, self._blur, M, not getattr(self, "init", False),
+                           self.Pa, self.clutter, meas=self.meas, bins=self.bins)
+        self.init = True
+        for a in range(2):
+            arm = self.arms[a]
+            arm.update(self.meas[a], mask=(1 << arm.m) - 1, frame=frame)
+            arm.getEstimator(self.est[a])
+        return self.est
 
     def step(self, frame, roi, cand):
         """roi: (2,4) per-arm ROI or None (no face -> skip); cand: (M,2) CUDA float64."""

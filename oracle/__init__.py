@@ -124,6 +124,8 @@ def _declare(L):
     L.mko_bpf_run_tracks.argtypes = [I, P, I, I, I, P, P, P, P, P, P, P, P,
                                      F, F, F, F, P, P, P, P, P, I]
     L.mko_num_threads.restype = I
+    L.mko_gaussian_blur_u8.argtypes = [P, I, I, P]
+    L.mko_image_lookup.argtypes = [I, P, P, I, I, P]
     L.mko_pose_decode.argtypes = [I, I, P, P, P, P]
     L.mko_pose3d.argtypes = [P, P, P]
     L.mko_pose2d_record.argtypes = [P, P, P]
@@ -545,3 +547,21 @@ def pose2d_record(e1, e2):
     out = np.zeros(16)
     lib().mko_pose2d_record(_p(_c(e1, np.float64)), _p(_c(e2, np.float64)), _p(out))
     return out.reshape(8, 2)
+
+
+# ---------------------------------------------------------------- f1 image front end
+def gaussian_blur_u8(img):
+    img = np.ascontiguousarray(img, np.uint8)
+    H, W = img.shape
+    out = np.zeros_like(img)
+    lib().mko_gaussian_blur_u8(_p(img), W, H, _p(out))
+    return out
+
+
+def image_lookup(cand, img):
+    img = np.ascontiguousarray(img, np.uint8)
+    H, W = img.shape
+    cand = _c(cand, np.float64).reshape(-1, 2)
+    L = np.zeros(cand.shape[0])
+    lib().mko_image_lookup(cand.shape[0], _p(cand), _p(img), W, H, _p(L))
+    return L

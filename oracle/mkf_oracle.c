@@ -804,3 +804,42 @@ void mko_pose2d_record(const double* e1, const double* e2, double* p) {
   p[12] = e1[6]; p[13] = e1[7];                                 /* shoulder1 */
   p[14] = e2[6]; p[15] = e2[7];                                 /* shoulder2 */
 }
+
+/* ------------------------------------------------------------------------ */
+/* f1: likelihood-image front end (pfPose.cpp:210-301)                        */
+/* ------------------------------------------------------------------------ */
+static int reflect101(int i, int n) {
+  if (i < 0) i = -i;
+  if (i >= n) i = 2 * n - 2 - i;
+  return i;
+}
+
+void mko_gaussian_blur_u8(const uint8_t* in, int W, int H, uint8_t* out) {
+  float w[15];
+  double e[15], sum = 0.0;
+  for (int k = 0; k < 15; ++k) { double x = (double)(k - 7); e[k] = exp(-x * x / 18.0); sum += e[k]; }
+  for (int k = 0; k < 15; ++k) w[k] = (float)(e[k] / sum);
+  float* h = (float*)malloc(sizeof(float) * (size_t)W * H);
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      float acc = 0.0f;
+      for (int k = 0; k < 15; ++k) acc = fmaf(w[k], (float)in[(size_t)y * W + reflect101(x + k - 7, W)], acc);
+      h[(size_t)y * W + x] = acc;
+    }
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      float acc = 0.0f;
+      for (int k = 0; k < 15; ++k) acc = fmaf(w[k], h[(size_t)reflect101(y + k - 7, H) * W + x], acc);
+      float v = rintf(acc);
+      v = v < 0.0f ? 0.0f : (v > 255.0f ? 255.0f : v);
+      out[(size_t)y * W + x] = (uint8_t)v;
+    }
+  free(h);
+}
+
+void mko_image_lookup(int M, const double* cand, const uint8_t* img, int W, int H, double* L) {
+  for (int j = 0; j < M; ++j) {
+    double x = cand[2 * j], y = cand[2 * j + 1];
+    L[j] = (y > 0 && y < H && x > 0 && x < W) ? (double)img[(size_t)(int)y * W + (int)x] / 255.0 : 0.0;
+  }
+}

@@ -237,6 +237,15 @@ void mko_pose3d(const double* e, const double* Kc, double* pos3d);
  * (mean of both arms), neck (mean), elbow1, elbow2, shoulder1, shoulder2 */
 void mko_pose2d_record(const double* e1, const double* e2, double* pts16);
 
+/* ---- f1: likelihood-image front end (pfPose.cpp:210-301)
+ * GaussianBlur 15x15, sigma 3, BORDER_DEFAULT (reflect-101), as a separable
+ * float filter: taps w_k = (float)(exp(-(k-7)^2/18) / sum), each pass the fmaf
+ * chain over the taps in order, round to nearest-even, saturate to 8 bits. */
+void mko_gaussian_blur_u8(const uint8_t* in, int W, int H, uint8_t* out);
+/* candidate likelihoods L = img[(int)y][(int)x] / 255 inside (0 < x < W,
+ * 0 < y < H), else 0 (pfPose.cpp:250-254) */
+void mko_image_lookup(int M, const double* cand, const uint8_t* img, int W, int H, double* L);
+
 #ifdef __cplusplus
 }
 #endif

@@ -390,3 +390,24 @@ def test_pose3d_oracle_against_closed_form(olib):
     np.testing.assert_array_equal(rec[2], 0.5 * (e1[9:11] + e2[9:11]))
     np.testing.assert_array_equal(rec[3], 0.5 * (e1[12:14] + e2[12:14]))
     np.testing.assert_array_equal(rec[4:], np.stack([e1[3:5], e2[3:5], e1[6:8], e2[6:8]]))
+
+
+def test_blur_oracle_against_float64_convolution(olib):
+    """GaussianBlur restatement (15x15, sigma 3, reflect-101, 8-bit): against a
+    float64 separable convolution it differs by at most one grey level, and a
+    constant image stays constant."""
+    rng = np.random.default_rng(6)
+    img = rng.integers(0, 256, (48, 64)).astype(np.uint8)
+    out = olib.gaussian_blur_u8(img)
+    x = np.arange(15) - 7.0
+    g = np.exp(-x * x / 18.0)
+    g /= g.sum()
+    pad = np.pad(img.astype(np.float64), 7, mode="reflect")          # numpy "reflect" = reflect-101
+    hz = sum(g[k] * pad[:, k:k + 64] for k in range(15))
+    ref = sum(g[k] * hz[k:k + 48, :] for k in range(15))
+    assert np.abs(out.astype(np.int64) - np.rint(ref).astype(np.int64)).max() <= 1
+    const = np.full((20, 30), 137, np.uint8)
+    np.testing.assert_array_equal(olib.gaussian_blur_u8(const), const)
+    cand = np.array([[0.0, 5.0], [10.5, 7.9], [63.99, 47.5], [64.0, 1.0], [3.0, -1.0]])
+    L = olib.image_lookup(cand, out)
+    np.testing.assert_array_equal(L, [0.0, out[7, 10] / 255.0, out[47, 63] / 255.0, 0.0, 0.0])
