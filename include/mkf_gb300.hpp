@@ -11,8 +11,8 @@
 //     .update(measurement)     pf2DRao.cpp:125      .update(d_meas, mask, frame)
 //     .getEstimator()          pf2DRao.cpp:23       .getEstimator()
 //   pf2D ParticleFilter(N, d, side) pf2D.h:25-51    mkf::LegacyParticleFilter
-//   PFTracker::getMeasurementProposal + update      mkf::PoseTracker::step
-//     (pfPose.cpp:210-329, 332-385)
+//   PFTracker::getMeasurementProposal + update      mkf::PoseTracker::stepImage (likelihood
+//     (pfPose.cpp:210-329, 332-385)                  image) / ::step (detection list)
 //   get3Dpose / publish2Dpos (pfPose.cpp:93-208)     mkf::PoseDecoder
 //
 // Errors: every non-MKF_OK status becomes an mkf::Error carrying the status and
@@ -215,6 +215,28 @@ class PoseTracker {
   // candidates (PDAF, pfPose.cpp:210-329) and update both arms; without one the
   // frame is skipped (pfPose.cpp:370-378) and false is returned.  roi: 8 doubles
   // (x_offset, y_offset, width, height per arm) or nullptr; cand: M (x, y) pairs.
+  // The reference's own frame (pfPose.cpp:332-385, 210-329): blur the MONO8
+  // likelihood (device, row pitch in bytes), propose nCand candidates per arm
+  // (10 N when 0; uniform in the box below the face on the first frame after a
+  // start or a no-face frame, else around the decoded hands), weight by the
+  // likelihood over the PDA normaliser, resample and update both arms.
+  bool stepImage(uint32_t frame, const double* roi, const uint8_t* d_likelihood, int width, int height, int pitch,
+                 int nCand = 0) {
+    if (!roi) { init_ = false; return false; }
+    if (blur_.size() < static_cast<size_t>(width) * height) blur_ = DeviceArray<uint8_t>(static_cast<size_t>(width) * height);
+    check(mkf_likelihood_blur(d_likelihood, width, height, pitch, blur_.data(), width, a1_.stream()),
+          "mkf_likelihood_blur");
+    const int M = nCand > 0 ? nCand : 10 * a1_.nParticles;
+    check(mkf_pdaf_propose_image(a1_.handle(), a2_.handle(), frame, roi, blur_.data(), width, height, width, M,
+                                 init_ ? 0 : 1, Pa_, clutter_, meas1_.data(), meas2_.data(), nullptr, nullptr,
+                                 nullptr, nullptr, a1_.stream()),
+          "mkf_pdaf_propose_image");
+    init_ = true;
+    a1_.update(meas1_.data(), (1u << a1_.m) - 1u, frame);
+    a2_.update(meas2_.data(), (1u << a2_.m) - 1u, frame);
+    return true;
+  }
+
   bool step(uint32_t frame, const double* roi, const std::vector<double>& cand) {
     if (!roi) return false;
     const int M = static_cast<int>(cand.size() / 2);
@@ -235,6 +257,8 @@ class PoseTracker {
   RaoParticleFilter& a2_;
   double Pa_, clutter_;
   DeviceArray<double> meas1_, meas2_, cand_;
+  DeviceArray<uint8_t> blur_;
+  bool init_ = false;
 };
 
 // ------------------------------------- decode, get3Dpose and publish2Dpos record

@@ -20,6 +20,10 @@
 // Frame file (little-endian): "MKFFRM01", int32 n_frames, then per frame:
 //   int32 frame_id, int32 has_roi, double roi[8] (x_offset, y_offset, width,
 //   height per arm), int32 M, double cand[2M] (hand candidate x, y).
+// Version "MKFFRM02" adds int32 width, height after n_frames and a MONO8
+// likelihood image (height x width bytes) after each frame's candidates; the
+// harness then runs the reference's image path (blur, 10 N proposals per arm,
+// likelihood weights) instead of the candidate list.
 // Output file: "MKFOUT01", int32 n_frames, int32 d, int32 F, then per frame:
 //   int32 frame_id, int32 valid, double est[2][d], double e[2][F],
 //   double points[8][2] (hand1, hand2, head, neck, elbow1, elbow2, shoulder1,
@@ -45,6 +49,12 @@ struct Frame {
   int32_t id = 0, has_roi = 0;
   double roi[8] = {0};
   std::vector<double> cand;
+  std::vector<uint8_t> like;   // MONO8 likelihood image (frame files of version 2)
+};
+
+struct FrameFile {
+  std::vector<Frame> frames;
+  int width = 0, height = 0;   // likelihood image size (0: detection-list frames)
 };
 
 template <class T>
@@ -57,17 +67,26 @@ void wr(std::ofstream& f, const T* v, size_t n = 1) {
   f.write(reinterpret_cast<const char*>(v), static_cast<std::streamsize>(sizeof(T) * n));
 }
 
-std::vector<Frame> read_frames(const std::string& path) {
+FrameFile read_frames(const std::string& path) {
   std::ifstream f(path, std::ios::binary);
   if (!f) throw std::runtime_error("cannot open " + path);
   char magic[8];
   rd(f, magic, 8);
-  if (std::memcmp(magic, "MKFFRM01", 8) != 0) throw std::runtime_error("not a frame file: " + path);
+  const bool v2 = std::memcmp(magic, "MKFFRM02", 8) == 0;
+  if (!v2 && std::memcmp(magic, "MKFFRM01", 8) != 0) throw std::runtime_error("not a frame file: " + path);
+  FrameFile ff;
   int32_t n = 0;
   rd(f, &n);
   if (n < 0) throw std::runtime_error("bad frame count");
-  std::vector<Frame> frames(static_cast<size_t>(n));
-  for (Frame& fr : frames) {
+  if (v2) {
+    int32_t wh[2];
+    rd(f, wh, 2);
+    if (wh[0] < 8 || wh[1] < 8 || wh[0] > 8192 || wh[1] > 8192) throw std::runtime_error("bad image size");
+    ff.width = wh[0];
+    ff.height = wh[1];
+  }
+  ff.frames.resize(static_cast<size_t>(n));
+  for (Frame& fr : ff.frames) {
     rd(f, &fr.id);
     rd(f, &fr.has_roi);
     rd(f, fr.roi, 8);
@@ -76,8 +95,12 @@ std::vector<Frame> read_frames(const std::string& path) {
     if (M < 0 || M > 65536) throw std::runtime_error("bad candidate count");
     fr.cand.resize(static_cast<size_t>(2 * M));
     if (M) rd(f, fr.cand.data(), fr.cand.size());
+    if (v2) {
+      fr.like.resize(static_cast<size_t>(ff.width) * ff.height);
+      rd(f, fr.like.data(), fr.like.size());
+    }
   }
-  return frames;
+  return ff;
 }
 
 struct ArmModel {
@@ -147,7 +170,9 @@ int cmd_track(int argc, char** argv) {
   if (arm1.empty() || arm2.empty() || frames_path.empty() || out_path.empty())
     throw std::runtime_error("track needs --arm1 --arm2 --frames --out");
   const ArmModel m1 = load_arm(mkf::yaml::load(arm1)), m2 = load_arm(mkf::yaml::load(arm2));
-  const std::vector<Frame> frames = read_frames(frames_path);
+  const FrameFile ff = read_frames(frames_path);
+  const std::vector<Frame>& frames = ff.frames;
+  const bool image_mode = ff.width > 0;
   const int K = m1.means.rows, d = m1.means.cols, F = m1.pca_proj.cols;
   const int T = static_cast<int>(frames.size());
 
@@ -159,6 +184,11 @@ int cmd_track(int argc, char** argv) {
     load_filter(pf2, m2, m2.gamma);
     mkf::PoseTracker tracker(pf1, pf2, Pa, clutter);
     mkf::DeviceArray<double> est1(static_cast<size_t>(T) * d + 1), est2(static_cast<size_t>(T) * d + 1);
+    // likelihood images are staged into a ring of device buffers up front (the
+    // image transport is the caller's, as the ROS topics were)
+    std::vector<mkf::DeviceArray<uint8_t>> like;
+    if (image_mode)
+      for (const Frame& fr : frames) like.emplace_back(fr.like);
     std::vector<int> valid(static_cast<size_t>(T), 0);
     mkf::cuda_check(cudaStreamSynchronize(s), "sync");
     cudaEvent_t e0, e1;
@@ -168,7 +198,11 @@ int cmd_track(int argc, char** argv) {
     mkf::cuda_check(cudaEventRecord(e0, s), "event");
     for (int t = 0; t < T; ++t) {
       const Frame& fr = frames[t];
-      if (tracker.step(static_cast<uint32_t>(fr.id), fr.has_roi ? fr.roi : nullptr, fr.cand)) {
+      const bool ok = image_mode
+                          ? tracker.stepImage(static_cast<uint32_t>(fr.id), fr.has_roi ? fr.roi : nullptr,
+                                              like[t].data(), ff.width, ff.height, ff.width)
+                          : tracker.step(static_cast<uint32_t>(fr.id), fr.has_roi ? fr.roi : nullptr, fr.cand);
+      if (ok) {
         pf1.estimateInto(est1.data() + static_cast<size_t>(t) * d);
         pf2.estimateInto(est2.data() + static_cast<size_t>(t) * d);
         valid[t] = 1;
@@ -211,10 +245,10 @@ int cmd_track(int argc, char** argv) {
     }
     int nvalid = 0;
     for (int v : valid) nvalid += v;
-    std::printf("{\"harness\": \"track\", \"frames\": %d, \"valid_frames\": %d, \"particles_per_arm\": %d, "
+    std::printf("{\"harness\": \"track\", \"input\": \"%s\", \"frames\": %d, \"valid_frames\": %d, \"particles_per_arm\": %d, "
                 "\"wall_s\": %.6f, \"device_s\": %.6f, \"frames_per_s\": %.3f, \"arm_frames_per_s\": %.3f, "
                 "\"status\": [%d, %d]}\n",
-                T, nvalid, N, wall, ms / 1000.0, T / wall, 2.0 * nvalid / wall, pf1.status(), pf2.status());
+                image_mode ? "likelihood images" : "candidate lists", T, nvalid, N, wall, ms / 1000.0, T / wall, 2.0 * nvalid / wall, pf1.status(), pf2.status());
   }
   cudaStreamDestroy(s);
   return 0;

@@ -4,7 +4,8 @@ ROI) input and its HFPose2DArray / TF output (pfPose.cpp:16-21, 173-208).
 
 Frame file: b"MKFFRM01", int32 n, then per frame int32 id, int32 has_roi,
 float64 roi[8] (x_offset, y_offset, width, height per arm), int32 M,
-float64 cand[2M].  Output file: b"MKFOUT01", int32 n, d, F, then per frame
+float64 cand[2M].  Version b"MKFFRM02" adds int32 W, H after n and a W x H
+uint8 likelihood image after each frame's candidates (the image path).  Output file: b"MKFOUT01", int32 n, d, F, then per frame
 int32 id, int32 valid, float64 est[2][d], e[2][F], points[8][2] (hand1, hand2,
 head, neck, elbow1, elbow2, shoulder1, shoulder2), pos3d[2][3][5]."""
 from __future__ import annotations
@@ -18,18 +19,24 @@ import numpy as np
 HARNESS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "harness", "mkf_harness")
 
 
-def write_frames(path, frame_ids, rois, cands):
-    """rois[t]: (2, 4) array or None (no face); cands[t]: (M, 2) array."""
+def write_frames(path, frame_ids, rois, cands, images=None):
+    """rois[t]: (2, 4) array or None (no face); cands[t]: (M, 2) array or None;
+    images (optional): per-frame (H, W) uint8 likelihood images (version 2)."""
     with open(path, "wb") as f:
-        f.write(b"MKFFRM01")
+        f.write(b"MKFFRM02" if images is not None else b"MKFFRM01")
         f.write(struct.pack("<i", len(frame_ids)))
-        for fid, roi, c in zip(frame_ids, rois, cands):
+        if images is not None:
+            H, W = np.asarray(images[0]).shape
+            f.write(struct.pack("<ii", W, H))
+        for t, (fid, roi, c) in enumerate(zip(frame_ids, rois, cands)):
             c = np.zeros((0, 2)) if c is None else np.asarray(c, np.float64).reshape(-1, 2)
             f.write(struct.pack("<ii", int(fid), 0 if roi is None else 1))
             r = np.zeros(8) if roi is None else np.asarray(roi, np.float64).reshape(8)
             f.write(r.astype("<f8").tobytes())
             f.write(struct.pack("<i", c.shape[0]))
             f.write(c.astype("<f8").tobytes())
+            if images is not None:
+                f.write(np.ascontiguousarray(images[t], np.uint8).tobytes())
 
 
 def read_output(path):

@@ -66,3 +66,54 @@ def test_harness_matches_python_path(cuda, olib, tmp_path):
     hands = np.stack([np.stack([c[0], c[1]]) for c in cands])[ok]
     err = np.abs(out["points"][ok][:, 0:2] - hands).mean()
     assert err < 60.0, err
+
+
+def test_harness_image_path_matches_python(cuda, olib, tmp_path):
+    """Likelihood-image frames (the reference node's own input): the harness and
+    the Python PoseTracker.step_image give the same estimates bit for bit, and
+    no-face frames restart the proposals in both."""
+    from mkfbodytracker_pdaf_gb300 import build, cvyaml, harness_io, synth
+    from mkfbodytracker_pdaf_gb300.filters import PoseTracker, RaoBlackwellisedPF
+    torch = cuda
+    build.build_harness()
+    z = np.load(os.path.join(HERE, "golden", "ref_models.npz"))
+    paths = []
+    for a in range(2):
+        p = str(tmp_path / ("arm%d.yml" % a))
+        cvyaml.save_arm_model(p, z["arm%d_means" % a], z["arm%d_covs" % a], z["arm%d_weights" % a],
+                              z["arm%d_pca_proj" % a], z["arm%d_pca_mean" % a],
+                              z["arm0_gamma_own_file"] if a == 0 else z["arm1_gamma"])
+        paths.append(p)
+    arms = cvyaml.load_reference_models(paths[0], paths[1])
+    T, N, seed = 12, 200, 5
+    _, e, rois, _ = synth.make_reference_scene(arms, T=T, no_face_every=5)
+    rng = np.random.default_rng(9)
+    yy, xx = np.mgrid[0:480, 0:640]
+    images = []
+    for t in range(T):
+        img = rng.uniform(0, 30, (480, 640))
+        for a in range(2):
+            img += 255.0 * np.exp(-0.5 * ((xx - e[a, t, 0]) ** 2 + (yy - e[a, t, 1]) ** 2) / 10.0 ** 2)
+        images.append(np.clip(img, 0, 255).astype(np.uint8))
+    fpath, opath = str(tmp_path / "frames2.bin"), str(tmp_path / "out2.bin")
+    harness_io.write_frames(fpath, list(range(T)), rois, [None] * T, images=images)
+    line = json.loads(harness_io.run_track(paths[0], paths[1], fpath, opath, particles=N, seed=seed))
+    assert line["input"] == "likelihood images" and line["status"] == [0, 0]
+    out = harness_io.read_output(opath)
+    pfs = []
+    for a in range(2):
+        arm = arms[a]
+        pf = RaoBlackwellisedPF(12, 6, 15, N, seed=seed, track_id=a)
+        for k in range(15):
+            pf.loadGaussian(k, arm["means"][k], arm["covs"][k * 12:(k + 1) * 12], arm["pca_proj"], arm["pca_mean"],
+                            arm["weights"][k], arm["gamma"][k])
+        pf.set_hand_decode(arm["pca_proj"][:, 0:2].T.copy(), arm["pca_mean"][0:2].copy())
+        pf.resetTracker()
+        pfs.append(pf)
+    trk = PoseTracker(pfs[0], pfs[1])
+    for t in range(T):
+        est = trk.step_image(t, rois[t], torch.from_numpy(images[t]).cuda())
+        assert (est is not None) == bool(out["valid"][t])
+        if est is not None:
+            for a in range(2):
+                np.testing.assert_array_equal(out["est"][t, a], est[a].cpu().numpy())
