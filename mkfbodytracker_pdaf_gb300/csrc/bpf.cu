@@ -1034,6 +1034,7 @@ static StreamArgs stream_args(BpfHandle& h) {
 }
 
 extern "C" int mkf_bpf_reset(mkf_bpf_t H, mkf_stream_t stream) {
+  MKF_RANGE("mkf_bpf_reset");
   MKF_ARG(H, "mkf_bpf_reset: null handle");
   BpfHandle& h = H->h;
   cudaStream_t s = (cudaStream_t)stream;
@@ -1077,6 +1078,7 @@ static int enqueue_update(BpfHandle& h, uint32_t frame, const uint32_t* frame_ba
 
 extern "C" int mkf_bpf_update(mkf_bpf_t H, uint32_t frame, const int* d_det_off, const float* d_det,
                               float* d_est, float* d_loglik, float* d_ess, mkf_stream_t stream) {
+  MKF_RANGE("mkf_bpf_update");
   MKF_ARG(H && d_det_off, "mkf_bpf_update: null argument");
   BpfHandle& h = H->h;
   if (!h.ready) { set_error("mkf_bpf_update: call mkf_bpf_reset first"); return MKF_ERR_STATE; }
@@ -1145,6 +1147,7 @@ extern "C" int mkf_bpf_graph_create(mkf_bpf_t H, int n_frames, const int* d_det_
 }
 
 extern "C" int mkf_bpf_graph_launch(mkf_bpf_graph_t g, uint32_t frame0, mkf_stream_t stream) {
+  MKF_RANGE("mkf_bpf_graph_launch");
   MKF_ARG(g && g->exec, "mkf_bpf_graph_launch: null graph");
   cudaStream_t s = (cudaStream_t)stream;
   set_frame_base_kernel<<<1, 1, 0, s>>>(g->frame_base, frame0);
@@ -1337,6 +1340,7 @@ extern "C" int mkf_bpf_batch_set_variant(mkf_bpf_batch_t B, int flags) {
 extern "C" int mkf_bpf_batch_run(mkf_bpf_batch_t B, const int* d_det_off, const float* d_det,
                                  float* d_est, float* d_loglik, float* d_ess, int* d_status,
                                  mkf_stream_t stream) {
+  MKF_RANGE("mkf_bpf_batch_run");
   MKF_ARG(B && d_det_off && d_est && d_loglik && d_ess && d_status, "mkf_bpf_batch_run: null argument");
   BatchArgs a;
   memset(&a, 0, sizeof(a));
@@ -1354,6 +1358,7 @@ extern "C" int mkf_bpf_batch_run(mkf_bpf_batch_t B, const int* d_det_off, const 
 extern "C" int mkf_bpf_batch_run_host(mkf_bpf_batch_t B, const int* det_off, const float* det, int64_t n_det,
                                       float* est, float* loglik, float* ess, int* status,
                                       mkf_stream_t stream) {
+  MKF_RANGE("mkf_bpf_batch_run_host");
   MKF_ARG(B && det_off && det && est && loglik && ess && status && n_det >= 0, "mkf_bpf_batch_run_host: null argument");
   cudaStream_t s = (cudaStream_t)stream;
   const size_t G = (size_t)B->G, J = (size_t)B->J, d = (size_t)B->d;

@@ -1036,6 +1036,7 @@ static MixArgs mix_args(mkf_mixkf* h, const int* det_off, const float* det) {
 
 extern "C" int mkf_mixkf_forward(mkf_mixkf_t h, const int* d_det_off, const float* d_det, double* d_loglik,
                                  double* d_total, mkf_stream_t stream) {
+  MKF_RANGE("mkf_mixkf_forward");
   MKF_ARG(h && d_det_off && d_det, "mkf_mixkf_forward: null argument");
   if (!h->have_theta) { set_error("mkf_mixkf_forward: set theta first"); return MKF_ERR_STATE; }
   cudaStream_t s = (cudaStream_t)stream;
@@ -1052,6 +1053,7 @@ extern "C" int mkf_mixkf_forward(mkf_mixkf_t h, const int* d_det_off, const floa
 
 extern "C" int mkf_mixkf_backward(mkf_mixkf_t h, const int* d_det_off, const float* d_det, double* d_grad,
                                   mkf_stream_t stream) {
+  MKF_RANGE("mkf_mixkf_backward");
   MKF_ARG(h && d_det_off && d_det && d_grad, "mkf_mixkf_backward: null argument");
   if (!h->have_theta) { set_error("mkf_mixkf_backward: set theta first"); return MKF_ERR_STATE; }
   if (h->fwd_C != h->C) {
@@ -1094,6 +1096,7 @@ extern "C" int mkf_mixkf_destroy(mkf_mixkf_t h) {
 extern "C" int mkf_adam_step(double* d_theta, const double* d_grad, double* d_m, double* d_v, const uint8_t* d_mask,
                              int n, int step, double lr, double b1, double b2, double eps, int maximize,
                              mkf_stream_t stream) {
+  MKF_RANGE("mkf_adam_step");
   MKF_ARG(d_theta && d_grad && d_m && d_v && n > 0 && step >= 1, "mkf_adam_step: bad argument");
   const double c1 = 1.0 - std::pow(b1, step), c2 = 1.0 - std::pow(b2, step);
   adam_kernel<<<(n + 255) / 256, 256, 0, (cudaStream_t)stream>>>(d_theta, d_grad, d_m, d_v, d_mask, n, c1, c2, lr,

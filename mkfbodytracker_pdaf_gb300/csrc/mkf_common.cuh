@@ -1,6 +1,7 @@
 // mkf_common.cuh -- shared device/host pieces of the GB300 filtering hot path.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 #include <string>
 #include "../../include/mkf_gb300.h"
@@ -28,6 +29,16 @@ int cuda_fail(cudaError_t e, const char* what, const char* file, int line);
   } while (0)
 
 int num_sms();
+
+// NVTX range around the host side of one C-ABI call (named on Nsight
+// timelines; a no-op unless a tool is attached)
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define MKF_RANGE(name) ::mkf::NvtxRange mkf_nvtx_range_(name)
 
 // ---------------------------------------------------------------- Philox4x32-10
 // Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy as 1, 2, 3",

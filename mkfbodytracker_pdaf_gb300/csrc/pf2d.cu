@@ -298,6 +298,7 @@ extern "C" int mkf_pf2d_create(int n_particles, int d, int side, int K, const do
 }
 
 extern "C" int mkf_pf2d_update(mkf_pf2d_t h, uint32_t frame, const double* z, mkf_stream_t stream) {
+  MKF_RANGE("mkf_pf2d_update");
   MKF_ARG(h && z, "mkf_pf2d_update: null argument");
   cudaStream_t s = (cudaStream_t)stream;
   Pf2dArgs a = pf2d_args(h);

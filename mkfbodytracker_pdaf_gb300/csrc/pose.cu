@@ -113,6 +113,7 @@ using namespace mkf;
 
 extern "C" int mkf_pose_decode(const double* d_x, int B, int d, int F, const double* d_Hpca, const double* d_mpca,
                                const double* Kc, double* d_e, double* d_pos3d, int* d_status, mkf_stream_t stream) {
+  MKF_RANGE("mkf_pose_decode");
   MKF_ARG(B >= 0 && d >= 1 && d <= MKF_MAX_D && F >= 1 && F <= kPoseMaxF,
           "mkf_pose_decode: bad argument (B >= 0, 1 <= d <= 24, 1 <= F <= 64)");
   if (B == 0) return MKF_OK;

@@ -828,6 +828,7 @@ extern "C" int mkf_rbpf_set_hand_decode(mkf_rbpf_t h, const double* Hd, const do
 }
 
 extern "C" int mkf_rbpf_reset(mkf_rbpf_t h, const int* bins, mkf_stream_t stream) {
+  MKF_RANGE("mkf_rbpf_reset");
   MKF_ARG(h, "mkf_rbpf_reset: null handle");
   cudaStream_t s = (cudaStream_t)stream;
   int st = rbpf_sync_params(h);
@@ -853,6 +854,7 @@ extern "C" int mkf_rbpf_reset(mkf_rbpf_t h, const int* bins, mkf_stream_t stream
 
 extern "C" int mkf_rbpf_update_u(mkf_rbpf_t h, const double* d_meas, unsigned mask, uint32_t U_ind,
                                  uint32_t U_anc, mkf_stream_t stream) {
+  MKF_RANGE("mkf_rbpf_update_u");
   MKF_ARG(h && d_meas, "mkf_rbpf_update: null argument");
   if (!h->ready) { set_error("mkf_rbpf_update: call mkf_rbpf_reset first"); return MKF_ERR_STATE; }
   int st = rbpf_sync_params(h);
@@ -886,6 +888,7 @@ extern "C" int mkf_rbpf_update_u(mkf_rbpf_t h, const double* d_meas, unsigned ma
 
 extern "C" int mkf_rbpf_update(mkf_rbpf_t h, uint32_t frame, const double* d_meas, unsigned mask,
                                mkf_stream_t stream) {
+  MKF_RANGE("mkf_rbpf_update");
   MKF_ARG(h, "mkf_rbpf_update: null handle");
   const uint32_t U_ind = draw_block(h->seed, h->track, frame, kItemFrame, kStreamIndicator).x;
   const uint32_t U_anc = resample_uniform(h->seed, h->track, frame);
@@ -893,6 +896,7 @@ extern "C" int mkf_rbpf_update(mkf_rbpf_t h, uint32_t frame, const double* d_mea
 }
 
 extern "C" int mkf_rbpf_estimate(mkf_rbpf_t h, double* d_est, mkf_stream_t stream) {
+  MKF_RANGE("mkf_rbpf_estimate");
   MKF_ARG(h && d_est, "mkf_rbpf_estimate: null argument");
   rbpf_estimate_kernel<<<1, 256, 0, (cudaStream_t)stream>>>(h->x, h->N, h->d, d_est);
   MKF_CHECK_LAUNCH("mkf_rbpf_estimate");
@@ -943,6 +947,7 @@ extern "C" int mkf_rbpf_destroy(mkf_rbpf_t h) {
 extern "C" int mkf_pdaf_associate(mkf_rbpf_t arm0, mkf_rbpf_t arm1, uint32_t frame, const double* roi,
                                   const double* d_cand, int M, double Pa, double clutter, double* d_meas0,
                                   double* d_meas1, int* d_bins0, int* d_bins1, mkf_stream_t stream) {
+  MKF_RANGE("mkf_pdaf_associate");
   MKF_ARG(arm0 && arm1 && roi && d_meas0 && d_meas1, "mkf_pdaf_associate: null argument");
   MKF_ARG(M >= 0 && M <= 65536 && (M == 0 || d_cand), "mkf_pdaf_associate: bad candidate list");
   MKF_ARG(arm0->m >= 4 && arm1->m >= 4, "mkf_pdaf_associate: measurement needs head and hand rows");
@@ -977,6 +982,7 @@ extern "C" int mkf_pdaf_propose_image(mkf_rbpf_t arm0, mkf_rbpf_t arm1, uint32_t
                                       const uint8_t* d_like, int width, int height, int pitch, int M, int init,
                                       double Pa, double clutter, double* d_meas0, double* d_meas1, int* d_bins0,
                                       int* d_bins1, double* d_cand0, double* d_cand1, mkf_stream_t stream) {
+  MKF_RANGE("mkf_pdaf_propose_image");
   MKF_ARG(arm0 && arm1 && roi && d_like && d_meas0 && d_meas1, "mkf_pdaf_propose_image: null argument");
   MKF_ARG(width >= 1 && height >= 1 && pitch >= width, "mkf_pdaf_propose_image: bad image size");
   MKF_ARG(M >= 1 && M <= (1 << 20), "mkf_pdaf_propose_image: M must be in [1, 1048576]");
@@ -1013,6 +1019,7 @@ extern "C" int mkf_pdaf_propose_image(mkf_rbpf_t arm0, mkf_rbpf_t arm1, uint32_t
 
 extern "C" int mkf_likelihood_blur(const uint8_t* d_in, int width, int height, int pitch_in, uint8_t* d_out,
                                    int pitch_out, mkf_stream_t stream) {
+  MKF_RANGE("mkf_likelihood_blur");
   MKF_ARG(d_in && d_out && d_in != d_out, "mkf_likelihood_blur: null or aliased buffers");
   MKF_ARG(width >= 8 && height >= 8 && pitch_in >= width && pitch_out >= width,
           "mkf_likelihood_blur: image must be at least 8 x 8 with pitches >= width");

@@ -268,10 +268,12 @@ extern "C" int mkf_draw_particles(uint64_t seed, uint32_t track, uint32_t frame,
 
 extern "C" int mkf_resample_f64(const double* d_w, int L, int N, uint32_t U, int* d_idx, int* d_fallback,
                                 mkf_stream_t stream) {
+  MKF_RANGE("mkf_resample_f64");
   return resample_impl<double>(d_w, L, N, U, d_idx, d_fallback, (cudaStream_t)stream);
 }
 extern "C" int mkf_resample_f32(const float* d_w, int L, int N, uint32_t U, int* d_idx, int* d_fallback,
                                 mkf_stream_t stream) {
+  MKF_RANGE("mkf_resample_f32");
   return resample_impl<float>(d_w, L, N, U, d_idx, d_fallback, (cudaStream_t)stream);
 }
 
@@ -315,6 +317,7 @@ static int noalloc_scratch(unsigned long long** out) {
 
 extern "C" int mkf_resample_f32_noalloc(const float* d_w, int L, int N, uint32_t U, int* d_idx,
                                         int* d_fallback, mkf_stream_t stream) {
+  MKF_RANGE("mkf_resample_f32_noalloc");
   MKF_ARG(d_w && d_idx, "mkf_resample_f32_noalloc: null pointer");
   if (L < 1 || L > kNoAllocMaxWeights) {
     set_error("mkf_resample_f32_noalloc: L must be in [1, 1048576] (the fixed scratch holds 256 tiles "

@@ -24,6 +24,46 @@ def theta_split(theta, K, d):
             theta[2 * K * d:2 * K * d + K * DD].reshape(K, DD), float(theta[-1]))
 
 
+class FitState:
+    """Adam fitting state (theta and moments after `step` steps)."""
+
+    def __init__(self, theta, m, v, step, lr, K, d):
+        self.theta, self.m, self.v = (np.ascontiguousarray(a, np.float64) for a in (theta, m, v))
+        self.step, self.lr, self.K, self.d = int(step), float(lr), int(K), int(d)
+
+
+_FIT_MAGIC = b"MKFFIT01"
+
+
+def save_fit_state(path, st):
+    """Binary file: magic, uint32 header length, JSON header (sizes, step,
+    learning rate, K, d), then theta, m, v as little-endian float64."""
+    import json
+    import struct
+    hdr = json.dumps({"n_theta": int(st.theta.size), "step": st.step, "lr": st.lr, "K": st.K, "d": st.d,
+                      "layout": "theta = [mu (K d), a (K d), Lq packed lower (K d(d+1)/2), sigma]"}).encode()
+    with open(path, "wb") as f:
+        f.write(_FIT_MAGIC)
+        f.write(struct.pack("<I", len(hdr)))
+        f.write(hdr)
+        for a in (st.theta, st.m, st.v):
+            f.write(a.astype("<f8").tobytes())
+
+
+def load_fit_state(path):
+    import json
+    import struct
+    with open(path, "rb") as f:
+        buf = f.read()
+    if buf[:8] != _FIT_MAGIC:
+        raise ValueError("not a fit-state file")
+    (n,) = struct.unpack_from("<I", buf, 8)
+    hdr = json.loads(buf[12:12 + n].decode())
+    k = hdr["n_theta"]
+    arr = np.frombuffer(buf, "<f8", 3 * k, 12 + n).reshape(3, k)
+    return FitState(arr[0], arr[1], arr[2], hdr["step"], hdr["lr"], hdr["K"], hdr["d"])
+
+
 class MixtureKF:
     """Batched mixture KF over the tracks of a synth.MixBatch-like object."""
 
@@ -87,25 +127,40 @@ class MixtureKF:
         N.check(N.lib().mkf_mixkf_status(self.h, C.byref(s)), "mkf_mixkf_status")
         return s.value
 
-    def fit_adam(self, theta0, steps, lr=1e-2, mask=None, callback=None):
+    def fit_adam(self, theta0, steps, lr=1e-2, mask=None, callback=None, resume=None):
         """Maximise the total logL with Adam on the device (theta, moments, mask
-        and gradient stay in HBM; one forward + backward + update per step)."""
+        and gradient stay in HBM; one forward + backward + update per step).
+        resume: a FitState (load_fit_state) to continue from: its theta and
+        moments replace theta0, and the step count continues after its step.
+        Returns (theta, history); self.fit_state holds the state to save."""
         torch = self.torch
+        start = 1
+        if resume is not None:
+            assert resume.theta.size == self.n_theta
+            theta0 = resume.theta
+            start = resume.step + 1
         th = torch.from_numpy(np.ascontiguousarray(theta0, np.float64)).cuda()
-        m = torch.zeros_like(th)
-        v = torch.zeros_like(th)
+        m = torch.zeros_like(th) if resume is None else torch.from_numpy(resume.m.copy()).cuda()
+        v = torch.zeros_like(th) if resume is None else torch.from_numpy(resume.v.copy()).cuda()
         mk = None if mask is None else torch.from_numpy(np.ascontiguousarray(mask, np.uint8)).cuda()
         hist = []
-        for it in range(1, steps + 1):
+        self._fit_tensors = (th, m, v, start - 1, lr)
+        for it in range(start, start + steps):
             self.set_theta(th)
             self.forward()
             self.backward()
             N.check(N.lib().mkf_adam_step(_ptr(th), _ptr(self.grad), _ptr(m), _ptr(v), _ptr(mk), self.n_theta, it,
                                           float(lr), 0.9, 0.999, 1e-8, 1, _stream(torch)), "mkf_adam_step")
+            self._fit_tensors = (th, m, v, it, lr)
             if callback is not None:
                 callback(it, th, self.total)
             hist.append(self.total)
         return th, hist
+
+    @property
+    def fit_state(self):
+        th, m, v, step, lr = self._fit_tensors
+        return FitState(th.cpu().numpy(), m.cpu().numpy(), v.cpu().numpy(), step, lr, self.K, self.d)
 
     def __del__(self):
         try:

@@ -68,3 +68,14 @@ def test_frame_file_layout(tmp_path):
     fid, has = struct.unpack_from("<ii", buf, 120)
     assert (fid, has) == (6, 0)
     assert len(buf) == 120 + 8 + 64 + 4
+
+
+def test_fit_state_file_roundtrip(tmp_path):
+    from mkfbodytracker_pdaf_gb300 import mixkf
+    st = mixkf.FitState(np.linspace(-1, 1, 37), np.full(37, 0.5), np.full(37, 2.0), 12, 0.02, 2, 12)
+    p = str(tmp_path / "fit.bin")
+    mixkf.save_fit_state(p, st)
+    back = mixkf.load_fit_state(p)
+    assert (back.step, back.lr, back.K, back.d) == (12, 0.02, 2, 12)
+    for a, b in ((back.theta, st.theta), (back.m, st.m), (back.v, st.v)):
+        np.testing.assert_array_equal(a, b)

@@ -87,3 +87,20 @@ def test_checkpoint_stride_does_not_change_the_gradient(cuda, olib):
     from mkfbodytracker_pdaf_gb300._native import MkfError
     with pytest.raises(MkfError):
         g.backward()
+
+
+def test_fit_resumes_from_a_saved_state(cuda, olib, tmp_path):
+    """Four Adam steps in one go equal two steps, a save/load of the fitting
+    state, and two more steps (the kernels are deterministic)."""
+    from mkfbodytracker_pdaf_gb300 import mixkf
+    b, om, th, g = _setup(olib, n_tracks=4, T=16)
+    th0 = th * 1.01
+    full, _ = g.fit_adam(th0, 4, lr=1e-2)
+    full = full.cpu().numpy()
+    g.fit_adam(th0, 2, lr=1e-2)
+    p = str(tmp_path / "fit.bin")
+    mixkf.save_fit_state(p, g.fit_state)
+    st = mixkf.load_fit_state(p)
+    assert st.step == 2 and st.theta.size == th.size
+    resumed, _ = g.fit_adam(None, 2, lr=1e-2, resume=st)
+    np.testing.assert_array_equal(resumed.cpu().numpy(), full)
