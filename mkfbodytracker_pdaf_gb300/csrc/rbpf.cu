@@ -599,9 +599,15 @@ struct BlurArgs {
   int width, height, pitch_in, pitch_out;
   float w[2 * kBlurR + 1];
 };
+// reflect-101 index for any i (n >= 2): fold with period 2n - 2.  The staged
+// tile reaches up to T + R - 1 past its origin, beyond one reflection when the
+// image is narrower than a tile; those positions feed no output pixel, but
+// they must still be addresses inside the image.
 __device__ __forceinline__ int reflect101(int i, int n) {
-  if (i < 0) i = -i;
-  if (i >= n) i = 2 * n - 2 - i;
+  const int p = 2 * n - 2;
+  i %= p;
+  if (i < 0) i += p;
+  if (i >= n) i = p - i;
   return i;
 }
 __global__ void __launch_bounds__(256) blur_kernel(BlurArgs A) {
