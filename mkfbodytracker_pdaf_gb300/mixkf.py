@@ -60,7 +60,7 @@ def load_fit_state(path):
     (n,) = struct.unpack_from("<I", buf, 8)
     hdr = json.loads(buf[12:12 + n].decode())
     k = hdr["n_theta"]
-    arr = np.frombuffer(buf, "<f8", 3 * k, 12 + n).reshape(3, k)
+    arr = np.frombuffer(buf, "<f8", 3 * k, 12 + n).reshape(3, k).copy()
     return FitState(arr[0], arr[1], arr[2], hdr["step"], hdr["lr"], hdr["K"], hdr["d"])
 
 
