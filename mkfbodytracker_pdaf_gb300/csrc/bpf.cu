@@ -718,9 +718,19 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
   __shared__ int s_cnt[MKF_MAX_J];
   __shared__ float s_red[32 * (D + 3)];
   __shared__ bool s_last;
+  __shared__ float s_cum[MKF_MAX_K];
+  __shared__ uint8_t s_ktab[kPickBins];
   const int tid = threadIdx.x, TB = blockDim.x;
   const int J = A.pv.J;
   const LikConst LK = lik_const(A.pv, A.kappa, A.pd, A.sigma);
+  // this block's copy of the cumulative mixture weights and their pick table
+  PView pv = A.pv;
+  for (int q = tid; q < pv.K; q += TB) s_cum[q] = pv.cumpi[q];
+  __syncthreads();
+  build_pick_table(s_cum, pv.K, s_ktab, tid, TB);
+  pv.cumpi = s_cum;
+  pv.ktab = s_ktab;
+  __syncthreads();
   if (!A.prior) {
     if (tid < J) {
       int n = A.det_off[tid + 1] - A.det_off[tid];
@@ -747,7 +757,7 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
     float x[D], eps[D];
     if (A.prior) {
       float uc = particle_draws<D>(A.seed, A.track, kFramePrior, (uint32_t)i, eps);
-      prior_sample<D>(A.pv, eps, uc, x);
+      prior_sample<D>(pv, eps, uc, x);
 #pragma unroll
       for (int r = 0; r < D; ++r) A.xb[(size_t)r * A.N + i] = x[r];
       continue;
@@ -756,10 +766,10 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
 #pragma unroll
     for (int r = 0; r < D; ++r) x[r] = A.xa[(size_t)r * A.N + an];
     float uc = particle_draws<D>(A.seed, A.track, frame, (uint32_t)i, eps);
-    propagate<D, DIAG>(A.pv, eps, uc, x);
+    propagate<D, DIAG>(pv, eps, uc, x);
 #pragma unroll
     for (int r = 0; r < D; ++r) A.xb[(size_t)r * A.N + i] = x[r];
-    float ll = loglik<D>(A.pv, x, s_cnt, s_det, LK);
+    float ll = loglik<D>(pv, x, s_cnt, s_det, LK);
     A.logw[i] = ll;
     // online accumulation
     if (ll > m) {
@@ -830,10 +840,9 @@ __global__ void __launch_bounds__(256) bpf_stream_b(StreamArgs A) {
   const float M = A.fs->M;
   const int fb = A.fs->fb;
   const int base = blockIdx.x * A.tile_b, end = min(A.N, base + A.tile_b);
-  const int E = (A.tile_b + TB - 1) / TB;
-  const int j0 = min(end, base + tid * E), j1 = min(end, j0 + E);
+  // integer sums are order-free: coalesced striped reads
   uint64_t cs = 0;
-  for (int j = j0; j < j1; ++j) {
+  for (int j = base + tid; j < end; j += TB) {
     float w = stream_weight(A.logw[j], M, fb);
     if (A.dbg_w) A.dbg_w[j] = w;
     cs += quantize_f32(w, 1);
@@ -885,15 +894,20 @@ __global__ void __launch_bounds__(256) bpf_stream_c(StreamArgs A, int tile_c) {
     for (int i = base + tid; i < end; i += TB) A.anc_out[i] = resample_fallback_index(U, i, A.N);
     return;
   }
-  const int E = (tile_c + TB - 1) / TB;
-  const int j0 = min(end, base + tid * E), j1 = min(end, j0 + E);
+  // the tile's integer weights, read coalesced, then prefix sums over
+  // contiguous chunks of an odd length (distinct banks across a warp)
+  for (int j = tid; j < n; j += TB) sQ[j] = quantize_f32(stream_weight(A.logw[base + j], M, fb), 1);
+  __syncthreads();
+  int E = (n + TB - 1) / TB;
+  if (E > 1 && !(E & 1)) ++E;
+  const int j0 = min(n, tid * E), j1 = min(n, j0 + E);
   uint64_t cs = 0;
-  for (int j = j0; j < j1; ++j) cs += quantize_f32(stream_weight(A.logw[j], M, fb), 1);
+  for (int j = j0; j < j1; ++j) cs += sQ[j];
   uint64_t tot;
   uint64_t pre = block_excl_scan_u64(cs, s_red64, &tot) + A.bsum[blockIdx.x];
   for (int j = j0; j < j1; ++j) {
-    pre += quantize_f32(stream_weight(A.logw[j], M, fb), 1);
-    sQ[j - base] = pre;
+    pre += sQ[j];
+    sQ[j] = pre;
   }
   if (tid == 0) {
     uint64_t Xprev = A.bsum[blockIdx.x];
@@ -901,8 +915,19 @@ __global__ void __launch_bounds__(256) bpf_stream_c(StreamArgs A, int tile_c) {
     s_hi = (blockIdx.x == gridDim.x - 1) ? A.N : count_targets_le(Xprev + tot, A.N, U, Qt);
   }
   __syncthreads();
-  for (int i = s_lo + tid; i < s_hi; i += TB)
-    A.anc_out[i] = base + resample_search(sQ, n, A.N, resample_rhs(i, U, Qt));
+  // targets of this tile by 64-bit thresholds, four interleaved searches per thread
+  const RsThresh th = rs_thresh_setup(Qt, A.N, U);
+  const int lo = s_lo, hi = s_hi;
+  for (int i0 = lo + tid; i0 < hi; i0 += 4 * TB) {
+    uint64_t T4[4];
+    int r4[4];
+#pragma unroll
+    for (int g = 0; g < 4; ++g) T4[g] = rs_threshold64(th, (uint32_t)min(i0 + g * TB, hi - 1));
+    search_u64_multi<4>(sQ, n, T4, r4);
+#pragma unroll
+    for (int g = 0; g < 4; ++g)
+      if (i0 + g * TB < hi) A.anc_out[i0 + g * TB] = base + r4[g];
+  }
 }
 
 // ------------------------------------------------------------------ handles

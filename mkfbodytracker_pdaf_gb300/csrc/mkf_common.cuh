@@ -206,6 +206,7 @@ __device__ __forceinline__ int resample_fallback_index(uint32_t U, int i, int L)
 struct RsThresh {
   uint64_t A, C;
   uint32_t r, s, N, low;
+  float invN;
 };
 MKF_HD RsThresh rs_thresh_setup(uint64_t Qt, int N, uint32_t U) {
   RsThresh t;
@@ -217,6 +218,7 @@ MKF_HD RsThresh rs_thresh_setup(uint64_t Qt, int N, uint32_t U) {
   t.low = (uint32_t)UQ;
   t.C = UQh / t.N;
   t.s = (uint32_t)(UQh - t.C * t.N);
+  t.invN = 1.0f / (float)N;
   return t;
 }
 MKF_HD uint64_t rs_threshold(const RsThresh& t, uint32_t i) {
@@ -224,6 +226,24 @@ MKF_HD uint64_t rs_threshold(const RsThresh& t, uint32_t i) {
   const uint32_t g = V / t.N, h = V - g * t.N;
   return (uint64_t)i * t.A + t.C + g + (((h | t.low) != 0u) ? 1u : 0u);
 }
+// The same threshold for any N <= 2^22 (V_i < 2^45): floor(V_i / N) from a
+// float estimate (relative error <= 3 2^-24, so within one of the truth) and
+// exact integer correction.
+#ifdef __CUDACC__
+__device__ __forceinline__ uint64_t rs_threshold64(const RsThresh& t, uint32_t i) {
+  const uint64_t V = (uint64_t)i * t.r + t.s;
+  uint32_t g = __float2uint_rz((float)V * t.invN);
+  long long h = (long long)V - (long long)g * (long long)t.N;
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+    if (h < 0) { --g; h += t.N; }
+#pragma unroll
+  for (int k = 0; k < 2; ++k)
+    if (h >= (long long)t.N) { ++g; h -= t.N; }
+  return (uint64_t)i * t.A + t.C + g + (((h != 0) || (t.low != 0u)) ? 1u : 0u);
+}
+#endif
+
 // first j in [0, n) with Q[j] >= T (Q nondecreasing, T <= Q[n-1])
 __device__ __forceinline__ int search_u64(const uint64_t* Q, int n, uint64_t T) {
   int lo = 0, hi = n - 1;
