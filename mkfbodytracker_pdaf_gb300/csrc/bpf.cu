@@ -157,13 +157,15 @@ __device__ __forceinline__ void propagate(const PView& p, const float* eps, floa
   if (DIAG) {
     const float* l = p.Ld + k * D;
     if (VEC) {
+      // x[r] = fmaf(l[r], eps[r], fmaf(a[r], x[r], mb[r])) two dimensions per instruction
 #pragma unroll
       for (int r = 0; r < D; r += 4) {
         float4 av = ld4(a + r), mv = ld4(mb + r), lv = ld4(l + r);
-        x[r + 0] = fmaf(lv.x, eps[r + 0], fmaf(av.x, x[r + 0], mv.x));
-        x[r + 1] = fmaf(lv.y, eps[r + 1], fmaf(av.y, x[r + 1], mv.y));
-        x[r + 2] = fmaf(lv.z, eps[r + 2], fmaf(av.z, x[r + 2], mv.z));
-        x[r + 3] = fmaf(lv.w, eps[r + 3], fmaf(av.w, x[r + 3], mv.w));
+        float2 t0 = pk_fma(make_float2(av.x, av.y), make_float2(x[r], x[r + 1]), make_float2(mv.x, mv.y));
+        float2 t1 = pk_fma(make_float2(av.z, av.w), make_float2(x[r + 2], x[r + 3]), make_float2(mv.z, mv.w));
+        t0 = pk_fma(make_float2(lv.x, lv.y), make_float2(eps[r], eps[r + 1]), t0);
+        t1 = pk_fma(make_float2(lv.z, lv.w), make_float2(eps[r + 2], eps[r + 3]), t1);
+        x[r] = t0.x; x[r + 1] = t0.y; x[r + 2] = t1.x; x[r + 3] = t1.y;
       }
     } else {
 #pragma unroll
@@ -210,30 +212,39 @@ __device__ __forceinline__ float ex2_neg(float s) {   // 2^(-s), MUFU.EX2
   return r;
 }
 
+// Shared-memory detection layout of one joint (2 MKF_MAX_DET floats): pairs of
+// detections as (x_i, x_i+1, y_i, y_i+1), scaled by L.k, so that one 16-byte
+// load gives two detections' x and y as packed pairs.
+__device__ __forceinline__ void stage_det(float* dj, int i, float2 z, float k) {
+  dj[(i >> 1) * 4 + (i & 1)] = z.x * k;
+  dj[(i >> 1) * 4 + 2 + (i & 1)] = z.y * k;
+}
+
 // log[(1-P_D) kappa + P_D sum_i N(z_i; pi(x), sigma^2 I)] summed over measured
-// joints; det holds the detections already scaled by L.k
+// joints; det holds each joint's detections in the stage_det layout
 template <int D, bool VEC = true>
-__device__ __forceinline__ float loglik(const PView& p, const float* x, const int* cnt, const float2* det,
+__device__ __forceinline__ float loglik(const PView& p, const float* x, const int* cnt, const float* det,
                                         const LikConst& L) {
   float ll = 0.0f;
   for (int j = 0; j < p.J; ++j) {
     const float* B = p.Bm + j * 3 * D;
     float q0, q1, q2;
     if (VEC) {
-      // two partial sums per row shorten the dependent FMA chains
-      float q0a = p.mm[j * 3 + 0], q1a = p.mm[j * 3 + 1], q2a = p.mm[j * 3 + 2];
-      float q0b = 0.0f, q1b = 0.0f, q2b = 0.0f;
+      // two partial sums per row (even and odd dimensions), one packed pair
+      float2 p0 = make_float2(p.mm[j * 3 + 0], 0.0f), p1 = make_float2(p.mm[j * 3 + 1], 0.0f);
+      float2 p2 = make_float2(p.mm[j * 3 + 2], 0.0f);
 #pragma unroll
       for (int c = 0; c < D; c += 4) {
         float4 b0 = ld4(B + c), b1 = ld4(B + D + c), b2 = ld4(B + 2 * D + c);
-        q0a = fmaf(b0.x, x[c], q0a); q0b = fmaf(b0.y, x[c + 1], q0b);
-        q1a = fmaf(b1.x, x[c], q1a); q1b = fmaf(b1.y, x[c + 1], q1b);
-        q2a = fmaf(b2.x, x[c], q2a); q2b = fmaf(b2.y, x[c + 1], q2b);
-        q0a = fmaf(b0.z, x[c + 2], q0a); q0b = fmaf(b0.w, x[c + 3], q0b);
-        q1a = fmaf(b1.z, x[c + 2], q1a); q1b = fmaf(b1.w, x[c + 3], q1b);
-        q2a = fmaf(b2.z, x[c + 2], q2a); q2b = fmaf(b2.w, x[c + 3], q2b);
+        const float2 xa = make_float2(x[c], x[c + 1]), xb = make_float2(x[c + 2], x[c + 3]);
+        p0 = pk_fma(make_float2(b0.x, b0.y), xa, p0);
+        p1 = pk_fma(make_float2(b1.x, b1.y), xa, p1);
+        p2 = pk_fma(make_float2(b2.x, b2.y), xa, p2);
+        p0 = pk_fma(make_float2(b0.z, b0.w), xb, p0);
+        p1 = pk_fma(make_float2(b1.z, b1.w), xb, p1);
+        p2 = pk_fma(make_float2(b2.z, b2.w), xb, p2);
       }
-      q0 = q0a + q0b; q1 = q1a + q1b; q2 = q2a + q2b;
+      q0 = p0.x + p0.y; q1 = p1.x + p1.y; q2 = p2.x + p2.y;
     } else {
       q0 = p.mm[j * 3 + 0]; q1 = p.mm[j * 3 + 1]; q2 = p.mm[j * 3 + 2];
 #pragma unroll
@@ -246,28 +257,26 @@ __device__ __forceinline__ float loglik(const PView& p, const float* x, const in
     if (!(q2 > kZMin)) { ll = __fadd_rn(ll, L.log_kappa); continue; }
     const float iz = __fdividef(1.0f, q2);
     const float u = fmaf(L.fxk * q0, iz, L.cxk), v = fmaf(L.fyk * q1, iz, L.cyk);
-    // four independent partial sums so the exponentials of a list overlap
-    float acc0 = 0.0f, acc1 = 0.0f, acc2 = 0.0f, acc3 = 0.0f;
-    const float2* dj = det + j * MKF_MAX_DET;
+    // four partial sums (detection i into sum i mod 4, the remainder into sum 0)
+    // so the exponentials of a list overlap; sums (0, 1) and (2, 3) are packed pairs
+    float2 accA = make_float2(0.0f, 0.0f), accB = make_float2(0.0f, 0.0f);
+    const float* dj = det + j * 2 * MKF_MAX_DET;
+    const float2 uu = make_float2(u, u), vv = make_float2(v, v);
     const int n = cnt[j];
     int i = 0;
     for (; i + 4 <= n; i += 4) {
-      const float4 d01 = *reinterpret_cast<const float4*>(dj + i);
-      const float4 d23 = *reinterpret_cast<const float4*>(dj + i + 2);
-      float dx = d01.x - u, dy = d01.y - v;
-      acc0 += ex2_neg(fmaf(dy, dy, dx * dx));
-      dx = d01.z - u; dy = d01.w - v;
-      acc1 += ex2_neg(fmaf(dy, dy, dx * dx));
-      dx = d23.x - u; dy = d23.y - v;
-      acc2 += ex2_neg(fmaf(dy, dy, dx * dx));
-      dx = d23.z - u; dy = d23.w - v;
-      acc3 += ex2_neg(fmaf(dy, dy, dx * dx));
+      const float4 g0 = ld4(dj + 2 * i), g1 = ld4(dj + 2 * i + 4);
+      const float2 dxA = pk_sub(make_float2(g0.x, g0.y), uu), dyA = pk_sub(make_float2(g0.z, g0.w), vv);
+      const float2 dxB = pk_sub(make_float2(g1.x, g1.y), uu), dyB = pk_sub(make_float2(g1.z, g1.w), vv);
+      const float2 sA = pk_fma(dyA, dyA, pk_mul(dxA, dxA)), sB = pk_fma(dyB, dyB, pk_mul(dxB, dxB));
+      accA = pk_add(accA, make_float2(ex2_neg(sA.x), ex2_neg(sA.y)));
+      accB = pk_add(accB, make_float2(ex2_neg(sB.x), ex2_neg(sB.y)));
     }
     for (; i < n; ++i) {
-      const float dx = dj[i].x - u, dy = dj[i].y - v;
-      acc0 += ex2_neg(fmaf(dy, dy, dx * dx));
+      const float dx = dj[(i >> 1) * 4 + (i & 1)] - u, dy = dj[(i >> 1) * 4 + 2 + (i & 1)] - v;
+      accA.x += ex2_neg(fmaf(dy, dy, dx * dx));
     }
-    const float acc = (acc0 + acc1) + (acc2 + acc3);
+    const float acc = (accA.x + accA.y) + (accB.x + accB.y);
     // __fadd_rn: never merged with the multiply inside __logf, so every kernel
     // that inlines this function rounds the log-likelihood the same way
     ll = __fadd_rn(ll, __logf(fmaf(L.norm, acc, L.floor_)));
@@ -352,8 +361,8 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
   float* s_Bm = s_L + Lsz;
   float* s_mm = s_Bm + J * 3 * D;
   float* s_cum = s_mm + pad4(J * 3);
-  float2* s_det = reinterpret_cast<float2*>(sP + params_floats<D>(K, J, DIAG));
-  int* s_cnt = reinterpret_cast<int*>(s_det + MKF_MAX_J * MKF_MAX_DET);
+  float* s_det = sP + params_floats<D>(K, J, DIAG);
+  int* s_cnt = reinterpret_cast<int*>(s_det + MKF_MAX_J * 2 * MKF_MAX_DET);
   float* s_red = reinterpret_cast<float*>(s_cnt + 8);                    // 32*NV floats
   uint64_t* s_red64 = reinterpret_cast<uint64_t*>(s_red + 32 * NV + 2);
   s_red64 = reinterpret_cast<uint64_t*>((reinterpret_cast<uintptr_t>(s_red64) + 7) & ~uintptr_t(7));
@@ -432,8 +441,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       for (int q = tid; q < J * MKF_MAX_DET; q += TB) {
         int j = q / MKF_MAX_DET, i = q - j * MKF_MAX_DET;
         if (i < s_cnt[j]) {
-          const float2 z = A.det[A.det_off[g * J + j] + i];
-          s_det[j * MKF_MAX_DET + i] = make_float2(z.x * LK.k, z.y * LK.k);
+          stage_det(s_det + j * 2 * MKF_MAX_DET, i, A.det[A.det_off[g * J + j] + i], LK.k);
         }
       }
       __syncthreads();
@@ -447,9 +455,10 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       float lmax = -INFINITY;
       float Lub = 0.0f;
       for (int j = 0; j < J; ++j) Lub += fmaxf(LK.log_kappa, __logf(fmaf(LK.norm, (float)s_cnt[j], LK.floor_)));
-      float fs = 0.0f, fs2 = 0.0f, fv[D];
+      float fs = 0.0f, fs2 = 0.0f;
+      float2 fv[D / 2];
 #pragma unroll
-      for (int r = 0; r < D; ++r) fv[r] = 0.0f;
+      for (int r = 0; r < D / 2; ++r) fv[r] = make_float2(0.0f, 0.0f);
       if (PAIR) {
         // particles i and i + TB of this thread together: two independent
         // dependency chains for the scheduler (same particles, same results)
@@ -489,8 +498,9 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
           const float wl = __expf(ll - Lub);
           fs += wl;
           fs2 = fmaf(wl, wl, fs2);
+          const float2 ww = make_float2(wl, wl);
 #pragma unroll
-          for (int r = 0; r < D; ++r) fv[r] = fmaf(wl, x[r], fv[r]);
+          for (int r = 0; r < D / 2; ++r) fv[r] = pk_fma(ww, make_float2(x[2 * r], x[2 * r + 1]), fv[r]);
         }
       }
       const float M = block_max(lmax, s_red);
@@ -524,7 +534,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
         acc[0] = fs;
         acc[1] = fs2;
 #pragma unroll
-        for (int r = 0; r < D; ++r) acc[3 + r] = fv[r];
+        for (int r = 0; r < D / 2; ++r) { acc[3 + 2 * r] = fv[r].x; acc[4 + 2 * r] = fv[r].y; }
       }
       {
         const int lane = tid & 31, w = tid >> 5, nw = (TB + 31) >> 5;
@@ -714,7 +724,7 @@ __device__ void block_merge(float& m, float& s, float& s2, float* v, float* red)
 
 template <int D, bool DIAG>
 __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
-  __shared__ __align__(16) float2 s_det[MKF_MAX_J * MKF_MAX_DET];
+  __shared__ __align__(16) float s_det[MKF_MAX_J * 2 * MKF_MAX_DET];
   __shared__ int s_cnt[MKF_MAX_J];
   __shared__ float s_red[32 * (D + 3)];
   __shared__ bool s_last;
@@ -741,8 +751,7 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
     for (int q = tid; q < J * MKF_MAX_DET; q += TB) {
       int j = q / MKF_MAX_DET, i = q - j * MKF_MAX_DET;
       if (i < s_cnt[j]) {
-        const float2 z = A.det[A.det_off[j] + i];
-        s_det[j * MKF_MAX_DET + i] = make_float2(z.x * LK.k, z.y * LK.k);
+        stage_det(s_det + j * 2 * MKF_MAX_DET, i, A.det[A.det_off[j] + i], LK.k);
       }
     }
     __syncthreads();

@@ -111,6 +111,35 @@ __device__ __forceinline__ float particle_draws(uint64_t seed, uint32_t track, u
   return (float)lowb * (1.0f / 16777216.0f);
 }
 
+// ---------------------------------------------------------------- packed FP32 pairs
+// Blackwell f32x2 instructions: one issue for two lanes, each lane rounded as
+// the scalar operation would be (so results equal the scalar code's).
+union F2U { float2 f; unsigned long long u; };
+__device__ __forceinline__ float2 pk_fma(float2 a, float2 b, float2 c) {
+  F2U x, y, z, d;
+  x.f = a; y.f = b; z.f = c;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d.u) : "l"(x.u), "l"(y.u), "l"(z.u));
+  return d.f;
+}
+__device__ __forceinline__ float2 pk_add(float2 a, float2 b) {
+  F2U x, y, d;
+  x.f = a; y.f = b;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d.u) : "l"(x.u), "l"(y.u));
+  return d.f;
+}
+__device__ __forceinline__ float2 pk_sub(float2 a, float2 b) {
+  F2U x, y, d;
+  x.f = a; y.f = b;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d.u) : "l"(x.u), "l"(y.u));
+  return d.f;
+}
+__device__ __forceinline__ float2 pk_mul(float2 a, float2 b) {
+  F2U x, y, d;
+  x.f = a; y.f = b;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d.u) : "l"(x.u), "l"(y.u));
+  return d.f;
+}
+
 // ---------------------------------------------------------------- block helpers
 __device__ __forceinline__ float warp_max(float v) {
 #pragma unroll
