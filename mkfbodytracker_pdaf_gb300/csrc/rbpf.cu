@@ -180,6 +180,16 @@ __global__ void __launch_bounds__(128) rbpf_step_kernel(RbpfStepArgs A) {
         }
       }
     }
+    // a non-finite measurement (a caller's fault) gives the particle zero
+    // weight and no update, so that a frame of them resamples by the uniform
+    // fallback instead of turning every state into NaN; flagged MKF_ST_NAN
+    bool finite = true;
+    for (int a = 0; a < mm; ++a) finite = finite && isfinite(sy[a]);
+    if (!finite) {
+      ok = 0;
+      lw = -INFINITY;
+      atomicOr(A.status, MKF_ST_NAN);
+    }
     if (ok) {
       for (int a = 0; a < mm; ++a) {
         double s = sy[a];
@@ -203,7 +213,7 @@ __global__ void __launch_bounds__(128) rbpf_step_kernel(RbpfStepArgs A) {
           for (int c = (a > b ? a : b); c < mm; ++c) s += Li[c * mm + a] * Li[c * mm + b];
           sSi[a * mm + b] = s;
         }
-    } else {
+    } else if (finite) {
       lw = -INFINITY;
       atomicOr(A.status, MKF_ST_NONPD);
     }
