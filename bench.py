@@ -335,7 +335,7 @@ def run_sweep(args):
     peak, peak_kind = load_peaks()
     rows = []
     T = args.sweep_frames
-    for lg in range(12, 23, 2):
+    for lg in (args.sweep_sizes or list(range(12, 23, 2))):
         N = 1 << lg
         batch = synth.config1_batch(N, n_frames=T)
         t = batch.tracks[0]
@@ -595,6 +595,8 @@ def parse_args(argv=None):
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="batched", choices=["batched", "sweep", "plain0", "adjoint", "fit"])
     ap.add_argument("--sweep-frames", type=int, default=200)
+    ap.add_argument("--sweep-sizes", type=int, nargs="*", default=None,
+                    help="log2 particle counts of the sweep (default 12 14 ... 22)")
     ap.add_argument("--adj-tracks", type=int, default=1024)
     ap.add_argument("--adj-frames", type=int, default=1000)
     ap.add_argument("--adj-check-tracks", type=int, default=8)
