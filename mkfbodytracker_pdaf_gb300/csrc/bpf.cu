@@ -518,7 +518,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
         // SEARCH: the integer weight straight into the prefix array; the max
         // weight is exactly 1 (or every weight is 0), so the quantisation
         // exponent is 1
-        if (SEARCH) sQ[i] = quantize_f32(w, 1); else sW[i] = w;
+        if (SEARCH) sQ[i] = quantize39(w); else sW[i] = w;
         if (dbg) A.dbg_w[(size_t)t * N + i] = w;
         acc[2] = fmaxf(acc[2], w);
         if (!fused) {
@@ -854,7 +854,7 @@ __global__ void __launch_bounds__(256) bpf_stream_b(StreamArgs A) {
   for (int j = base + tid; j < end; j += TB) {
     float w = stream_weight(A.logw[j], M, fb);
     if (A.dbg_w) A.dbg_w[j] = w;
-    cs += quantize_f32(w, 1);
+    cs += quantize39(w);
   }
   uint64_t tot;
   block_excl_scan_u64(cs, s_red64, &tot);
@@ -905,7 +905,7 @@ __global__ void __launch_bounds__(256) bpf_stream_c(StreamArgs A, int tile_c) {
   }
   // the tile's integer weights, read coalesced, then prefix sums over
   // contiguous chunks of an odd length (distinct banks across a warp)
-  for (int j = tid; j < n; j += TB) sQ[j] = quantize_f32(stream_weight(A.logw[base + j], M, fb), 1);
+  for (int j = tid; j < n; j += TB) sQ[j] = quantize39(stream_weight(A.logw[base + j], M, fb));
   __syncthreads();
   int E = (n + TB - 1) / TB;
   if (E > 1 && !(E & 1)) ++E;

@@ -204,6 +204,16 @@ constexpr int kQBits = 40;
 __device__ __forceinline__ uint64_t quantize_f32(float w, int e) {
   return (w > 0.0f) ? (uint64_t)__float2ull_rz(ldexpf(w, kQBits - e)) : 0ull;
 }
+// quantize_f32(w, 1) for a weight normalised to max 1, without the 64-bit
+// conversion (which runs on GB300's small FP64 pipe): floor(w 2^39) from the
+// float's fields with integer shifts; 0 for zero, negative, NaN and subnormal w
+__device__ __forceinline__ uint64_t quantize39(float w) {
+  const uint32_t b = __float_as_uint(w);
+  const int e = (int)(b >> 23) - 111;
+  const uint64_t m = (uint64_t)((b & 0x7FFFFFu) | 0x800000u);
+  const uint64_t q = e >= 0 ? (m << e) : (e > -24 ? (m >> -e) : 0ull);
+  return (w > 0.0f) ? q : 0ull;
+}
 __device__ __forceinline__ uint64_t quantize_f64(double w, int e) {
   return (w > 0.0) ? (uint64_t)__double2ull_rz(ldexp(w, kQBits - e)) : 0ull;
 }
@@ -256,12 +266,14 @@ MKF_HD uint64_t rs_threshold(const RsThresh& t, uint32_t i) {
   return (uint64_t)i * t.A + t.C + g + (((h | t.low) != 0u) ? 1u : 0u);
 }
 // The same threshold for any N <= 2^22 (V_i < 2^45): floor(V_i / N) from a
-// float estimate (relative error <= 3 2^-24, so within one of the truth) and
+// float estimate (relative error <= 4 2^-24, so within one of the truth) and
 // exact integer correction.
 #ifdef __CUDACC__
 __device__ __forceinline__ uint64_t rs_threshold64(const RsThresh& t, uint32_t i) {
   const uint64_t V = (uint64_t)i * t.r + t.s;
-  uint32_t g = __float2uint_rz((float)V * t.invN);
+  // float(V) from two 32-bit conversions (V < 2^45); the 64-bit one runs on the FP64 pipe
+  const float vf = fmaf((float)(uint32_t)(V >> 20), 1048576.0f, (float)(uint32_t)(V & 0xFFFFFu));
+  uint32_t g = __float2uint_rz(vf * t.invN);
   long long h = (long long)V - (long long)g * (long long)t.N;
 #pragma unroll
   for (int k = 0; k < 2; ++k)
