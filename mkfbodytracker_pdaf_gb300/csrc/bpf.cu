@@ -767,17 +767,14 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
     if (A.prior) {
       float uc = particle_draws<D>(A.seed, A.track, kFramePrior, (uint32_t)i, eps);
       prior_sample<D>(pv, eps, uc, x);
-#pragma unroll
-      for (int r = 0; r < D; ++r) A.xb[(size_t)r * A.N + i] = x[r];
+      store_state<D>(A.xb, A.N, i, x);
       continue;
     }
     const int an = A.anc[i];
-#pragma unroll
-    for (int r = 0; r < D; ++r) x[r] = A.xa[(size_t)r * A.N + an];
+    load_state<D>(A.xa, A.N, an, x);
     float uc = particle_draws<D>(A.seed, A.track, frame, (uint32_t)i, eps);
     propagate<D, DIAG>(pv, eps, uc, x);
-#pragma unroll
-    for (int r = 0; r < D; ++r) A.xb[(size_t)r * A.N + i] = x[r];
+    store_state<D>(A.xb, A.N, i, x);
     float ll = loglik<D>(pv, x, s_cnt, s_det, LK);
     A.logw[i] = ll;
     // online accumulation
@@ -1198,13 +1195,24 @@ extern "C" int mkf_bpf_graph_destroy(mkf_bpf_graph_t g) {
   return MKF_OK;
 }
 
+// particle i's dimension r lives at plane r / 4, lane r % 4 of the state buffer
+__global__ void soa_from_planes_kernel(const float* planes, int N, int d, float* soa) {
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < (size_t)N * d; q += (size_t)gridDim.x * blockDim.x) {
+    const int r = (int)(q / N), i = (int)(q - (size_t)r * N);
+    soa[q] = planes[((size_t)(r >> 2) * N + i) * 4 + (r & 3)];
+  }
+}
+
 extern "C" int mkf_bpf_read_debug(mkf_bpf_t H, float* d_x, float* d_logw, float* d_w, int* d_anc,
                                   mkf_stream_t stream) {
   MKF_ARG(H, "mkf_bpf_read_debug: null handle");
   BpfHandle& h = H->h;
   cudaStream_t s = (cudaStream_t)stream;
   const size_t N = h.N;
-  if (d_x) MKF_CUDA(cudaMemcpyAsync(d_x, h.xa, N * h.d * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  if (d_x) {   // float4 planes -> the documented SoA (d, N)
+    soa_from_planes_kernel<<<(int)std::min<size_t>((N * h.d + 255) / 256, 65535), 256, 0, s>>>(h.xa, h.N, h.d, d_x);
+    MKF_CHECK_LAUNCH("mkf_bpf_read_debug: layout");
+  }
   if (d_logw) MKF_CUDA(cudaMemcpyAsync(d_logw, h.logw, N * sizeof(float), cudaMemcpyDeviceToDevice, s));
   if (d_w) MKF_CUDA(cudaMemcpyAsync(d_w, h.w, N * sizeof(float), cudaMemcpyDeviceToDevice, s));
   if (d_anc) MKF_CUDA(cudaMemcpyAsync(d_anc, h.anc, N * sizeof(int), cudaMemcpyDeviceToDevice, s));
