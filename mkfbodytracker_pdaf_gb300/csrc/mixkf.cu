@@ -672,8 +672,19 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
           if (lane < d) xb[lane] = Dkb[lane] + wk * s.xt[lane];
           for (int i = lane; i < d * d; i += 32) Pb[i] = wk * s.Pcb[i];
           __syncwarp();
-          for (int j = J - 1; j >= 0; --j)
-            joint_bwd<D>(M, cb + j * rec_size(d), Bm + j * 3 * d, pd, kappa, xb, Pb, lb, wb + WL.tmp, sbl, lane);
+          // each joint's record is copied (coalesced, 16 bytes per lane and step)
+          // into this warp's forward scratch, idle during the reverse sweep, so
+          // that the reverse reads it from shared memory instead of L2
+          float* Rs = scr + (size_t)k * SR;
+          const int RS4 = rec_size(d) / 4;
+          for (int j = J - 1; j >= 0; --j) {
+            const float4* src = reinterpret_cast<const float4*>(cb + j * rec_size(d));
+            float4* dst = reinterpret_cast<float4*>(Rs);
+            for (int q = lane; q < RS4; q += 32) dst[q] = src[q];
+            __syncwarp();
+            joint_bwd<D>(M, Rs, Bm + j * 3 * d, pd, kappa, xb, Pb, lb, wb + WL.tmp, sbl, lane);
+            __syncwarp();
+          }
           // predict reverse: x = a*xin + (1-a)*mu ; P = A Pin A + Q
           float* gmu = wb + WL.gmu;
           float* ga = wb + WL.ga;
@@ -885,6 +896,8 @@ static int mix_occ(KF kern, int tpb, size_t smem, int* occ) {
 // shared-memory sizes, STAGE choice and the persistent grid
 static int mix_grid(mkf_mixkf* h) {
   const int d = h->d, K = h->K;
+  // the reverse sweep stages one joint record in a warp's forward scratch
+  if (rec_size(d) > fwd_scratch_floats(d)) { set_error("mkf_mixkf: record larger than the warp scratch"); return MKF_ERR_ARG; }
   const FrameLayout FL = frame_layout(d, K, h->J);
   const WorkLayout WL = work_layout(d);
   const size_t base = mix_smem_bytes(d);
