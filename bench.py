@@ -312,6 +312,12 @@ def run_gb300(args):
                                   "batched_over_plain": value / ws / pr}
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(batch, args.cpu_sample_tracks, os.cpu_count() or 1)
+        if not args.no_adjoint:
+            # the metric's "+adjoint" half: config 3's gradient through the mixture KF
+            a = adjoint_result(args)
+            line["adjoint"] = {k: a[k] for k in ("workload", "forward_ms", "backward_ms", "backward_over_forward",
+                                                 "gradient_evals_per_s", "checkpoint_stride", "fd_directions",
+                                                 "grad_rel_err_vs_fd", "grad_rel_err_vs_cpu_adjoint")}
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.barrier()
@@ -442,6 +448,10 @@ def run_plain0(args):
 
 
 def run_adjoint(args):
+    print(json.dumps(adjoint_result(args)), flush=True)
+
+
+def adjoint_result(args):
     """Config 3: mixture-KF logL over B=1024 x T=1000, K=15, d=12; forward and
     backward times, backward/forward ratio, and gradient accuracy against the
     FP64 CPU adjoint and FP64 central differences on a track subset."""
@@ -499,7 +509,7 @@ def run_adjoint(args):
     L_sub_gpu = float(gs.ll.sum().item())
     tf = float(np.median(fwd))
     tb = float(np.median(bwd))
-    print(json.dumps({
+    return {
         "workload": "config 3: mixture-KF logL, B=%d x T=%d, K=15, d=12, PDAF <=16 candidates, FP32 + FP64 sums"
                     % (b.n_tracks, args.adj_frames),
         "forward_ms": tf, "backward_ms": tb, "backward_over_forward": tb / tf,
@@ -511,7 +521,7 @@ def run_adjoint(args):
         "grad_rel_err_vs_fd": {"median": float(np.median(rel_fd)), "max": float(np.max(rel_fd))},
         "grad_rel_err_vs_cpu_adjoint": {"median": float(np.median(rel_adj)), "max": float(np.max(rel_adj))},
         "cpu_adjoint_rel_err_vs_fd": {"median": float(np.median(rel_cpu_fd)), "max": float(np.max(rel_cpu_fd))},
-        "cpu_adjoint_s_subset": cpu_adj_s}), flush=True)
+        "cpu_adjoint_s_subset": cpu_adj_s}
 
 
 def run_fit(args):
@@ -593,6 +603,7 @@ def parse_args(argv=None):
     ap.add_argument("--plain-frames", type=int, default=300)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the config-3 adjoint summary of the default run")
     ap.add_argument("--workload", default="batched", choices=["batched", "sweep", "plain0", "adjoint", "fit"])
     ap.add_argument("--sweep-frames", type=int, default=200)
     ap.add_argument("--sweep-sizes", type=int, nargs="*", default=None,
@@ -600,7 +611,7 @@ def parse_args(argv=None):
     ap.add_argument("--adj-tracks", type=int, default=1024)
     ap.add_argument("--adj-frames", type=int, default=1000)
     ap.add_argument("--adj-check-tracks", type=int, default=8)
-    ap.add_argument("--fd-dirs", type=int, default=64)
+    ap.add_argument("--fd-dirs", type=int, default=16)
     ap.add_argument("--fit-tracks", type=int, default=16384)
     ap.add_argument("--fit-frames", type=int, default=500)
     ap.add_argument("--fit-steps", type=int, default=200)
