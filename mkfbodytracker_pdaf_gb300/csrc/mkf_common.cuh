@@ -82,35 +82,6 @@ MKF_HD uint32_t resample_uniform(uint64_t seed, uint32_t track, uint32_t frame) 
 }
 
 #ifdef __CUDACC__
-// Box-Muller pair from two words (top 24 bits): u1 in (0,1], u2 in [0,1).
-// MUFU intrinsics: the CPU oracle consumes these values dumped by
-// mkf_draw_particles, so libm-vs-device rounding never enters parity.
-__device__ __forceinline__ void box_muller(uint32_t w0, uint32_t w1, float& z0, float& z1) {
-  float u1 = (float)((w0 >> 8) + 1u) * (1.0f / 16777216.0f);
-  float u2 = (float)(w1 >> 8) * (1.0f / 16777216.0f);
-  const float y = -2.0f * __logf(u1);                 // >= 0; y * rsqrt(y) is the MUFU square root
-  float r = y * rsqrtf(fmaxf(y, 1e-30f));
-  float s, c;
-  __sincosf(3.14159265358979f * (2.0f * u2 - 1.0f), &s, &c);
-  z0 = r * c;
-  z1 = r * s;
-}
-
-// All draws of one particle-frame.
-template <int D>
-__device__ __forceinline__ float particle_draws(uint64_t seed, uint32_t track, uint32_t frame,
-                                                uint32_t item, float* eps) {
-  uint32_t lowb = 0;
-#pragma unroll
-  for (int b = 0; b < (D + 3) / 4; ++b) {
-    u32x4 w = draw_block(seed, track, frame, item, (uint32_t)b);
-    if (b == 0) lowb = (w.x & 0xFFu) | ((w.y & 0xFFu) << 8) | ((w.z & 0xFFu) << 16);
-    if (4 * b + 1 < D) box_muller(w.x, w.y, eps[4 * b], eps[4 * b + 1]);
-    if (4 * b + 3 < D) box_muller(w.z, w.w, eps[4 * b + 2], eps[4 * b + 3]);
-  }
-  return (float)lowb * (1.0f / 16777216.0f);
-}
-
 // ---------------------------------------------------------------- packed FP32 pairs
 // Blackwell f32x2 instructions: one issue for two lanes, each lane rounded as
 // the scalar operation would be (so results equal the scalar code's).
@@ -138,6 +109,62 @@ __device__ __forceinline__ float2 pk_mul(float2 a, float2 b) {
   x.f = a; y.f = b;
   asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d.u) : "l"(x.u), "l"(y.u));
   return d.f;
+}
+
+// Box-Muller pair from two words (top 24 bits): u1 in (0,1], u2 in [0,1).
+// MUFU intrinsics: the CPU oracle consumes these values dumped by
+// mkf_draw_particles, so libm-vs-device rounding never enters parity.
+__device__ __forceinline__ void box_muller(uint32_t w0, uint32_t w1, float& z0, float& z1) {
+  float u1 = (float)((w0 >> 8) + 1u) * (1.0f / 16777216.0f);
+  float u2 = (float)(w1 >> 8) * (1.0f / 16777216.0f);
+  const float y = -2.0f * __logf(u1);                 // >= 0; y * rsqrt(y) is the MUFU square root
+  float r = y * rsqrtf(fmaxf(y, 1e-30f));
+  float s, c;
+  __sincosf(3.14159265358979f * (2.0f * u2 - 1.0f), &s, &c);
+  z0 = r * c;
+  z1 = r * s;
+}
+
+__device__ __forceinline__ float lg2_approx(float x) {
+  float r;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// Both Box-Muller pairs of one Philox block, (w.x, w.y) -> z[0], z[1] and
+// (w.z, w.w) -> z[2], z[3], with the two pairs' arithmetic in packed f32x2
+// instructions: r = sqrt(-2 ln u1) with -2 ln u1 = lg2(u1) (-2 ln 2), angle
+// pi (2 u2 - 1) as fma(2 pi, u2, -pi) (the same single rounding), z = r (cos, sin).
+__device__ __forceinline__ void box_muller2(u32x4 w, float* z) {
+  const float2 s24 = make_float2(1.0f / 16777216.0f, 1.0f / 16777216.0f);
+  const float2 u1 = pk_mul(make_float2((float)((w.x >> 8) + 1u), (float)((w.z >> 8) + 1u)), s24);
+  const float2 u2 = pk_mul(make_float2((float)(w.y >> 8), (float)(w.w >> 8)), s24);
+  const float2 y = pk_mul(make_float2(lg2_approx(u1.x), lg2_approx(u1.y)),
+                          make_float2(-1.3862943611198906f, -1.3862943611198906f));
+  const float2 r = pk_mul(y, make_float2(rsqrtf(fmaxf(y.x, 1e-30f)), rsqrtf(fmaxf(y.y, 1e-30f))));
+  const float2 ang = pk_fma(make_float2(6.283185307179586f, 6.283185307179586f), u2,
+                            make_float2(-3.14159265358979f, -3.14159265358979f));
+  float s0, c0, s1, c1;
+  __sincosf(ang.x, &s0, &c0);
+  __sincosf(ang.y, &s1, &c1);
+  const float2 z01 = pk_mul(make_float2(r.x, r.x), make_float2(c0, s0));
+  const float2 z23 = pk_mul(make_float2(r.y, r.y), make_float2(c1, s1));
+  z[0] = z01.x; z[1] = z01.y; z[2] = z23.x; z[3] = z23.y;
+}
+
+// All draws of one particle-frame.
+template <int D>
+__device__ __forceinline__ float particle_draws(uint64_t seed, uint32_t track, uint32_t frame,
+                                                uint32_t item, float* eps) {
+  static_assert(D % 4 == 0, "particle_draws: D must be a multiple of 4");
+  uint32_t lowb = 0;
+#pragma unroll
+  for (int b = 0; b < D / 4; ++b) {
+    u32x4 w = draw_block(seed, track, frame, item, (uint32_t)b);
+    if (b == 0) lowb = (w.x & 0xFFu) | ((w.y & 0xFFu) << 8) | ((w.z & 0xFFu) << 16);
+    box_muller2(w, eps + 4 * b);
+  }
+  return (float)lowb * (1.0f / 16777216.0f);
 }
 
 // ---------------------------------------------------------------- block helpers
