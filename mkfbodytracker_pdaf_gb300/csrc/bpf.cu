@@ -507,27 +507,49 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       const bool fb = !(M > -INFINITY) || !(M < INFINITY);
       const bool fused = !PAIR && (M - Lub >= -60.0f);
 
-      // ---- weights normalised to the max, weighted-mean estimate, ESS
+      // ---- weights normalised to the max, weighted-mean estimate, ESS.
+      // SEARCH: each thread weights its own contiguous chunk and writes the
+      // integer weights straight into the prefix array (the max weight is
+      // exactly 1, or every weight is 0, so the quantisation exponent is 1);
+      // one combined pass then reduces the estimate sums and scans the chunk sums.
       float acc[NV];
 #pragma unroll
       for (int c = 0; c < NV; ++c) acc[c] = 0.0f;   // s, s2, wmax, v[D]
-      for (int i = tid; i < N; i += TB) {
-        float ll = SEARCH ? __int_as_float(sA[i]) : sW[i];
-        float w = fb ? 0.0f : (ll == M ? 1.0f : __expf(ll - M));
-        if (!(w >= 0.0f)) w = 0.0f;
-        // SEARCH: the integer weight straight into the prefix array; the max
-        // weight is exactly 1 (or every weight is 0), so the quantisation
-        // exponent is 1
-        if (SEARCH) sQ[i] = quantize39(w); else sW[i] = w;
-        if (dbg) A.dbg_w[(size_t)t * N + i] = w;
-        acc[2] = fmaxf(acc[2], w);
-        if (!fused) {
-          acc[0] += w;
-          acc[1] = fmaf(w, w, acc[1]);
-          float xi[D];
-          load_state<D>(xb, Nmax, i, xi);
+      uint64_t cs = 0;
+      if (SEARCH) {
+        for (int j = j0; j < j1; ++j) {
+          const float ll = __int_as_float(sA[j]);
+          float w = fb ? 0.0f : (ll == M ? 1.0f : __expf(ll - M));
+          if (!(w >= 0.0f)) w = 0.0f;
+          const uint64_t q = quantize39(w);
+          sQ[j] = q;
+          cs += q;
+          if (dbg) A.dbg_w[(size_t)t * N + j] = w;
+          if (!fused) {
+            acc[0] += w;
+            acc[1] = fmaf(w, w, acc[1]);
+            float xi[D];
+            load_state<D>(xb, Nmax, j, xi);
 #pragma unroll
-          for (int r = 0; r < D; ++r) acc[3 + r] = fmaf(w, xi[r], acc[3 + r]);
+            for (int r = 0; r < D; ++r) acc[3 + r] = fmaf(w, xi[r], acc[3 + r]);
+          }
+        }
+      } else {
+        for (int i = tid; i < N; i += TB) {
+          const float ll = sW[i];
+          float w = fb ? 0.0f : (ll == M ? 1.0f : __expf(ll - M));
+          if (!(w >= 0.0f)) w = 0.0f;
+          sW[i] = w;
+          if (dbg) A.dbg_w[(size_t)t * N + i] = w;
+          acc[2] = fmaxf(acc[2], w);
+          if (!fused) {
+            acc[0] += w;
+            acc[1] = fmaf(w, w, acc[1]);
+            float xi[D];
+            load_state<D>(xb, Nmax, i, xi);
+#pragma unroll
+            for (int r = 0; r < D; ++r) acc[3 + r] = fmaf(w, xi[r], acc[3 + r]);
+          }
         }
       }
       if (fused) {
@@ -536,21 +558,37 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
 #pragma unroll
         for (int r = 0; r < D / 2; ++r) { acc[3 + 2 * r] = fv[r].x; acc[4 + 2 * r] = fv[r].y; }
       }
+      uint64_t P = 0, Qt = 0;
       {
         const int lane = tid & 31, w = tid >> 5, nw = (TB + 31) >> 5;
 #pragma unroll
         for (int c = 0; c < NV; ++c) acc[c] = (c == 2) ? warp_max(acc[c]) : warp_sum(acc[c]);
+        const uint64_t inc = SEARCH ? warp_incl_scan_u64(cs, lane) : 0ull;
         __syncthreads();
         if (lane == 0)
 #pragma unroll
           for (int c = 0; c < NV; ++c) s_red[w * NV + c] = acc[c];
+        if (SEARCH && lane == 31) s_red64[w] = inc;
         __syncthreads();
-        if (tid < NV) {   // thread c alone reads column c, then stores its total in slot c
-          float r = 0.0f;
-          for (int q = 0; q < nw; ++q) r = (tid == 2) ? fmaxf(r, s_red[q * NV + tid]) : r + s_red[q * NV + tid];
-          s_red[tid] = r;
+        if (tid < 32) {
+          if (SEARCH) {   // warp 0: exclusive scan of the warps' chunk totals
+            const uint64_t v = lane < nw ? s_red64[lane] : 0ull;
+            const uint64_t vi = warp_incl_scan_u64(v, lane);
+            __syncwarp();
+            if (lane < nw) s_red64[lane] = vi - v;
+            if (lane == 31) s_red64[32] = vi;
+          }
+          if (tid < NV) {   // thread c alone reads column c, then stores its total in slot c
+            float r = 0.0f;
+            for (int q = 0; q < nw; ++q) r = (tid == 2) ? fmaxf(r, s_red[q * NV + tid]) : r + s_red[q * NV + tid];
+            s_red[tid] = r;
+          }
         }
         __syncthreads();
+        if (SEARCH) {
+          P = s_red64[w] + inc - cs;
+          Qt = s_red64[32];
+        }
       }
       const float S = s_red[0], S2 = s_red[1], Wmax = s_red[2];
       if (tid < D) A.est[(size_t)g * D + tid] = s_red[3 + tid] / S;
@@ -559,15 +597,10 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
         A.ess[g] = S * S / S2;
         if (fb) s_flag |= MKF_ST_FALLBACK | MKF_ST_NAN;
       }
-      int e = 0;
-      frexpf(Wmax, &e);
 
-      // ---- exact systematic resampling: chunk sums and block scan, then either
-      // a binary search per target (SEARCH) or a scatter walk per chunk
-      uint64_t cs = 0;
-      for (int j = j0; j < j1; ++j) cs += SEARCH ? sQ[j] : quantize_f32(sW[j], e);
-      uint64_t Qt;
-      uint64_t P = block_excl_scan_u64(cs, s_red64, &Qt);   // includes barriers
+      // ---- exact systematic resampling: SEARCH: chunk prefix sums in place,
+      // then a binary search per target; otherwise chunk sums, block scan and
+      // a scatter walk per chunk
       const uint32_t U = resample_uniform(seed, trk, (uint32_t)t);
       if (SEARCH) {
         uint64_t pre = P;
@@ -592,15 +625,21 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
               if (i0 + g * TB < N) sA[i0 + g * TB] = r4[g];
           }
         }
-      } else if (fb || Qt == 0) {
-        for (int i = tid; i < N; i += TB) sA[i] = resample_fallback_index(U, i, N);
-      } else if (j0 < j1) {
-        int i = (j0 == 0) ? 0 : count_targets_le(P, N, U, Qt);
-        uint64_t Qj = P;
-        for (int j = j0; j < j1; ++j) {
-          Qj += quantize_f32(sW[j], e);
-          const unsigned __int128 lim = ((unsigned __int128)(uint64_t)N * (unsigned __int128)Qj) << 32;
-          while (i < N && resample_rhs(i, U, Qt) <= lim) sA[i++] = j;
+      } else {
+        int e = 0;
+        frexpf(Wmax, &e);
+        for (int j = j0; j < j1; ++j) cs += quantize_f32(sW[j], e);
+        P = block_excl_scan_u64(cs, s_red64, &Qt);   // includes barriers
+        if (fb || Qt == 0) {
+          for (int i = tid; i < N; i += TB) sA[i] = resample_fallback_index(U, i, N);
+        } else if (j0 < j1) {
+          int i = (j0 == 0) ? 0 : count_targets_le(P, N, U, Qt);
+          uint64_t Qj = P;
+          for (int j = j0; j < j1; ++j) {
+            Qj += quantize_f32(sW[j], e);
+            const unsigned __int128 lim = ((unsigned __int128)(uint64_t)N * (unsigned __int128)Qj) << 32;
+            while (i < N && resample_rhs(i, U, Qt) <= lim) sA[i++] = j;
+          }
         }
       }
       __syncthreads();
