@@ -431,18 +431,16 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
     const int j0 = min(N, tid * E), j1 = min(N, j0 + E);
     for (int t = 0; t < T; ++t) {
       const long long g = g0 + t;
-      if (tid < J) {
-        int lo = A.det_off[g * J + tid], hi = A.det_off[g * J + tid + 1];
-        int n = hi - lo;
-        if (n > MKF_MAX_DET) { n = MKF_MAX_DET; atomicOr(&s_flag, MKF_ST_TRUNC); }
-        s_cnt[tid] = n < 0 ? 0 : n;
-      }
-      __syncthreads();
+      // this frame's detection lists (each staging thread reads its list's
+      // bounds itself, so one barrier suffices)
       for (int q = tid; q < J * MKF_MAX_DET; q += TB) {
-        int j = q / MKF_MAX_DET, i = q - j * MKF_MAX_DET;
-        if (i < s_cnt[j]) {
-          stage_det(s_det + j * 2 * MKF_MAX_DET, i, A.det[A.det_off[g * J + j] + i], LK.k);
+        const int j = q / MKF_MAX_DET, i = q - j * MKF_MAX_DET;
+        const int lo = A.det_off[g * J + j], n = A.det_off[g * J + j + 1] - lo;
+        if (i == 0) {
+          if (n > MKF_MAX_DET) atomicOr(&s_flag, MKF_ST_TRUNC);
+          s_cnt[j] = min(max(n, 0), MKF_MAX_DET);
         }
+        if (i < n) stage_det(s_det + j * 2 * MKF_MAX_DET, i, A.det[lo + i], LK.k);
       }
       __syncthreads();
 
@@ -781,17 +779,14 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
   pv.ktab = s_ktab;
   __syncthreads();
   if (!A.prior) {
-    if (tid < J) {
-      int n = A.det_off[tid + 1] - A.det_off[tid];
-      if (n > MKF_MAX_DET) { n = MKF_MAX_DET; if (blockIdx.x == 0) atomicOr(&A.fs->status, MKF_ST_TRUNC); }
-      s_cnt[tid] = n < 0 ? 0 : n;
-    }
-    __syncthreads();
     for (int q = tid; q < J * MKF_MAX_DET; q += TB) {
-      int j = q / MKF_MAX_DET, i = q - j * MKF_MAX_DET;
-      if (i < s_cnt[j]) {
-        stage_det(s_det + j * 2 * MKF_MAX_DET, i, A.det[A.det_off[j] + i], LK.k);
+      const int j = q / MKF_MAX_DET, i = q - j * MKF_MAX_DET;
+      const int lo = A.det_off[j], n = A.det_off[j + 1] - lo;
+      if (i == 0) {
+        if (n > MKF_MAX_DET && blockIdx.x == 0) atomicOr(&A.fs->status, MKF_ST_TRUNC);
+        s_cnt[j] = min(max(n, 0), MKF_MAX_DET);
       }
+      if (i < n) stage_det(s_det + j * 2 * MKF_MAX_DET, i, A.det[lo + i], LK.k);
     }
     __syncthreads();
   }
