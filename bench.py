@@ -36,9 +36,9 @@ UNIT = "track-frames/s"
 BYTES_PER_PF = 112          # algorithmic bytes per particle-frame (state in/out 4d+4d, logw 8, anc 8)
 # DRAM bytes per particle-frame of bpf_batched_kernel: dram__bytes_read.sum +
 # dram__bytes_write.sum of one ncu capture on 2048 tracks of the same workload
-# (210.1 GB over 4.148e9 particle-frames), scaled to a full launch by
+# (210.7 GB over 4.148e9 particle-frames), scaled to a full launch by
 # particle-frames (profiles/bpf_batched_kernel_config2.md)
-TRAFFIC_BYTES_PER_PF = 50.65
+TRAFFIC_BYTES_PER_PF = 50.8
 
 
 def load_peaks():
