@@ -37,7 +37,7 @@ BYTES_PER_PF = 112          # algorithmic bytes per particle-frame (state in/out
 # DRAM bytes per particle-frame of bpf_batched_kernel: dram__bytes_read.sum +
 # dram__bytes_write.sum of one ncu capture on 2048 tracks of the same workload
 # (210.7 GB over 4.148e9 particle-frames), scaled to a full launch by
-# particle-frames (profiles/bpf_batched_kernel_config2.md)
+# particle-frames (profiles/bpf_batched_kernel_uneven_tracks_B8192.md)
 TRAFFIC_BYTES_PER_PF = 50.8
 
 
@@ -108,7 +108,7 @@ def dist_env():
 def workload(rank, n_tracks):
     from mkfbodytracker_pdaf_gb300 import synth
     from mkfbodytracker_pdaf_gb300.replicas import rank_seed
-    return synth.config2_batch(n_tracks=n_tracks, seed=rank_seed(synth.MASTER_SEED + 2, rank))
+    return synth.uneven_tracks_batch(n_tracks=n_tracks, seed=rank_seed(synth.MASTER_SEED + 2, rank))
 
 
 def pf_count(batch, ids=None):
@@ -313,7 +313,7 @@ def run_gb300(args):
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(batch, args.cpu_sample_tracks, os.cpu_count() or 1)
         if not args.no_adjoint:
-            # the metric's "+adjoint" half: config 3's gradient through the mixture KF
+            # the metric's "+adjoint" half: the mixture-KF gradient (B=1024, T=1000)
             a = adjoint_result(args)
             line["adjoint"] = {k: a[k] for k in ("workload", "forward_ms", "backward_ms", "backward_over_forward",
                                                  "gradient_evals_per_s", "checkpoint_stride", "fd_directions",
@@ -330,7 +330,7 @@ def _events(torch):
 
 
 def run_sweep(args):
-    """Particle-count sweep (config 1): one track, T=200, N = 2^12 .. 2^22,
+    """Particle-count sweep: one track, T=200, N = 2^12 .. 2^22,
     through the plain per-track C-ABI path (three grid-wide kernels per frame).
     Reports particle-frames/s and the HBM roofline fraction at 112 B per
     particle-frame."""
@@ -343,7 +343,7 @@ def run_sweep(args):
     T = args.sweep_frames
     for lg in (args.sweep_sizes or list(range(12, 23, 2))):
         N = 1 << lg
-        batch = synth.config1_batch(N, n_frames=T)
+        batch = synth.sweep_batch(N, n_frames=T)
         t = batch.tracks[0]
         J = batch.model["J"]
         lo = batch.det_off.astype(np.int64)
@@ -390,7 +390,7 @@ def run_sweep(args):
 
 
 def run_plain0(args):
-    """Config 0: two arms, K=15, d=12, N=1000 particles per arm, T=500, FP64
+    """Two-arm pose tracking: two arms, K=15, d=12, N=1000 particles per arm, T=500, FP64
     Rao-Blackwellised filters + PDAF association through PoseTracker, against
     the CPU restatement of the reference frame loop."""
     import torch
@@ -440,7 +440,7 @@ def run_plain0(args):
     ok = ~skipped
     rel = float(np.abs(est[:, ok] - est_c[:, ok]).max() / np.abs(est_c[:, ok]).max())
     err = float(np.abs(est_c[:, ok] - sc.truth[:, ok]).mean())
-    print(json.dumps({"workload": "config 0: 2 arms x T=%d, N=%d, K=15, d=12, FP64 RBPF + PDAF" % (T, N),
+    print(json.dumps({"workload": "two-arm pose tracking: 2 arms x T=%d, N=%d, K=15, d=12, FP64 RBPF + PDAF" % (T, N),
                       "gpu_track_frames_per_s": 2 * T / gpu_s, "gpu_s": gpu_s,
                       "cpu_track_frames_per_s": 2 * T / cpu_s, "cpu_s": cpu_s, "cpu_threads": 1,
                       "max_rel_est_err_vs_cpu": rel, "mean_abs_latent_err_vs_truth": err,
@@ -452,7 +452,7 @@ def run_adjoint(args):
 
 
 def adjoint_result(args):
-    """Config 3: mixture-KF logL over B=1024 x T=1000, K=15, d=12; forward and
+    """Mixture-KF logL over B=1024 x T=1000, K=15, d=12; forward and
     backward times, backward/forward ratio, and gradient accuracy against the
     FP64 CPU adjoint and FP64 central differences on a track subset."""
     import torch
@@ -460,7 +460,7 @@ def adjoint_result(args):
     from mkfbodytracker_pdaf_gb300 import build, mixkf, synth
     build.build()
     oracle.build()
-    b = synth.config3_batch(n_tracks=args.adj_tracks, T=args.adj_frames)
+    b = synth.mixkf_batch_k15(n_tracks=args.adj_tracks, T=args.adj_frames)
     tt = b.theta_true()
     om = oracle.MixModel(tt["mu"], tt["a"], tt["Lq"], tt["sigma"], tt["pi"], tt["S0"])
     th = om.theta()
@@ -510,7 +510,7 @@ def adjoint_result(args):
     tf = float(np.median(fwd))
     tb = float(np.median(bwd))
     return {
-        "workload": "config 3: mixture-KF logL, B=%d x T=%d, K=15, d=12, PDAF <=16 candidates, FP32 + FP64 sums"
+        "workload": "mixture-KF logL and adjoint, B=%d x T=%d, K=15, d=12, PDAF <=16 candidates, FP32 + FP64 sums"
                     % (b.n_tracks, args.adj_frames),
         "forward_ms": tf, "backward_ms": tb, "backward_over_forward": tb / tf,
         "track_frames_per_s_forward": b.n_frames_total / tf * 1e3,
@@ -525,12 +525,12 @@ def adjoint_result(args):
 
 
 def run_fit(args):
-    """Config 4: fit the motion model (K=32, d=24) by gradient on the device
+    """Motion-model fit: fit the motion model (K=32, d=24) by gradient on the device
     from data the filter's own generative model produced."""
     import torch
     from mkfbodytracker_pdaf_gb300 import build, mixkf, synth
     build.build()
-    b = synth.config4_batch(n_tracks=args.fit_tracks, T=args.fit_frames)
+    b = synth.fit_batch_k32(n_tracks=args.fit_tracks, T=args.fit_frames)
     tt = b.theta_true()
     K, d = 32, 24
     th_true = mixkf.theta_from(tt["mu"], tt["a"], tt["Lq"], tt["sigma"])
@@ -575,7 +575,7 @@ def run_fit(args):
                "a_mae": err(a_f, tt["a"][perm]), "Q_mae": err(Qf, Qt[perm]),
                "components_relabelled": int((perm != np.arange(K)).sum())}
     print(json.dumps({
-        "workload": "config 4: fit K=32, d=24 from B=%d x T=%d, %d Adam steps (lr %g) on the device"
+        "workload": "motion-model fit: K=32, d=24 from B=%d x T=%d, %d Adam steps (lr %g) on the device"
                     % (b.n_tracks, args.fit_frames, args.fit_steps, args.fit_lr),
         "seconds_total": wall, "seconds_per_gradient_eval": wall / args.fit_steps,
         "logL_init": L0, "logL_final": Lf, "logL_true_params": Ltrue, "logL_history": hist,
@@ -603,7 +603,7 @@ def parse_args(argv=None):
     ap.add_argument("--plain-frames", type=int, default=300)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-adjoint", action="store_true", help="skip the config-3 adjoint summary of the default run")
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the mixture-KF adjoint summary of the default run")
     ap.add_argument("--workload", default="batched", choices=["batched", "sweep", "plain0", "adjoint", "fit"])
     ap.add_argument("--sweep-frames", type=int, default=200)
     ap.add_argument("--sweep-sizes", type=int, nargs="*", default=None,

@@ -42,7 +42,7 @@ def tune(n_tracks=8192, reps=2, seed=None):
     from .filters import BatchedBootstrapPF
     build.build()
     kw = {} if seed is None else {"seed": seed}
-    batch = synth.config2_batch(n_tracks=n_tracks, **kw)
+    batch = synth.uneven_tracks_batch(n_tracks=n_tracks, **kw)
     runner = BatchedBootstrapPF(batch)
     det_off, det = runner.device_inputs()
     outs = runner.alloc_outputs()

@@ -2,7 +2,7 @@
 
 The reference's own data (a rosbag of Kinect + webcam frames and ChaLearn
 sequences) is not available, so every workload is generated here from a
-committed master seed.  Generative model (shared by all configs):
+committed master seed.  Generative model (shared by all workloads):
 
 * motion model (my_gmm.cpp:45-75 generalised): K components over a d-dim PCA
   state; mu_k ~ N(0, I); Sigma_k = Wishart(d+2, 0.1 I)/(d+2); mean reversion
@@ -284,16 +284,16 @@ def make_bpf_batch(seed, n_particles, n_frames, lam, pd, d=12, K=15, max_det=16,
     return BpfBatch(model, tracks, off.astype(np.int32), pts, truth)
 
 
-# ----------------------------------------------------------------- configs
+# ----------------------------------------------------------------- workloads
 MASTER_SEED = 20140601
 
 
-def config1_batch(n_particles, n_frames=200, seed=MASTER_SEED + 1, lam=3.0, pd=0.9):
+def sweep_batch(n_particles, n_frames=200, seed=MASTER_SEED + 1, lam=3.0, pd=0.9):
     """Particle-count sweep: one track, one arm."""
     return make_bpf_batch(seed, [n_particles], [n_frames], [lam], [pd])
 
 
-def config2_spec(seed=MASTER_SEED + 2, n_tracks=8192, t_range=(50, 2000), n_range=(128, 8192),
+def uneven_tracks_spec(seed=MASTER_SEED + 2, n_tracks=8192, t_range=(50, 2000), n_range=(128, 8192),
                  lam_range=(0.0, 12.0), pd_range=(0.7, 1.0)):
     rng = np.random.default_rng(seed)
     T = rng.integers(t_range[0], t_range[1] + 1, n_tracks)
@@ -304,16 +304,16 @@ def config2_spec(seed=MASTER_SEED + 2, n_tracks=8192, t_range=(50, 2000), n_rang
     return N, T, lam, pd
 
 
-def config2_batch(n_tracks=8192, seed=MASTER_SEED + 2, **kw):
+def uneven_tracks_batch(n_tracks=8192, seed=MASTER_SEED + 2, **kw):
     """Batched uneven tracks: per-track GMM, T ~ U{50..2000}, N log-uniform
     in [128, 8192], lambda ~ U[0, 12], P_D ~ U[0.7, 1]."""
-    N, T, lam, pd = config2_spec(seed, n_tracks, **kw)
+    N, T, lam, pd = uneven_tracks_spec(seed, n_tracks, **kw)
     return make_bpf_batch(seed + 100, N, T, lam, pd)
 
 
-# ----------------------------------------------------------------- config 0
+# ----------------------------------------------------------------- two-arm pose scene
 class RbpfScene:
-    """Config-0 scene: two arms, each its own K=15, d=12 GMM and body; per frame
+    """Two-arm pose scene: two arms, each its own K=15, d=12 GMM and body; per frame
     a head ROI list per arm (true head first) and one pooled, shuffled hand list."""
 
     def __init__(self, arms, frames, truth):
@@ -367,7 +367,7 @@ def make_rbpf_scene(seed=MASTER_SEED, T=500, d=12, K=15, lam=3.0, pd=0.9, max_de
     return RbpfScene(arms, frames, np.stack(truths))
 
 
-# ----------------------------------------------------------------- configs 3/4: mixture KF
+# ----------------------------------------------------------------- mixture-KF logL and fitting
 class MixBatch:
     """Tracks sharing one motion model (theta), each with its own body
     (basis + mean pose + depth) and detection lists.  det_off indexes
@@ -414,12 +414,12 @@ def make_mix_batch(seed, n_tracks, T, K=15, d=12, lam=3.0, pd=0.9, layout="arm4"
     return MixBatch(gmm, tracks, Bm, mm, off.astype(np.int32), pts, truth)
 
 
-def config3_batch(n_tracks=1024, T=1000, seed=MASTER_SEED + 3):
+def mixkf_batch_k15(n_tracks=1024, T=1000, seed=MASTER_SEED + 3):
     """Differentiation workload: B=1024 x T=1000, K=15, d=12, PDAF over <=16 candidates."""
     return make_mix_batch(seed, n_tracks, T, K=15, d=12, lam=3.0, pd=0.9)
 
 
-def config4_batch(n_tracks=16384, T=500, seed=MASTER_SEED + 4):
+def fit_batch_k32(n_tracks=16384, T=500, seed=MASTER_SEED + 4):
     """Fitting workload: ground-truth GMM K=32, d=24 (8 joints x 3D), lambda=5."""
     return make_mix_batch(seed, n_tracks, T, K=32, d=24, lam=5.0, pd=0.9, layout="body8")
 

@@ -368,7 +368,7 @@ def num_threads():
     return lib().mko_num_threads()
 
 
-# ---------------------------------------------------------------- config 0: PFTracker flow
+# ---------------------------------------------------------------- two-arm PFTracker flow
 def scene_roi(heads_a):
     """ROI (x_offset, y_offset, width, height) from an arm's head list (cx, cy, w)."""
     cx, cy, w = heads_a[0]
@@ -387,7 +387,7 @@ def project_joint(arm, x, joint, cam=(525.0, 525.0, 319.5, 239.5)):
 
 def pose_tracker_run(scene, N, seed, T=None, Pa=0.05, clutter=1e-4, hand_joint=1, alias=False):
     """CPU restatement of PFTracker's frame loop (pfPose.cpp:210-385) on the
-    config-0 scene: per frame, PDAF association of the pooled hand detections
+    two-arm pose scene: per frame, PDAF association of the pooled hand detections
     to each arm (pfPose.cpp:247-301), the per-particle measurement columns
     (303-323), both arms' ParticleFilter::update (325-326) and getEstimator
     (347-348).  A frame without a head ROI for either arm is skipped

@@ -114,7 +114,7 @@ void mko_pdaf_weights(int M, const double* cand, const double* Lc, const double*
                       const double* hat_other, int has_other, double var, double Pa,
                       double clutter, double* w);
 
-/* ---- A13: bootstrap PF with the mixture motion model (config 1/2 kernels) */
+/* ---- A13: bootstrap PF with the mixture motion model (the streaming and batched particle kernels) */
 typedef struct {
   int d, K, J;
   const float* a;        /* K*d */

@@ -80,7 +80,7 @@ def _run_stream(torch, batch, b, T, debug=True):
 def test_plain_path_teacher_forced_parity(cuda, olib):
     from mkfbodytracker_pdaf_gb300 import synth
     torch = cuda
-    batch = synth.config1_batch(3000, n_frames=6)     # two propagate tiles, one search tile
+    batch = synth.sweep_batch(3000, n_frames=6)     # two propagate tiles, one search tile
     frames, pf = _run_stream(torch, batch, 0, 6)
     rep = check_track(torch, olib, batch, 0, frames)
     assert rep.anc_frames == 6
@@ -101,7 +101,7 @@ def test_plain_path_offspring_property_large(cuda, olib):
     from mkfbodytracker_pdaf_gb300 import synth
     torch = cuda
     N = 1 << 20
-    batch = synth.config1_batch(N, n_frames=3)
+    batch = synth.sweep_batch(N, n_frames=3)
     frames, _ = _run_stream(torch, batch, 0, 3)
     for f in frames:
         anc = f["anc"]
@@ -160,7 +160,7 @@ def test_batched_host_buffers_match_device_run(cuda):
     from mkfbodytracker_pdaf_gb300 import synth
     from mkfbodytracker_pdaf_gb300.filters import BatchedBootstrapPF
     torch = cuda
-    batch = synth.config2_batch(n_tracks=64)
+    batch = synth.uneven_tracks_batch(n_tracks=64)
     runner = BatchedBootstrapPF(batch)
     est, ll, ess, st = runner.run(*runner.device_inputs())
     G = batch.n_frames_total

@@ -211,7 +211,7 @@ def test_pdaf_weights_formula(olib):
 # ----------------------------------------------------------------- bootstrap PF pieces (A13)
 def test_bpf_pieces_vs_numpy(olib):
     from mkfbodytracker_pdaf_gb300 import synth
-    b = synth.config1_batch(64, n_frames=3)
+    b = synth.sweep_batch(64, n_frames=3)
     m, t = b.model, b.tracks[0]
     prm, keep = olib.bpf_params(m, 0, t)
     d, K = m["d"], m["K"]

@@ -1,5 +1,5 @@
 """GPU parity of the Rao-Blackwellised PF (pf2DRao) and the PDAF association
-against the FP64 oracle: shipped yml models (LINEAR, m = 6) and the config-0
+against the FP64 oracle: shipped yml models (LINEAR, m = 6) and the two-arm
 synthetic scene (PINHOLE, m = 4)."""
 import os
 
@@ -145,8 +145,8 @@ def test_pdaf_associate_parity(cuda, olib):
             arms[a].update(mg, frame=t)
 
 
-def test_pose_tracker_config0(cuda, olib):
-    """Config 0 (two arms, K=15, d=12, N=1000, FP64): the GPU PoseTracker and
+def test_pose_tracker_two_arm_scene(cuda, olib):
+    """Two-arm pose scene (K=15, d=12, N=1000, FP64): the GPU PoseTracker and
     the CPU restatement of the PFTracker loop agree to 1e-4 relative."""
     from mkfbodytracker_pdaf_gb300 import synth
     from mkfbodytracker_pdaf_gb300.filters import MEAS_PINHOLE, PoseTracker, RaoBlackwellisedPF
