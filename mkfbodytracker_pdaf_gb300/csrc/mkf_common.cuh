@@ -312,18 +312,9 @@ __device__ __forceinline__ uint64_t rs_threshold64(const RsThresh& t, uint32_t i
 }
 #endif
 
-// first j in [0, n) with Q[j] >= T (Q nondecreasing, T <= Q[n-1])
-__device__ __forceinline__ int search_u64(const uint64_t* Q, int n, uint64_t T) {
-  int lo = 0, hi = n - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (Q[mid] < T) lo = mid + 1; else hi = mid;
-  }
-  return lo;
-}
-
-// The same search for G targets at once: a branch-free lower bound whose
-// halving steps depend on n only, so the G searches run interleaved.  Needs
+// First j in [0, n) with Q[j] >= T (Q nondecreasing) for G targets at once: a
+// branch-free lower bound whose halving steps depend on n only, so the G
+// searches run interleaved.  Needs
 // T[g] <= Q[n-1].
 template <int G>
 __device__ __forceinline__ void search_u64_multi(const uint64_t* Q, int n, const uint64_t* T, int* out) {

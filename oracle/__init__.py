@@ -2,7 +2,7 @@
 
 TEST INFRASTRUCTURE ONLY: an FP64 C restatement of the reference's CPU
 arithmetic (KF_model.cpp, my_gmm.cpp, pf2DRao.cpp, pf2D.cpp, pfPose.cpp
-association), used by the tests as the checker, by ``__graft_entry__.smoke()``
+association), used by the tests as the parity reference, by ``__graft_entry__.smoke()``
 and by ``bench.py``'s CPU-baseline and reference legs.  The product package
 (``mkfbodytracker_pdaf_gb300``) never imports it.
 

@@ -1,6 +1,6 @@
 /*
  * mkf_oracle.c -- FP64 CPU restatement of the mkfbodytracker_pdaf filtering
- * hot path.  TEST INFRASTRUCTURE ONLY (the checker and the timed CPU baseline);
+ * hot path.  TEST INFRASTRUCTURE ONLY (the parity reference of the tests and the timed CPU baseline);
  * the CUDA product never links or calls it.  Parity against the reference's
  * own outputs is unpinned (the reference has no tests and cannot be built
  * here); see mkf_oracle.h for what is pinned.

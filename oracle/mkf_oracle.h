@@ -1,7 +1,7 @@
 /*
  * mkf_oracle.h -- FP64 CPU restatement of the mkfbodytracker_pdaf filtering hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA product
+ * TEST INFRASTRUCTURE ONLY.  This library is the parity reference for the CUDA product
  * (mkfbodytracker_pdaf_gb300/csrc) and the timed CPU baseline of bench.py; the
  * product never links, loads or calls it.
  *

@@ -1,7 +1,7 @@
 /*
  * mkf_oracle_mix.c -- FP64 CPU forward and reverse-mode adjoint of the
  * deterministic mixture Kalman filter with PDAF (declared in mkf_oracle.h).
- * TEST INFRASTRUCTURE ONLY: the checker of the GPU forward/adjoint kernels and
+ * TEST INFRASTRUCTURE ONLY: the parity reference of the GPU forward/adjoint kernels and
  * the CPU baseline of the gradient benchmark.  The adjoint stores every
  * frame's collapsed state (no checkpointing) and recomputes each frame's
  * intermediates, so it shares no structure with the GPU's sqrt(T) scheme.

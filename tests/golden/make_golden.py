@@ -1,5 +1,5 @@
 """Regenerate tests/golden/ from the reference checkout (run in the build
-container, where the reference is mounted; the GPU machine never runs this).
+container, where the reference is mounted; the test machines never run this).
 
 ref_models.npz: both arms' shipped model parameters (data13D/data23D
 _PCA_100000_15_12.yml) as the reference's constructor reads them, including
