@@ -597,7 +597,7 @@ def parse_args(argv=None):
     ap.add_argument("--block-threads", type=int, default=None, help="default: autotuned choice")
     ap.add_argument("--ctas-per-sm", type=int, default=None)
     ap.add_argument("--variant", type=int, default=None, help="bit 0 float4 loads, bit 1 binary-search resampling")
-    ap.add_argument("--cpu-sample-tracks", type=int, default=48)
+    ap.add_argument("--cpu-sample-tracks", type=int, default=96)
     ap.add_argument("--ref-sample-tracks", type=int, default=16)
     ap.add_argument("--plain-tracks", type=int, default=8)
     ap.add_argument("--plain-frames", type=int, default=300)
