@@ -48,3 +48,26 @@ def test_bad_arguments_are_rejected_without_gpu():
     assert b"null" in L.mkf_last_error()
     h = C.c_void_p()
     assert L.mkf_bpf_create(None, None, C.byref(h)) == 1
+
+
+def test_product_fails_loudly_without_the_library(tmp_path):
+    """No CPU fallback: with the library missing, the first call raises."""
+    import subprocess
+    import sys
+    code = ("import mkfbodytracker_pdaf_gb300._native as N\n"
+            "N.LIB_PATH = %r\n"
+            "N._lib = None\n"
+            "try:\n"
+            "    N.lib()\n"
+            "except N.MkfError as e:\n"
+            "    print('raised', e)\n" % str(tmp_path / "missing.so"))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, cwd=ROOT, timeout=120)
+    assert "raised" in r.stdout and "no CPU fallback" in r.stdout, r.stdout + r.stderr
+
+
+def test_product_package_never_imports_the_oracle():
+    pkg = os.path.join(ROOT, "mkfbodytracker_pdaf_gb300")
+    for fn in os.listdir(pkg):
+        if fn.endswith(".py"):
+            src = open(os.path.join(pkg, fn)).read()
+            assert not re.search(r"^\s*(import oracle|from oracle)", src, flags=re.M), fn
