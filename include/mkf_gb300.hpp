@@ -99,6 +99,21 @@ inline std::vector<int> resample(const std::vector<double>& w, int N, uint32_t U
   return idx.to_host(s);
 }
 
+// The reference node's hard-coded settings in one place (defaults = the
+// reference's values): particles per arm (pfPose.cpp:57), candidates per
+// particle (216), Pa (247), clutter floor (261, 282), image size (pf2D.cpp:49-50)
+// and the Kinect intrinsics of get3Dpose (pfPose.cpp:101).  The blur (15 x 15,
+// sigma 3), proposal spread (0.8 w) and R = 100 I are fixed in the kernels.
+struct TrackerConfig {
+  int particles = 500;
+  int candidates_per_particle = 10;
+  double Pa = 0.05;
+  double clutter = 1e-4;
+  int width = 640, height = 480;
+  double K[9] = {525.0, 0.0, 319.5, 0.0, 525.0, 239.5, 0.0, 0.0, 1.0};
+  uint64_t seed = 0;
+};
+
 // ------------------------------------------------------ pf2DRao::ParticleFilter
 class RaoParticleFilter {
  public:

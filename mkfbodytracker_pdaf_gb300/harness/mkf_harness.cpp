@@ -146,9 +146,10 @@ void load_filter(mkf::RaoParticleFilter& pf, const ArmModel& a, const mkf::yaml:
 
 int cmd_track(int argc, char** argv) {
   std::string arm1, arm2, frames_path, out_path;
-  int N = 500;
-  unsigned long long seed = 0;
-  double Pa = 0.05, clutter = 1e-4;
+  mkf::TrackerConfig cfg;
+  int& N = cfg.particles;
+  uint64_t& seed = cfg.seed;
+  double &Pa = cfg.Pa, &clutter = cfg.clutter;
   bool own_gamma = false;
   for (int i = 2; i < argc; ++i) {
     std::string a = argv[i];
@@ -200,7 +201,8 @@ int cmd_track(int argc, char** argv) {
       const Frame& fr = frames[t];
       const bool ok = image_mode
                           ? tracker.stepImage(static_cast<uint32_t>(fr.id), fr.has_roi ? fr.roi : nullptr,
-                                              like[t].data(), ff.width, ff.height, ff.width)
+                                              like[t].data(), ff.width, ff.height, ff.width,
+                                              cfg.candidates_per_particle * N)
                           : tracker.step(static_cast<uint32_t>(fr.id), fr.has_roi ? fr.roi : nullptr, fr.cand);
       if (ok) {
         pf1.estimateInto(est1.data() + static_cast<size_t>(t) * d);
@@ -209,8 +211,8 @@ int cmd_track(int argc, char** argv) {
       }
     }
     // batched decode of every frame's estimate (skipped frames decode zeros and are flagged invalid)
-    const double Kc[9] = {525.0, 0.0, 319.5, 0.0, 525.0, 239.5, 0.0, 0.0, 1.0};   // pfPose.cpp:101
-    mkf::PoseDecoder dec1(m1.pca_proj.data, m1.pca_mean.data, d, Kc, s), dec2(m2.pca_proj.data, m2.pca_mean.data, d, Kc, s);
+    mkf::PoseDecoder dec1(m1.pca_proj.data, m1.pca_mean.data, d, cfg.K, s),
+        dec2(m2.pca_proj.data, m2.pca_mean.data, d, cfg.K, s);
     mkf::DeviceArray<double> e_1(static_cast<size_t>(T) * F + 1), e_2(static_cast<size_t>(T) * F + 1);
     mkf::DeviceArray<double> p3_1(static_cast<size_t>(T) * 15 + 1), p3_2(static_cast<size_t>(T) * 15 + 1);
     mkf::DeviceArray<double> pts(static_cast<size_t>(T) * 16 + 1);
