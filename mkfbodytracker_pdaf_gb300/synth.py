@@ -229,7 +229,7 @@ def make_bpf_batch(seed, n_particles, n_frames, lam, pd, d=12, K=15, max_det=16,
     n_frames = np.asarray(n_frames, np.int64)
     nm = 1 if shared_model else B_
     gmm = make_gmm(rng, d, K, n=nm)
-    Bs, mbar, measured = make_body(rng, d, n=nm)
+    Bs, mbar, measured = make_body(rng, d, n=nm, layout="arm4" if d == 12 else "body8")
     J = len(measured)
     # simulate in chunks of tracks to bound memory
     G = int(n_frames.sum())
