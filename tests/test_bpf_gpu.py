@@ -80,17 +80,25 @@ def _run_stream(torch, batch, b, T, debug=True):
 def test_plain_path_teacher_forced_parity(cuda, olib):
     from mkfbodytracker_pdaf_gb300 import synth
     torch = cuda
-    batch = synth.sweep_batch(3000, n_frames=6)     # two propagate tiles, one search tile
+    batch = synth.sweep_batch(3000, n_frames=6)     # a dozen propagate and search tiles on 152 SMs
     frames, pf = _run_stream(torch, batch, 0, 6)
     rep = check_track(torch, olib, batch, 0, frames)
     assert rep.anc_frames == 6
     assert pf.status() == 0
 
 
+def test_plain_path_single_tile_parity(cuda, olib):
+    from mkfbodytracker_pdaf_gb300 import synth
+    torch = cuda
+    batch = synth.make_bpf_batch(78, [100], [4], [5.0], [0.85])    # one block per kernel
+    frames, _ = _run_stream(torch, batch, 0, 4)
+    check_track(torch, olib, batch, 0, frames)
+
+
 def test_plain_path_multi_tile_parity(cuda, olib):
     from mkfbodytracker_pdaf_gb300 import synth
     torch = cuda
-    batch = synth.make_bpf_batch(77, [9000], [3], [8.0], [0.8])   # 3 search tiles, 5 propagate tiles
+    batch = synth.make_bpf_batch(77, [9000], [3], [8.0], [0.8])   # ~36 propagate and search tiles
     frames, _ = _run_stream(torch, batch, 0, 3)
     check_track(torch, olib, batch, 0, frames)
 
