@@ -173,14 +173,20 @@ typedef struct mkf_bpf_batch* mkf_bpf_batch_t;
  * det[det_off[g*J+j] .. det_off[g*J+j+1]). */
 int mkf_bpf_batch_create(const mkf_bpf_models* models, int n_tracks, const mkf_bpf_track* tracks,
                          int64_t n_frames_total, mkf_bpf_batch_t* out);
-/* tuning: threads per CTA (64..512, multiple of 32) and CTAs per SM (0 = max) */
+/* tuning: threads per CTA (64..512, multiple of 32) and CTAs per SM (0 = max).
+ * Launch bounds of VEC_LOADS | SEARCH (with or without LOWSMEM): <= 256
+ * threads at 2 CTAs per SM (3 when ctas_per_sm >= 3), 257..384 threads at 2,
+ * 385..512 threads at 1; of the other variants: <= 256 threads at 2, 257..512
+ * threads at 1.  Shared memory can bound residency further. */
 int mkf_bpf_batch_set_tuning(mkf_bpf_batch_t h, int block_threads, int ctas_per_sm);
 /* code variants (autotuned; applied to the d = 12 diagonal-noise model):
  * MKF_BPF_VEC_LOADS = float4 model loads, MKF_BPF_SEARCH = ancestors by binary
  * search over shared prefix sums (12 bytes/particle of shared memory) instead
  * of the scatter walk (8 bytes/particle), MKF_BPF_PAIR = two particles per
- * loop iteration (implies the other two).  Results are identical. */
-enum { MKF_BPF_VEC_LOADS = 1, MKF_BPF_SEARCH = 2, MKF_BPF_PAIR = 4 };
+ * loop iteration (implies the other two), MKF_BPF_LOWSMEM = the search with
+ * 8 bytes/particle of shared memory (ancestors kept in global memory; needs
+ * VEC_LOADS | SEARCH, not PAIR).  Results are identical. */
+enum { MKF_BPF_VEC_LOADS = 1, MKF_BPF_SEARCH = 2, MKF_BPF_PAIR = 4, MKF_BPF_LOWSMEM = 8 };
 int mkf_bpf_batch_set_variant(mkf_bpf_batch_t h, int flags);
 /* device-resident run: outputs est (G*d), loglik (G), ess (G), status (n_tracks) */
 int mkf_bpf_batch_run(mkf_bpf_batch_t h, const int* d_det_off, const float* d_det,
@@ -194,6 +200,9 @@ int mkf_bpf_batch_run_host(mkf_bpf_batch_t h, const int* det_off, const float* d
 /* debug capture of one track's per-frame weights and ancestors (n_frames*N
  * each, device pointers; NULL disables) */
 int mkf_bpf_batch_set_debug(mkf_bpf_batch_t h, int track, float* d_w, int* d_anc);
+/* the persistent grid of the last run (SM count x resident CTAs per SM,
+ * capped at n_tracks); 0 before the first run */
+int mkf_bpf_batch_last_grid(mkf_bpf_batch_t h, int* grid);
 int mkf_bpf_batch_destroy(mkf_bpf_batch_t h);
 
 

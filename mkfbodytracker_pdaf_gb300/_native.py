@@ -71,6 +71,7 @@ SIGNATURES = {
     "mkf_bpf_batch_run": (I, [P, P, P, P, P, P, P, P]),
     "mkf_bpf_batch_run_host": (I, [P, P, P, I64, P, P, P, P, P]),
     "mkf_bpf_batch_set_debug": (I, [P, I, P, P]),
+    "mkf_bpf_batch_last_grid": (I, [P, C.POINTER(I)]),
     "mkf_bpf_batch_destroy": (I, [P]),
     "mkf_likelihood_blur": (I, [P, I, I, I, P, I, P]),
     "mkf_pdaf_propose_image": (I, [P, P, U32, P, P, I, I, I, I, I, C.c_double, C.c_double, P, P, P, P, P, P, P]),

@@ -20,11 +20,16 @@ import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 TUNING_FILE = os.path.join(HERE, "tuning_gb300.json")
+# variant bits: 1 float4 loads, 2 binary-search resampling, 4 particle pairs,
+# 8 the search with 8 bytes/particle of shared memory (ancestors in L2)
 # (block_threads, ctas_per_sm): 512x1 and 256x2 compile with a 128-register
-# budget, 256x3 with an 80-register budget (3 CTAs of 71 KB shared memory each)
-SHAPES = [(256, 2), (256, 3), (512, 1)]
-VARIANTS = [0, 1, 2, 3, 7]       # bit 0: float4 loads, bit 1: binary-search resampling, bit 2: particle pairs
-CANDIDATES = [(tb, cps, v) for (tb, cps) in SHAPES for v in VARIANTS]
+# budget; 256x3 and 384x2 (float4 loads + search only) with 80 registers.  At
+# 8192 particles the search keeps 12 bytes/particle in shared memory (2 CTAs
+# of 102 KB per SM), the LOW layout 8 (3 CTAs of 70 KB).
+CANDIDATES = ([(256, 2, v) for v in (0, 1, 2, 3, 7, 11)] + [(512, 1, v) for v in (0, 1, 2, 3, 7, 11)] +
+              [(256, 3, 3), (384, 2, 3), (256, 3, 11), (384, 2, 11)])
+# the candidates that have ranked at the top, for a short tuning run
+QUICK = [(256, 2, 3), (256, 3, 3), (384, 2, 3), (256, 3, 11), (384, 2, 11)]
 
 
 def load_tuning():
@@ -36,7 +41,7 @@ def load_tuning():
     return 256, 3, 1
 
 
-def tune(n_tracks=8192, reps=2, seed=None):
+def tune(n_tracks=8192, reps=2, seed=None, candidates=CANDIDATES):
     import torch
     from . import build, synth
     from .filters import BatchedBootstrapPF
@@ -48,7 +53,7 @@ def tune(n_tracks=8192, reps=2, seed=None):
     outs = runner.alloc_outputs()
     G = batch.n_frames_total
     res = []
-    for tb, cps, var in CANDIDATES:
+    for tb, cps, var in candidates:
         try:
             runner.set_tuning(tb, cps, var)
             runner.run(det_off, det, outs)
@@ -61,7 +66,7 @@ def tune(n_tracks=8192, reps=2, seed=None):
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1) / reps
             res.append({"block_threads": tb, "ctas_per_sm": cps, "variant": var, "ms": ms,
-                        "track_frames_per_s": G / ms * 1e3})
+                        "track_frames_per_s": G / ms * 1e3, "grid": runner.last_grid()})
         except Exception as ex:  # a shape that does not fit is reported, not fatal
             res.append({"block_threads": tb, "ctas_per_sm": cps, "variant": var, "error": str(ex)})
     ok = [r for r in res if "ms" in r]
@@ -76,8 +81,9 @@ def main():
     ap.add_argument("--tracks", type=int, default=8192)
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--out", default=TUNING_FILE)
+    ap.add_argument("--quick", action="store_true", help="rank only the usual top candidates")
     a = ap.parse_args()
-    r = tune(a.tracks, a.reps)
+    r = tune(a.tracks, a.reps, candidates=QUICK if a.quick else CANDIDATES)
     with open(a.out, "w") as f:
         json.dump(r, f, indent=1)
     print(json.dumps(r))

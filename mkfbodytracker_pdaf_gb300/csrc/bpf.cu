@@ -301,6 +301,7 @@ struct BatchArgs {
   float* ess;
   int* status;
   float* scratch;                   // gridDim.x * 2 * D * Nmax
+  int* anc;                         // LOW variant: gridDim.x * Nmax ancestors
   int dbg_track;
   float* dbg_w;
   int* dbg_anc;
@@ -341,18 +342,24 @@ __host__ __device__ constexpr int params_floats(int K, int J, bool diag) {
 // Code variants chosen by the autotuner: VEC (float4 vs scalar parameter loads)
 // and SEARCH (ancestors by binary search over the shared prefix sums, 12 Nmax
 // bytes of shared memory, vs the scatter walk over each thread's chunk, 8 Nmax).
-template <int D, bool DIAG, int TBMAX, int MINB, bool VEC, bool SEARCH, bool PAIR = false>
+// LOW (with SEARCH): 8 Nmax bytes of shared memory, so that three CTAs of the
+// largest tracks fit on an SM; the log-weights are kept in the prefix array's
+// entries and the ancestors in the CTA's global slot (L2).
+template <int D, bool DIAG, int TBMAX, int MINB, bool VEC, bool SEARCH, bool PAIR = false, bool LOW = false>
 __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
+  static_assert(!LOW || (SEARCH && !PAIR), "the LOW layout is a SEARCH variant");
   extern __shared__ __align__(16) unsigned char smem[];
   const int TB = blockDim.x, tid = threadIdx.x;
   constexpr int NV = D + 3;
   const int Nmax = A.Nmax;
   // SEARCH: sQ (u64) | sA (log-weights, weights, then ancestors, as int bits)
+  // LOW: sQ (log-weights in the low word, then integer weights, then prefix
+  //      sums); sA (ancestors) in global memory
   // scatter: sW (log-weights then weights) | sA (ancestors)
   uint64_t* sQ = reinterpret_cast<uint64_t*>(smem);
   float* sW = reinterpret_cast<float*>(smem);
-  int* sA = reinterpret_cast<int*>(smem + (SEARCH ? 8 : 4) * (size_t)Nmax);
-  float* sP = reinterpret_cast<float*>(smem + (SEARCH ? 12 : 8) * (size_t)Nmax);   // Nmax % 32 == 0
+  int* sA = LOW ? A.anc + (size_t)blockIdx.x * Nmax : reinterpret_cast<int*>(smem + (SEARCH ? 8 : 4) * (size_t)Nmax);
+  float* sP = reinterpret_cast<float*>(smem + (LOW ? 8 : SEARCH ? 12 : 8) * (size_t)Nmax);   // Nmax % 32 == 0
   const int K = A.K, J = A.J;
   const int Lsz = pad4(DIAG ? K * D : K * D * (D + 1) / 2);
   float* s_a = sP;
@@ -491,7 +498,9 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
           propagate<D, DIAG, VEC>(pv, eps, uc, x);
           store_state<D>(xb, Nmax, i, x);
           float ll = loglik<D, VEC>(pv, x, s_cnt, s_det, LK);
-          if (SEARCH) sA[i] = __float_as_int(ll); else sW[i] = ll;
+          if (LOW) sQ[i] = (uint64_t)__float_as_uint(ll);
+          else if (SEARCH) sA[i] = __float_as_int(ll);
+          else sW[i] = ll;
           lmax = fmaxf(lmax, ll);
           const float wl = __expf(ll - Lub);
           fs += wl;
@@ -516,7 +525,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       uint64_t cs = 0;
       if (SEARCH) {
         for (int j = j0; j < j1; ++j) {
-          const float ll = __int_as_float(sA[j]);
+          const float ll = LOW ? __uint_as_float((uint32_t)sQ[j]) : __int_as_float(sA[j]);
           float w = fb ? 0.0f : (ll == M ? 1.0f : __expf(ll - M));
           if (!(w >= 0.0f)) w = 0.0f;
           const uint64_t q = quantize39(w);
@@ -650,9 +659,9 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
   }
 }
 
-static size_t batched_smem_bytes(int D, int Nmax, int K, int J, bool diag, bool search) {
+static size_t batched_smem_bytes(int D, int Nmax, int K, int J, bool diag, bool search, bool low) {
   size_t pf = (D == 12) ? params_floats<12>(K, J, diag) : params_floats<24>(K, J, diag);
-  size_t bytes = (search ? 12 : 8) * (size_t)Nmax + 4 * pf + 8 * MKF_MAX_J * MKF_MAX_DET + 32 +
+  size_t bytes = (low ? 8 : search ? 12 : 8) * (size_t)Nmax + 4 * pf + 8 * MKF_MAX_J * MKF_MAX_DET + 32 +
                  4 * (32 * (D + 3) + 2) + 8 * 34 + 16 + kPickBins;
   return (bytes + 15) & ~size_t(15);
 }
@@ -1350,24 +1359,34 @@ extern "C" int mkf_bpf_batch_set_tuning(mkf_bpf_batch_t B, int block_threads, in
   return MKF_OK;
 }
 
+extern "C" int mkf_bpf_batch_last_grid(mkf_bpf_batch_t B, int* grid) {
+  MKF_ARG(B && grid, "mkf_bpf_batch_last_grid: null argument");
+  *grid = B->last_grid;
+  return MKF_OK;
+}
+
 extern "C" int mkf_bpf_batch_set_debug(mkf_bpf_batch_t B, int track, float* d_w, int* d_anc) {
   MKF_ARG(B, "mkf_bpf_batch_set_debug: null handle");
   B->dbg_track = track; B->dbg_w = d_w; B->dbg_anc = d_anc;
   return MKF_OK;
 }
 
-template <int D, bool DIAG, int TBMAX, int MINB, bool VEC, bool SEARCH, bool PAIR>
+template <int D, bool DIAG, int TBMAX, int MINB, bool VEC, bool SEARCH, bool PAIR, bool LOW>
 static int launch_batched_v(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
-  auto kern = bpf_batched_kernel<D, DIAG, TBMAX, MINB, VEC, SEARCH, PAIR>;
-  size_t smem = batched_smem_bytes(D, B->Nmax, B->K, B->J, DIAG, SEARCH);
+  auto kern = bpf_batched_kernel<D, DIAG, TBMAX, MINB, VEC, SEARCH, PAIR, LOW>;
+  size_t smem = batched_smem_bytes(D, B->Nmax, B->K, B->J, DIAG, SEARCH, LOW);
   MKF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // the largest shared-memory carveout: residency is bounded by shared memory
+  MKF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                (int)cudaSharedmemCarveoutMaxShared));
   int occ = 0;
   MKF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, B->tb, smem));
   if (occ < 1) { set_error("mkf_bpf_batch_run: block shape does not fit on an SM"); return MKF_ERR_ARG; }
   int per_sm = B->ctas_per_sm > 0 ? std::min(B->ctas_per_sm, occ) : occ;
   long long grid = (long long)num_sms() * per_sm;
   grid = std::min<long long>(grid, B->n_tracks);
-  size_t need = (size_t)grid * 2 * D * B->Nmax;
+  // per CTA: two state buffers (2 D Nmax floats); LOW adds Nmax ancestors
+  size_t need = (size_t)grid * (2 * D + (LOW ? 1 : 0)) * B->Nmax;
   if (need > B->scratch_slots) {
     if (B->scratch) cudaFree(B->scratch);
     B->scratch = nullptr;
@@ -1376,6 +1395,7 @@ static int launch_batched_v(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
     B->scratch_slots = need;
   }
   a.scratch = B->scratch;
+  a.anc = LOW ? reinterpret_cast<int*>(B->scratch + (size_t)grid * 2 * D * B->Nmax) : nullptr;
   B->last_grid = (int)grid;
   MKF_CUDA(cudaMemsetAsync(B->counter, 0, sizeof(int), s));
   kern<<<(int)grid, B->tb, smem, s>>>(a);
@@ -1383,32 +1403,49 @@ static int launch_batched_v(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
   return MKF_OK;
 }
 
-template <int D, bool DIAG, bool VEC, bool SEARCH, bool PAIR = false>
+// Launch bounds by block size and requested residency.  ALL: up to 256
+// threads at 2 (128 registers) or 3 (80 registers) CTAs per SM, up to 384
+// threads at 2 CTAs per SM (80 registers), up to 512 threads at 1.  Otherwise
+// (the variants the autotuner ranks below float4 loads + search): up to 256
+// threads at 2 CTAs per SM, up to 512 at 1, which keeps the number of compiled
+// kernels, and the build time, down.
+template <int D, bool DIAG, bool VEC, bool SEARCH, bool PAIR = false, bool LOW = false, bool ALL = false>
 static int launch_shape(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
-  if (B->tb > 256) return launch_batched_v<D, DIAG, 512, 1, VEC, SEARCH, PAIR>(B, a, s);
-  if (B->ctas_per_sm >= 3) return launch_batched_v<D, DIAG, 256, 3, VEC, SEARCH, PAIR>(B, a, s);
-  return launch_batched_v<D, DIAG, 256, 2, VEC, SEARCH, PAIR>(B, a, s);
+  if constexpr (ALL) {
+    if (B->tb > 384) return launch_batched_v<D, DIAG, 512, 1, VEC, SEARCH, PAIR, LOW>(B, a, s);
+    if (B->tb > 256) return launch_batched_v<D, DIAG, 384, 2, VEC, SEARCH, PAIR, LOW>(B, a, s);
+    if (B->ctas_per_sm >= 3) return launch_batched_v<D, DIAG, 256, 3, VEC, SEARCH, PAIR, LOW>(B, a, s);
+    return launch_batched_v<D, DIAG, 256, 2, VEC, SEARCH, PAIR, LOW>(B, a, s);
+  }
+  if (B->tb > 256) return launch_batched_v<D, DIAG, 512, 1, VEC, SEARCH, PAIR, LOW>(B, a, s);
+  return launch_batched_v<D, DIAG, 256, 2, VEC, SEARCH, PAIR, LOW>(B, a, s);
 }
 
-// launch-bound variant by block size and requested residency; the load-width
-// and resampler variants are compiled for the diagonal-noise d = 12 model only
+// the load-width and resampler variants are compiled for the diagonal-noise
+// d = 12 model only
 template <int D, bool DIAG>
 static int launch_batched(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
-  if (D == 12 && DIAG) {
+  if constexpr (D == 12 && DIAG) {
     const bool vec = (B->variant & MKF_BPF_VEC_LOADS) != 0, search = (B->variant & MKF_BPF_SEARCH) != 0;
     if (B->variant & MKF_BPF_PAIR) return launch_shape<D, DIAG, true, true, true>(B, a, s);
-    if (vec && search) return launch_shape<D, DIAG, true, true>(B, a, s);
+    if (B->variant & MKF_BPF_LOWSMEM) return launch_shape<D, DIAG, true, true, false, true, true>(B, a, s);
+    if (vec && search) return launch_shape<D, DIAG, true, true, false, false, true>(B, a, s);
     if (vec) return launch_shape<D, DIAG, true, false>(B, a, s);
     if (search) return launch_shape<D, DIAG, false, true>(B, a, s);
     return launch_shape<D, DIAG, false, false>(B, a, s);
+  } else {
+    return launch_shape<D, DIAG, true, false>(B, a, s);
   }
-  return launch_shape<D, DIAG, true, false>(B, a, s);
 }
 
 extern "C" int mkf_bpf_batch_set_variant(mkf_bpf_batch_t B, int flags) {
   MKF_ARG(B, "mkf_bpf_batch_set_variant: null handle");
-  MKF_ARG((flags & ~(MKF_BPF_VEC_LOADS | MKF_BPF_SEARCH | MKF_BPF_PAIR)) == 0,
+  MKF_ARG((flags & ~(MKF_BPF_VEC_LOADS | MKF_BPF_SEARCH | MKF_BPF_PAIR | MKF_BPF_LOWSMEM)) == 0,
           "mkf_bpf_batch_set_variant: unknown flag");
+  MKF_ARG(!(flags & MKF_BPF_LOWSMEM) ||
+              ((flags & (MKF_BPF_VEC_LOADS | MKF_BPF_SEARCH)) == (MKF_BPF_VEC_LOADS | MKF_BPF_SEARCH) &&
+               !(flags & MKF_BPF_PAIR)),
+          "mkf_bpf_batch_set_variant: MKF_BPF_LOWSMEM needs MKF_BPF_VEC_LOADS | MKF_BPF_SEARCH, without MKF_BPF_PAIR");
   B->variant = flags;
   return MKF_OK;
 }

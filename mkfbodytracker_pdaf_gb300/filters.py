@@ -150,10 +150,17 @@ class FrameGraph:
 
 
 class BatchedBootstrapPF:
-    """All tracks of a synth.BpfBatch (or equivalent) in one persistent launch."""
+    """All tracks of a synth.BpfBatch (or equivalent) in one persistent launch.
+    Launch shape and code variant default to the autotuned choice
+    (autotune.load_tuning); any of them can be given explicitly."""
 
-    def __init__(self, batch, block_threads=256, ctas_per_sm=0, variant=1):
+    def __init__(self, batch, block_threads=None, ctas_per_sm=None, variant=None):
         import torch
+        from .autotune import load_tuning
+        tb, cps, var = load_tuning()
+        block_threads = tb if block_threads is None else block_threads
+        ctas_per_sm = cps if ctas_per_sm is None else ctas_per_sm
+        variant = var if variant is None else variant
         self.torch = torch
         self.batch = batch
         m = batch.model
@@ -211,6 +218,12 @@ class BatchedBootstrapPF:
     def set_debug(self, track, w=None, anc=None):
         N.check(N.lib().mkf_bpf_batch_set_debug(self.h, int(track), _ptr(w), _ptr(anc)),
                 "mkf_bpf_batch_set_debug")
+
+    def last_grid(self):
+        """CTAs of the last run's persistent grid (SMs x resident CTAs per SM)."""
+        g = C.c_int()
+        N.check(N.lib().mkf_bpf_batch_last_grid(self.h, C.byref(g)), "mkf_bpf_batch_last_grid")
+        return g.value
 
     def __del__(self):
         try:

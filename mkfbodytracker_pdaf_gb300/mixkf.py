@@ -139,7 +139,7 @@ class MixtureKF:
             assert resume.theta.size == self.n_theta
             theta0 = resume.theta
             start = resume.step + 1
-        th = torch.from_numpy(np.ascontiguousarray(theta0, np.float64)).cuda()
+        th = torch.from_numpy(np.array(theta0, np.float64, order="C", copy=True)).cuda()
         m = torch.zeros_like(th) if resume is None else torch.from_numpy(resume.m.copy()).cuda()
         v = torch.zeros_like(th) if resume is None else torch.from_numpy(resume.v.copy()).cuda()
         mk = None if mask is None else torch.from_numpy(np.ascontiguousarray(mask, np.uint8)).cuda()

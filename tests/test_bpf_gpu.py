@@ -122,7 +122,16 @@ def test_plain_path_offspring_property_large(cuda, olib):
         assert 1.0 <= f["ess"] <= N
 
 
-def test_batched_teacher_forced_parity(cuda, olib):
+# (block_threads, ctas_per_sm, variant): every load/resampler variant of the
+# d = 12 kernel (bits: 1 float4 loads, 2 search, 4 pairs, 8 search with the
+# ancestors in global memory) and the four launch-bound shapes, including the
+# autotuned one
+BATCHED_SHAPES = [(256, 0, 0), (256, 0, 1), (256, 2, 2), (256, 2, 3), (256, 2, 7), (256, 3, 3), (512, 0, 3),
+                  (384, 2, 3), (256, 3, 11), (384, 2, 11), (512, 0, 11)]
+
+
+@pytest.mark.parametrize("shape", BATCHED_SHAPES, ids=lambda s: "tb%d_cps%d_v%d" % s)
+def test_batched_teacher_forced_parity(cuda, olib, shape):
     from mkfbodytracker_pdaf_gb300 import synth
     from mkfbodytracker_pdaf_gb300.filters import BatchedBootstrapPF
     torch = cuda
@@ -130,7 +139,8 @@ def test_batched_teacher_forced_parity(cuda, olib):
     Ts = [7, 5, 9, 4, 3, 2, 12, 0]
     batch = synth.make_bpf_batch(31, Ns, Ts, [3.0, 0.0, 12.0, 6.0, 1.0, 4.0, 2.0, 5.0],
                                  [0.9, 0.7, 0.99, 0.8, 0.75, 0.95, 0.9, 0.9])
-    runner = BatchedBootstrapPF(batch, block_threads=256)
+    tb, cps, var = shape
+    runner = BatchedBootstrapPF(batch, block_threads=tb, ctas_per_sm=cps, variant=var)
     det_off, det = runner.device_inputs()
     for dbg_track in (0, 3, 5):
         N = int(batch.tracks[dbg_track]["n_particles"])
@@ -147,13 +157,15 @@ def test_batched_teacher_forced_parity(cuda, olib):
         check_track(torch, olib, batch, dbg_track, frames)
 
 
-def test_batched_matches_plain_path(cuda, olib):
+@pytest.mark.parametrize("shape", BATCHED_SHAPES, ids=lambda s: "tb%d_cps%d_v%d" % s)
+def test_batched_matches_plain_path(cuda, olib, shape):
     """Both launch shapes run the same per-particle code on the same draws."""
     from mkfbodytracker_pdaf_gb300 import synth
     from mkfbodytracker_pdaf_gb300.filters import BatchedBootstrapPF
     torch = cuda
     batch = synth.make_bpf_batch(41, [500, 2048, 4000], [10, 6, 4], [3.0, 5.0, 2.0], [0.9, 0.9, 0.8])
-    runner = BatchedBootstrapPF(batch)
+    tb, cps, var = shape
+    runner = BatchedBootstrapPF(batch, block_threads=tb, ctas_per_sm=cps, variant=var)
     est, ll, ess, st = runner.run(*runner.device_inputs())
     torch.cuda.synchronize()
     for b in range(3):
@@ -182,3 +194,17 @@ def test_batched_host_buffers_match_device_run(cuda):
     # tracking sanity: the filter follows the ground truth on average
     err = np.abs(outs[0] - batch.truth).mean()
     assert err < 0.6, err
+
+
+def test_batched_variant_flags_checked(cuda):
+    """The search with global ancestors needs float4 loads and the search, not pairs."""
+    from mkfbodytracker_pdaf_gb300 import _native as N, synth
+    from mkfbodytracker_pdaf_gb300.filters import BatchedBootstrapPF
+    batch = synth.make_bpf_batch(3, [64], [2], [1.0], [0.9])
+    runner = BatchedBootstrapPF(batch, block_threads=256, ctas_per_sm=0, variant=3)
+    for bad in (8, 9, 10, 15, 16):
+        assert N.lib().mkf_bpf_batch_set_variant(runner.h, bad) == 1, bad          # MKF_ERR_ARG
+    assert N.lib().mkf_bpf_batch_set_variant(runner.h, 11) == 0
+    runner.run(*runner.device_inputs())
+    cuda.synchronize()
+    assert runner.last_grid() == 1          # capped at the number of tracks
