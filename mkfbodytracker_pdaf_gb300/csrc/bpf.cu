@@ -246,13 +246,20 @@ __device__ __forceinline__ float loglik(const PView& p, const float* x, const in
       }
       q0 = p0.x + p0.y; q1 = p1.x + p1.y; q2 = p2.x + p2.y;
     } else {
-      q0 = p.mm[j * 3 + 0]; q1 = p.mm[j * 3 + 1]; q2 = p.mm[j * 3 + 2];
+      // the packed path's two partial sums, one lane at a time, so that both
+      // load widths give bit-identical log-likelihoods
+      float e0 = p.mm[j * 3 + 0], e1 = p.mm[j * 3 + 1], e2 = p.mm[j * 3 + 2];
+      float o0 = 0.0f, o1 = 0.0f, o2 = 0.0f;
 #pragma unroll
-      for (int c = 0; c < D; ++c) {
-        q0 = fmaf(B[c], x[c], q0);
-        q1 = fmaf(B[D + c], x[c], q1);
-        q2 = fmaf(B[2 * D + c], x[c], q2);
+      for (int c = 0; c < D; c += 2) {
+        e0 = fmaf(B[c], x[c], e0);
+        o0 = fmaf(B[c + 1], x[c + 1], o0);
+        e1 = fmaf(B[D + c], x[c], e1);
+        o1 = fmaf(B[D + c + 1], x[c + 1], o1);
+        e2 = fmaf(B[2 * D + c], x[c], e2);
+        o2 = fmaf(B[2 * D + c + 1], x[c + 1], o2);
       }
+      q0 = e0 + o0; q1 = e1 + o1; q2 = e2 + o2;
     }
     if (!(q2 > kZMin)) { ll = __fadd_rn(ll, L.log_kappa); continue; }
     const float iz = __fdividef(1.0f, q2);

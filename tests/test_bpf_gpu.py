@@ -206,5 +206,5 @@ def test_batched_variant_flags_checked(cuda):
         assert N.lib().mkf_bpf_batch_set_variant(runner.h, bad) == 1, bad          # MKF_ERR_ARG
     assert N.lib().mkf_bpf_batch_set_variant(runner.h, 11) == 0
     runner.run(*runner.device_inputs())
-    cuda.synchronize()
+    cuda.cuda.synchronize()
     assert runner.last_grid() == 1          # capped at the number of tracks
