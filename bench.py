@@ -34,11 +34,13 @@ sys.path.insert(0, ROOT)
 METRIC = "track-frame updates/s, plain vs batched+adjoint on 1 GB300, at ≤1e-4 rel. error"
 UNIT = "track-frames/s"
 BYTES_PER_PF = 112          # algorithmic bytes per particle-frame (state in/out 4d+4d, logw 8, anc 8)
-# DRAM bytes per particle-frame of bpf_batched_kernel: dram__bytes_read.sum +
-# dram__bytes_write.sum of one ncu capture on 2048 tracks of the same workload
-# (210.7 GB over 4.148e9 particle-frames), scaled to a full launch by
-# particle-frames (profiles/bpf_batched_kernel_uneven_tracks_B8192.md)
-TRAFFIC_BYTES_PER_PF = 50.8
+# DRAM bytes per particle-frame of bpf_batched_kernel (autotuned shape: 256
+# threads x 3 CTAs/SM, float4 loads + search with ancestors in global memory):
+# dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture on 2048
+# tracks of the same workload (284.7 GB over 4.148e9 particle-frames), scaled
+# to a full launch by particle-frames
+# (profiles/bpf_batched_kernel_uneven_tracks_B8192.md)
+TRAFFIC_BYTES_PER_PF = 68.6
 
 
 def load_peaks():
