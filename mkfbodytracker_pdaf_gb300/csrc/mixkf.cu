@@ -27,10 +27,11 @@ namespace mkf {
 constexpr int kMixMaxC = MKF_MAX_DET;
 constexpr float kMixZMin = 0.05f;
 
-// joint record layout (floats)
+// joint record layout (floats); float 95 is padding, so that H, U, Kg, W, the
+// saved state and the saved covariance all start on a 16-byte boundary
 enum {
   R_VIS = 0, R_N = 1, R_P3 = 2, R_IZ = 5, R_ZH = 6, R_JP = 8, R_S = 14, R_SI = 18, R_LD = 22,
-  R_ELL = 23, R_B0 = 24, R_NB = 25, R_M = 27, R_NU = 31, R_E = 63, R_BETA = 79, R_H = 95
+  R_ELL = 23, R_B0 = 24, R_NB = 25, R_M = 27, R_NU = 31, R_E = 63, R_BETA = 79, R_H = 96
 };
 __host__ __device__ inline int rec_size(int d) { return (R_H + 9 * d + d * d + 3) & ~3; }
 __host__ __device__ inline int rec_U(int d) { return R_H + 2 * d; }
@@ -56,9 +57,12 @@ __host__ __device__ inline FrameLayout frame_layout(int d, int K, int J) {
   L.size = (o + 31) & ~31;
   return L;
 }
-// Per-component adjoint work block (floats)
+// Per-component adjoint work block (floats).  gmu, ga and Sq accumulate over
+// one backward segment: the mu and a adjoints, and Sq = the sum of the frames'
+// adjoints of the predicted covariance, from which the L_Q adjoint of the
+// segment is formed once (L_Q is the same in every frame).
 struct WorkLayout {
-  int xb, Pb, Xin, Pin, Dkb, tmp, gmu, ga, gL, size;
+  int xb, Pb, Xin, Pin, Dkb, tmp, gmu, ga, Sq, size;
 };
 __host__ __device__ inline WorkLayout work_layout(int d) {
   WorkLayout L;
@@ -67,7 +71,7 @@ __host__ __device__ inline WorkLayout work_layout(int d) {
   L.Xin = o; o += d; L.Pin = o; o += d * d;
   L.Dkb = o; o += d;
   L.tmp = o; o += 8 * d;
-  L.gmu = o; o += d; L.ga = o; o += d; L.gL = o; o += d * (d + 1) / 2;
+  L.gmu = o; o += d; L.ga = o; o += d; L.Sq = o; o += d * d;
   L.size = (o + 3) & ~3;
   return L;
 }
@@ -103,9 +107,10 @@ __device__ __forceinline__ float wsum(float v) { return warp_sum(v); }
 
 // ---------------------------------------------------------------- forward pieces
 // sequential PDAF/EKF update of one joint for one component (whole warp)
-// R: this warp's scratch record (shared memory, R_H + 8d floats); x, P: the
-// component state (shared memory, updated in place); Rg: when non-null the
-// global record that keeps this update for the reverse sweep
+// R: this warp's scratch record (shared memory, R_H + 8d floats, 16-byte
+// aligned); x, P: the component state (shared memory, updated in place, P = x + d,
+// 16-byte aligned); Rg: when non-null the global record (16-byte aligned) that
+// keeps this update for the reverse sweep
 template <int D>
 __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const float* Bj, const float* mj,
                            int n, const float2* z, float pd, float kappa, float* Rg, int lane) {
@@ -115,11 +120,10 @@ __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const 
   float* Kg = R + rec_Kg(d);
   float* W = R + rec_W(d);
   const bool rec = Rg != nullptr;
-  if (rec) {
-    float* Rx = Rg + rec_X(d);
-    float* RP = Rg + rec_Pin(d);
-    for (int i = lane; i < d; i += 32) Rx[i] = x[i];
-    for (int i = lane; i < d * d; i += 32) RP[i] = P[i];
+  if (rec) {   // x and P are contiguous, and so are their record copies (d % 4 == 0)
+    const float4* xP = reinterpret_cast<const float4*>(x);
+    float4* RxP = reinterpret_cast<float4*>(Rg + rec_X(d));
+    for (int i = lane; i < (d + d * d) / 4; i += 32) RxP[i] = xP[i];
   }
   float pt = 0.0f;
   if (lane < 3) {
@@ -205,8 +209,11 @@ __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const 
     R[R_E + lane] = e; R[R_BETA + lane] = beta;
   }
   __syncwarp();
-  if (rec)
-    for (int i = lane; i < rec_X(d); i += 32) Rg[i] = R[i];
+  if (rec) {
+    const float4* R4 = reinterpret_cast<const float4*>(R);
+    float4* G4 = reinterpret_cast<float4*>(Rg);
+    for (int i = lane; i < rec_X(d) / 4; i += 32) G4[i] = R4[i];
+  }
   __syncwarp();
   return logf(ell);
 }
@@ -431,9 +438,10 @@ __device__ float frame_forward(const MixArgs& A, float* scr, int SR, float* frg,
   for (int j = 0; j < J; ++j)
     ll += joint_fwd<D>(M, R, xk, Pk, Bm + j * 3 * d, mm + j * 3, s.cnt[j], s.det + j * kMixMaxC, pd, kappa,
                        cg ? cg + j * rec_size(d) : nullptr, lane);
-  if (cg) {
-    for (int i = lane; i < d; i += 32) cg[FL.comp_xk + i] = xk[i];
-    for (int i = lane; i < d * d; i += 32) cg[FL.comp_Pk + i] = Pk[i];
+  if (cg) {   // xk, Pk contiguous in the scratch and in the record (comp_Pk = comp_xk + d)
+    const float4* s4 = reinterpret_cast<const float4*>(xk);
+    float4* g4 = reinterpret_cast<float4*>(cg + FL.comp_xk);
+    for (int i = lane; i < (d + d * d) / 4; i += 32) g4[i] = s4[i];
   }
   if (lane == 0) s.l[k] = M.logpi[k] + ll;
   __syncthreads();
@@ -584,7 +592,13 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
   const float* mu = M.mu + k * d;
   const float* Lk = M.Lq + k * DD;
   float sbl = 0.0f;                                         // sigma adjoint, per lane
-  for (int i = lane; i < 2 * d + DD; i += 32) wb[WL.gmu + i] = 0.0f;
+  for (int i = lane; i < 2 * d + d * d; i += 32) wb[WL.gmu + i] = 0.0f;   // gmu, ga, Sq
+  // stage frame record fr's input state, mixture weights and collapsed mean
+  auto stage_frame = [&](const float* fr) {
+    for (int i = tid; i < d; i += TB) { s.xh[i] = fr[FL.xin + i]; s.xo[i] = fr[FL.xo + i]; }
+    for (int i = tid; i < d * d; i += TB) s.Ph[i] = fr[FL.Pin + i];
+    for (int i = tid; i < K; i += TB) s.w[i] = fr[FL.w + i];
+  };
   for (int b = blockIdx.x; b < A.n_tracks; b += gridDim.x) {
     const int T = A.n_frames[b];
     const long long g0 = A.frame_base[b];
@@ -615,13 +629,17 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
         for (int i = tid; i < d * d; i += TB) s.Ph[i] = s.Po[i];
         __syncthreads();
       }
-      // ---- reverse the segment
+      // ---- reverse the segment.  Four barriers a frame: the pass that sums
+      // frame t's per-component adjoints into Xb, Pb also stages frame t-1 and
+      // forms its symmetrised covariance adjoint Pcb from the same sums.
+      stage_frame(frames + (size_t)(t1 - 1 - t0) * FL.size);
+      for (int i = tid; i < d * d; i += TB) {
+        const int r = i / d, c = i - r * d;
+        s.Pcb[i] = 0.5f * (s.Pb[i] + s.Pb[c * d + r]);
+      }
+      __syncthreads();
       for (int t = t1 - 1; t >= t0; --t) {
         const float* fr = frames + (size_t)(t - t0) * FL.size;
-        // stage the frame's input state, mixture weights and collapsed mean
-        for (int i = tid; i < d; i += TB) { s.xh[i] = fr[FL.xin + i]; s.xo[i] = fr[FL.xo + i]; }
-        for (int i = tid; i < d * d; i += TB) s.Ph[i] = fr[FL.Pin + i];
-        for (int i = tid; i < K; i += TB) s.w[i] = fr[FL.w + i];
         const float* cb = fr + (size_t)k * FL.comp_size;
         const float* xin = s.xh;
         const float* Pin = s.Ph;
@@ -630,11 +648,6 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
         const float* Pk = cb + FL.comp_Pk;
         const float wk = fr[FL.w + k];
         // collapse reverse: P' = sym(sum w (P_k + D D^T)), x' = sum w x_k, softmax (dc = 1)
-        for (int i = tid; i < d * d; i += TB) {
-          const int r = i / d, c = i - r * d;
-          s.Pcb[i] = 0.5f * (s.Pb[i] + s.Pb[c * d + r]);
-        }
-        __syncthreads();
         float* Dkb = wb + WL.Dkb;
         if (lane < d) {
           float v = 0.0f;
@@ -642,14 +655,15 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
           Dkb[lane] = 2.0f * wk * v;
         }
         __syncthreads();
-        for (int r = tid; r < d; r += TB) {
-          float v = s.Xb[r];
+        // xt = Xb - sum_q Dkb_q: every warp forms its own copy (lane r), in the same order
+        float xt = 0.0f;
+        if (lane < d) {
+          float v = s.Xb[lane];
 #pragma unroll 4
-          for (int q = 0; q < K; ++q) v -= wbase[(size_t)q * WL.size + WL.Dkb + r];
-          s.xt[r] = v;
+          for (int q = 0; q < K; ++q) v -= wbase[(size_t)q * WL.size + WL.Dkb + lane];
+          xt = v;
         }
-        __syncthreads();
-        float wbp = (lane < d) ? xk[lane] * s.xt[lane] : 0.0f;
+        float wbp = (lane < d) ? xk[lane] * xt : 0.0f;
         for (int i = lane; i < d * d; i += 32) {
           const int r = i / d, c = i - r * d;
           wbp = fmaf(s.Pcb[i], Pk[i] + (xk[r] - xo[r]) * (xk[c] - xo[c]), wbp);
@@ -657,19 +671,15 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
         const float wbk = wsum(wbp);
         if (lane == 0) s.wb[k] = wbk;
         __syncthreads();
-        if (k == 0) {
-          const float v = lane < K ? s.w[lane] * s.wb[lane] : 0.0f;
-          const float sw = wsum(v);
-          if (lane == 0) s.red[1] = sw;
-        }
-        __syncthreads();
-        const float lb = wk * (wbk - s.red[1]) + wk;
+        // sum_q w_q wb_q, formed by every warp in the same order
+        const float swb = wsum(lane < K ? s.w[lane] * s.wb[lane] : 0.0f);
+        const float lb = wk * (wbk - swb) + wk;
         float* xb = wb + WL.xb;
         float* Pb = wb + WL.Pb;
         float* Xin = wb + WL.Xin;
         float* Pinb = wb + WL.Pin;
         if (wk > 0.0f) {
-          if (lane < d) xb[lane] = Dkb[lane] + wk * s.xt[lane];
+          if (lane < d) xb[lane] = Dkb[lane] + wk * xt;
           for (int i = lane; i < d * d; i += 32) Pb[i] = wk * s.Pcb[i];
           __syncwarp();
           // each joint's record is copied (coalesced, 16 bytes per lane and step)
@@ -685,10 +695,11 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
             joint_bwd<D>(M, Rs, Bm + j * 3 * d, pd, kappa, xb, Pb, lb, wb + WL.tmp, sbl, lane);
             __syncwarp();
           }
-          // predict reverse: x = a*xin + (1-a)*mu ; P = A Pin A + Q
+          // predict reverse: x = a*xin + (1-a)*mu ; P = A Pin A + Q (Q = L L^T: its
+          // adjoint Pb is summed here and turned into the L adjoint once a segment)
           float* gmu = wb + WL.gmu;
           float* ga = wb + WL.ga;
-          float* gL = wb + WL.gL;
+          float* Sq = wb + WL.Sq;
           if (lane < d) {
             Xin[lane] = a[lane] * xb[lane];
             gmu[lane] += (1.0f - a[lane]) * xb[lane];
@@ -700,15 +711,7 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
           for (int i = lane; i < d * d; i += 32) {
             const int r = i / d, c = i - r * d;
             Pinb[i] = a[r] * a[c] * Pb[i];
-          }
-          for (int i = lane; i < DD; i += 32) {
-            int r = (int)((sqrtf(8.0f * i + 1.0f) - 1.0f) * 0.5f);
-            while (r * (r + 1) / 2 > i) --r;
-            while ((r + 1) * (r + 2) / 2 <= i) ++r;
-            const int c = i - r * (r + 1) / 2;
-            float g = 0.0f;
-            for (int t2 = c; t2 < d; ++t2) g = fmaf(Pb[r * d + t2] + Pb[t2 * d + r], Lk[t2 * (t2 + 1) / 2 + c], g);
-            gL[i] += g;
+            Sq[i] += Pb[i];
           }
         } else {
           if (lane < d) Xin[lane] = 0.0f;
@@ -726,16 +729,37 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
 #pragma unroll 4
           for (int q = 0; q < K; ++q) v += wbase[(size_t)q * WL.size + WL.Pin + i];
           s.Pb[i] = v;
+          if (t > t0) {   // the transposed entry's sum, in the same order, for Pcb of frame t-1
+            const int r = i / d, c = i - r * d;
+            float vt = 0.0f;
+#pragma unroll 4
+            for (int q = 0; q < K; ++q) vt += wbase[(size_t)q * WL.size + WL.Pin + c * d + r];
+            s.Pcb[i] = 0.5f * (v + vt);
+          }
         }
+        if (t > t0) stage_frame(fr - FL.size);
         __syncthreads();
       }
-      // flush this segment's FP32 parameter adjoints into the CTA's FP64 accumulators
+      // flush this segment's FP32 parameter adjoints into the CTA's FP64
+      // accumulators; the L_Q adjoint is tril((Sq + Sq^T) L_Q)
       for (int i = lane; i < d; i += 32) {
         gacc[k * d + i] += (double)wb[WL.gmu + i];
         gacc[K * d + k * d + i] += (double)wb[WL.ga + i];
       }
-      for (int i = lane; i < DD; i += 32) gacc[2 * K * d + k * DD + i] += (double)wb[WL.gL + i];
-      for (int i = lane; i < 2 * d + DD; i += 32) wb[WL.gmu + i] = 0.0f;
+      {
+        const float* Sq = wb + WL.Sq;
+        for (int i = lane; i < DD; i += 32) {
+          int r = (int)((sqrtf(8.0f * i + 1.0f) - 1.0f) * 0.5f);
+          while (r * (r + 1) / 2 > i) --r;
+          while ((r + 1) * (r + 2) / 2 <= i) ++r;
+          const int c = i - r * (r + 1) / 2;
+          float g = 0.0f;
+          for (int t2 = c; t2 < d; ++t2) g = fmaf(Sq[r * d + t2] + Sq[t2 * d + r], Lk[t2 * (t2 + 1) / 2 + c], g);
+          gacc[2 * K * d + k * DD + i] += (double)g;
+        }
+      }
+      __syncwarp();
+      for (int i = lane; i < 2 * d + d * d; i += 32) wb[WL.gmu + i] = 0.0f;
       __syncthreads();
     }
     // prior: x = sum pi mu, P = sum pi (S0 + D D^T)
