@@ -411,3 +411,34 @@ def test_blur_oracle_against_float64_convolution(olib):
     cand = np.array([[0.0, 5.0], [10.5, 7.9], [63.99, 47.5], [64.0, 1.0], [3.0, -1.0]])
     L = olib.image_lookup(cand, out)
     np.testing.assert_array_equal(L, [0.0, out[7, 10] / 255.0, out[47, 63] / 255.0, 0.0, 0.0])
+
+
+# ----------------------------------------------------------------- mixture KF (A11)
+def test_mixkf_oracle_adjoint_against_central_differences(olib):
+    """The FP64 CPU adjoint of the mixture-KF log-likelihood (the GPU adjoint's
+    checker) against FP64 central differences of the FP64 forward, per
+    parameter block (mu, a, L_Q, sigma) and along random directions."""
+    from mkfbodytracker_pdaf_gb300 import synth
+    b = synth.make_mix_batch(9, 3, 14, K=3, d=12)
+    tt = b.theta_true()
+    om = olib.MixModel(tt["mu"], tt["a"], tt["Lq"], tt["sigma"], tt["pi"], tt["S0"])
+    th = om.theta()
+    L, ll, g = olib.mix_batch(om, b, grad=True)
+    assert np.isfinite(L) and np.all(np.isfinite(g))
+    np.testing.assert_allclose(ll.sum(), L, rtol=1e-12)
+    K, d = 3, 12
+    blocks = [slice(0, K * d), slice(K * d, 2 * K * d), slice(2 * K * d, th.size - 1), slice(th.size - 1, th.size)]
+    rng = np.random.default_rng(11)
+    dirs = []
+    for sl in blocks:
+        v = np.zeros(th.size)
+        v[sl] = rng.standard_normal(v[sl].size)
+        dirs.append(v)
+    dirs += [rng.standard_normal(th.size) for _ in range(3)]
+    for v in dirs:
+        v = v / np.linalg.norm(v)
+        h = 1e-6 * max(1.0, np.abs(th).max())
+        Lp, _ = olib.mix_batch(om.with_theta(th + h * v), b)
+        Lm, _ = olib.mix_batch(om.with_theta(th - h * v), b)
+        fd = (Lp - Lm) / (2 * h)
+        assert abs(v @ g - fd) <= 1e-6 * max(1.0, abs(fd)), (v @ g, fd)
