@@ -173,7 +173,8 @@ typedef struct mkf_bpf_batch* mkf_bpf_batch_t;
  * det[det_off[g*J+j] .. det_off[g*J+j+1]). */
 int mkf_bpf_batch_create(const mkf_bpf_models* models, int n_tracks, const mkf_bpf_track* tracks,
                          int64_t n_frames_total, mkf_bpf_batch_t* out);
-/* tuning: threads per CTA (64..512, multiple of 32) and CTAs per SM (0 = max).
+/* tuning: threads per CTA (64..512, multiple of 32) and CTAs per SM (0 = max);
+ * default 256 threads, 3 CTAs per SM, variant VEC_LOADS | SEARCH | LOWSMEM.
  * Launch bounds of VEC_LOADS | SEARCH (with or without LOWSMEM): <= 256
  * threads at 2 CTAs per SM (3 when ctas_per_sm >= 3), 257..384 threads at 2,
  * 385..512 threads at 1; of the other variants: <= 256 threads at 2, 257..512

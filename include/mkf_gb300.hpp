@@ -14,6 +14,8 @@
 //   PFTracker::getMeasurementProposal + update      mkf::PoseTracker::stepImage (likelihood
 //     (pfPose.cpp:210-329, 332-385)                  image) / ::step (detection list)
 //   get3Dpose / publish2Dpos (pfPose.cpp:93-208)     mkf::PoseDecoder
+//   (no counterpart: one tracker per arm)            mkf::BatchedBootstrapPF (thousands of
+//                                                      uneven tracks in one persistent launch)
 //
 // Errors: every non-MKF_OK status becomes an mkf::Error carrying the status and
 // mkf_last_error().  Handles are move-only RAII owners.  Device buffers are
@@ -298,6 +300,58 @@ class PoseDecoder {
   DeviceArray<int> status_;
   double Kc_[9];
   cudaStream_t stream_;
+};
+
+// ---------------------------------------- batched bootstrap PFs, one launch
+// Independent bootstrap trackers (the pf2D structure, pf2D.cpp:148-210, with
+// the mixture motion model of my_gmm) of uneven length, particle count and
+// clutter, all run by one persistent kernel.  Track b's frames are the global
+// frames [frame_base, frame_base + n_frames); detections are per (global frame,
+// joint) lists, det_off (n_frames_total * J + 1 offsets) into det (x, y pairs).
+class BatchedBootstrapPF {
+ public:
+  BatchedBootstrapPF(const mkf_bpf_models& models, const std::vector<mkf_bpf_track>& tracks, int64_t n_frames_total)
+      : d(models.d), J(models.J), n_tracks(static_cast<int>(tracks.size())), n_frames_total(n_frames_total) {
+    check(mkf_bpf_batch_create(&models, n_tracks, tracks.data(), n_frames_total, &h_), "mkf_bpf_batch_create");
+  }
+  ~BatchedBootstrapPF() { if (h_) mkf_bpf_batch_destroy(h_); }
+  BatchedBootstrapPF(const BatchedBootstrapPF&) = delete;
+  BatchedBootstrapPF& operator=(const BatchedBootstrapPF&) = delete;
+  // launch shape and code variant (MKF_BPF_*); the defaults are the fastest measured
+  void setTuning(int block_threads, int ctas_per_sm) {
+    check(mkf_bpf_batch_set_tuning(h_, block_threads, ctas_per_sm), "mkf_bpf_batch_set_tuning");
+  }
+  void setVariant(int flags) { check(mkf_bpf_batch_set_variant(h_, flags), "mkf_bpf_batch_set_variant"); }
+  // device buffers: est (n_frames_total * d), loglik and ess (n_frames_total),
+  // status (n_tracks); asynchronous on the stream
+  void run(const int* d_det_off, const float* d_det, float* d_est, float* d_loglik, float* d_ess, int* d_status,
+           cudaStream_t stream = nullptr) {
+    check(mkf_bpf_batch_run(h_, d_det_off, d_det, d_est, d_loglik, d_ess, d_status, stream), "mkf_bpf_batch_run");
+  }
+  // host buffers (copied in and out, synchronous); outputs are resized
+  void run(const std::vector<int>& det_off, const std::vector<float>& det, std::vector<float>& est,
+           std::vector<float>& loglik, std::vector<float>& ess, std::vector<int>& status,
+           cudaStream_t stream = nullptr) {
+    const size_t G = static_cast<size_t>(n_frames_total);
+    if (det_off.size() != G * J + 1 || det.size() % 2)
+      throw Error(MKF_ERR_ARG, "BatchedBootstrapPF::run: det_off needs n_frames_total * J + 1 entries, det pairs");
+    est.resize(G * d); loglik.resize(G); ess.resize(G); status.resize(static_cast<size_t>(n_tracks));
+    static const float no_det[2] = {0.0f, 0.0f};
+    check(mkf_bpf_batch_run_host(h_, det_off.data(), det.empty() ? no_det : det.data(),
+                                 static_cast<int64_t>(det.size() / 2), est.data(),
+                                 loglik.data(), ess.data(), status.data(), stream),
+          "mkf_bpf_batch_run_host");
+  }
+  int lastGrid() const {
+    int g = 0;
+    check(mkf_bpf_batch_last_grid(h_, &g), "mkf_bpf_batch_last_grid");
+    return g;
+  }
+  const int d, J, n_tracks;
+  const int64_t n_frames_total;
+
+ private:
+  mkf_bpf_batch_t h_ = nullptr;
 };
 
 }  // namespace mkf

@@ -1317,7 +1317,8 @@ extern "C" int mkf_bpf_batch_create(const mkf_bpf_models* models, int n_tracks, 
   if (st) { free_models(B->m); delete B; return st; }
   B->n_tracks = n_tracks; B->Nmax = (Nmax + 31) & ~31; B->d = models->d; B->K = models->K; B->J = models->J;
   B->G = n_frames_total;
-  B->tb = 256; B->ctas_per_sm = 0; B->variant = MKF_BPF_VEC_LOADS;
+  // the fastest shape measured on GB300 for the uneven-track workload
+  B->tb = 256; B->ctas_per_sm = 3; B->variant = MKF_BPF_VEC_LOADS | MKF_BPF_SEARCH | MKF_BPF_LOWSMEM;
   B->dbg_track = -1;
   std::vector<int4> meta(n_tracks);
   std::vector<long long> fb(n_tracks);
