@@ -73,17 +73,16 @@ static int build_models(const mkf_bpf_models* M, DevModels& out) {
   out.n = n; out.d = d; out.K = K; out.J = J; out.diag = diag;
   out.fx = M->fx; out.fy = M->fy; out.cx = M->cx; out.cy = M->cy;
   auto vec = [](const float* p, size_t cnt) { return std::vector<float>(p, p + cnt); };
-  int st;
-  if ((st = upload(&out.a, vec(M->a, nKd)))) return st;
-  if ((st = upload(&out.mb, mb))) return st;
-  if ((st = upload(&out.mu, vec(M->mu, nKd)))) return st;
-  if ((st = upload(&out.Lq, vec(M->Lq, (size_t)n * K * DD)))) return st;
-  if ((st = upload(&out.Ld, Ld))) return st;
-  if ((st = upload(&out.S0c, vec(M->S0c, (size_t)n * K * DD)))) return st;
-  if ((st = upload(&out.cumpi, cum))) return st;
-  if ((st = upload(&out.Bm, vec(M->Bm, (size_t)n * J * 3 * d)))) return st;
-  if ((st = upload(&out.mm, vec(M->mm, (size_t)n * J * 3)))) return st;
-  return MKF_OK;
+  int st = upload(&out.a, vec(M->a, nKd));   // stops at the first failure
+  if (st == MKF_OK) st = upload(&out.mb, mb);
+  if (st == MKF_OK) st = upload(&out.mu, vec(M->mu, nKd));
+  if (st == MKF_OK) st = upload(&out.Lq, vec(M->Lq, (size_t)n * K * DD));
+  if (st == MKF_OK) st = upload(&out.Ld, Ld);
+  if (st == MKF_OK) st = upload(&out.S0c, vec(M->S0c, (size_t)n * K * DD));
+  if (st == MKF_OK) st = upload(&out.cumpi, cum);
+  if (st == MKF_OK) st = upload(&out.Bm, vec(M->Bm, (size_t)n * J * 3 * d));
+  if (st == MKF_OK) st = upload(&out.mm, vec(M->mm, (size_t)n * J * 3));
+  return st;
 }
 
 // ------------------------------------------------------------------ per-particle math

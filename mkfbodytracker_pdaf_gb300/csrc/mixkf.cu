@@ -922,7 +922,6 @@ static int mix_grid(mkf_mixkf* h) {
   const int d = h->d, K = h->K;
   // the reverse sweep stages one joint record in a warp's forward scratch
   if (rec_size(d) > fwd_scratch_floats(d)) { set_error("mkf_mixkf: record larger than the warp scratch"); return MKF_ERR_ARG; }
-  const FrameLayout FL = frame_layout(d, K, h->J);
   const WorkLayout WL = work_layout(d);
   const size_t base = mix_smem_bytes(d);
   const int SRf = fwd_scratch_floats(d);
