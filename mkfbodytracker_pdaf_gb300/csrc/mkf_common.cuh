@@ -46,7 +46,9 @@ struct NvtxRange {
 struct u32x4 { uint32_t x, y, z, w; };
 
 MKF_HD u32x4 philox4x32_10(u32x4 c, uint32_t k0, uint32_t k1) {
+#ifdef __CUDA_ARCH__
 #pragma unroll
+#endif
   for (int r = 0; r < 10; ++r) {
     if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
 #ifdef __CUDA_ARCH__
