@@ -170,7 +170,8 @@ int mkf_bpf_graph_destroy(mkf_bpf_graph_t g);
 typedef struct mkf_bpf_batch* mkf_bpf_batch_t;
 /* tracks: n_tracks descriptors; n_frames_total = sum of n_frames (global frame
  * index space); detections are per (global frame g, joint j) lists
- * det[det_off[g*J+j] .. det_off[g*J+j+1]). */
+ * det[det_off[g*J+j] .. det_off[g*J+j+1]).  The offsets are int32, so one run
+ * holds at most 2^31 - 1 detections. */
 int mkf_bpf_batch_create(const mkf_bpf_models* models, int n_tracks, const mkf_bpf_track* tracks,
                          int64_t n_frames_total, mkf_bpf_batch_t* out);
 /* tuning: threads per CTA (64..512, multiple of 32) and CTAs per SM (0 = max);

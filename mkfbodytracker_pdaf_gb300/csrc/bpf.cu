@@ -1480,6 +1480,7 @@ extern "C" int mkf_bpf_batch_run_host(mkf_bpf_batch_t B, const int* det_off, con
                                       mkf_stream_t stream) {
   MKF_RANGE("mkf_bpf_batch_run_host");
   MKF_ARG(B && det_off && det && est && loglik && ess && status && n_det >= 0, "mkf_bpf_batch_run_host: null argument");
+  MKF_ARG(n_det <= 0x7FFFFFFFLL, "mkf_bpf_batch_run_host: more than 2^31 - 1 detections (int32 offsets)");
   cudaStream_t s = (cudaStream_t)stream;
   const size_t G = (size_t)B->G, J = (size_t)B->J, d = (size_t)B->d;
   if (!B->h_det_off_dev) {
