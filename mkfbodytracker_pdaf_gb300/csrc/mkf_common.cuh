@@ -265,9 +265,12 @@ __device__ __forceinline__ int resample_fallback_index(uint32_t U, int i, int L)
   u32x4 o = philox4x32_10(u32x4{(uint32_t)i, 0u, 0u, 0u}, U, 0x5EEDu);
   return (int)(((uint64_t)o.x * (uint64_t)L) >> 32);
 }
-// The same rule with 64-bit thresholds: target i takes the first j whose
-// inclusive prefix Q_j >= T_i = ceil((i 2^32 + U) Qt / (N 2^32)), the 128-bit
-// comparison N Q_j 2^32 >= (i 2^32 + U) Qt restated exactly.  With
+#endif  // __CUDACC__
+
+// The same rule with 64-bit thresholds (integer only, host and device): target
+// i takes the first j whose inclusive prefix Q_j >= T_i = ceil((i 2^32 + U) Qt /
+// (N 2^32)), the 128-bit comparison N Q_j 2^32 >= (i 2^32 + U) Qt restated
+// exactly.  With
 // Qt = A N + r and floor(U Qt / 2^32) = C N + s, and V_i = i r + s:
 //   T_i = i A + C + floor(V_i / N) + [V_i mod N > 0 or (U Qt mod 2^32) > 0].
 // Needs N <= 65536 (V_i < N^2 fits 32 bits) and i A + C < 2^64.
@@ -294,10 +297,11 @@ MKF_HD uint64_t rs_threshold(const RsThresh& t, uint32_t i) {
   const uint32_t g = V / t.N, h = V - g * t.N;
   return (uint64_t)i * t.A + t.C + g + (((h | t.low) != 0u) ? 1u : 0u);
 }
+
+#ifdef __CUDACC__
 // The same threshold for any N <= 2^22 (V_i < 2^45): floor(V_i / N) from a
 // float estimate (relative error <= 4 2^-24, so within one of the truth) and
 // exact integer correction.
-#ifdef __CUDACC__
 __device__ __forceinline__ uint64_t rs_threshold64(const RsThresh& t, uint32_t i) {
   const uint64_t V = (uint64_t)i * t.r + t.s;
   // float(V) from two 32-bit conversions (V < 2^45); the 64-bit one runs on the FP64 pipe
@@ -312,7 +316,6 @@ __device__ __forceinline__ uint64_t rs_threshold64(const RsThresh& t, uint32_t i
     if (h >= (long long)t.N) { ++g; h -= t.N; }
   return (uint64_t)i * t.A + t.C + g + (((h != 0) || (t.low != 0u)) ? 1u : 0u);
 }
-#endif
 
 // First j in [0, n) with Q[j] >= T (Q nondecreasing) for G targets at once: a
 // branch-free lower bound whose halving steps depend on n only, so the G
