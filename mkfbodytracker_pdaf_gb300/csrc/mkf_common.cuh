@@ -1,6 +1,7 @@
 // mkf_common.cuh -- shared device/host pieces of the GB300 filtering hot path.
 #pragma once
 #include <cuda_runtime.h>
+#include <math.h>
 #include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 #include <string>
@@ -297,26 +298,27 @@ MKF_HD uint64_t rs_threshold(const RsThresh& t, uint32_t i) {
   const uint32_t g = V / t.N, h = V - g * t.N;
   return (uint64_t)i * t.A + t.C + g + (((h | t.low) != 0u) ? 1u : 0u);
 }
-
-#ifdef __CUDACC__
 // The same threshold for any N <= 2^22 (V_i < 2^45): floor(V_i / N) from a
 // float estimate (relative error <= 4 2^-24, so within one of the truth) and
 // exact integer correction.
-__device__ __forceinline__ uint64_t rs_threshold64(const RsThresh& t, uint32_t i) {
+MKF_HD uint64_t rs_threshold64(const RsThresh& t, uint32_t i) {
   const uint64_t V = (uint64_t)i * t.r + t.s;
   // float(V) from two 32-bit conversions (V < 2^45); the 64-bit one runs on the FP64 pipe
   const float vf = fmaf((float)(uint32_t)(V >> 20), 1048576.0f, (float)(uint32_t)(V & 0xFFFFFu));
+#ifdef __CUDA_ARCH__
   uint32_t g = __float2uint_rz(vf * t.invN);
+#else
+  uint32_t g = (uint32_t)(vf * t.invN);   // truncation, as __float2uint_rz
+#endif
   long long h = (long long)V - (long long)g * (long long)t.N;
-#pragma unroll
   for (int k = 0; k < 2; ++k)
     if (h < 0) { --g; h += t.N; }
-#pragma unroll
   for (int k = 0; k < 2; ++k)
     if (h >= (long long)t.N) { ++g; h -= t.N; }
   return (uint64_t)i * t.A + t.C + g + (((h != 0) || (t.low != 0u)) ? 1u : 0u);
 }
 
+#ifdef __CUDACC__
 // First j in [0, n) with Q[j] >= T (Q nondecreasing) for G targets at once: a
 // branch-free lower bound whose halving steps depend on n only, so the G
 // searches run interleaved.  Needs

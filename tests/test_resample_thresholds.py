@@ -25,5 +25,5 @@ def test_rs_threshold_matches_128_bit_rule(tmp_path):
     subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "mkfbodytracker_pdaf_gb300", "csrc"),
                     "-I", inc, src, "-o", exe], check=True)
     bad, n = map(int, subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split())
-    assert n > 200000
+    assert n > 400000
     assert bad == 0, "%d of %d thresholds differ from the 128-bit rule" % (bad, n)
