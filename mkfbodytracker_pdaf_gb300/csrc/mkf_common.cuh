@@ -4,10 +4,17 @@
 #include <math.h>
 #include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
+#include <string.h>
 #include <string>
 #include "../../include/mkf_gb300.h"
 
 #define MKF_HD __host__ __device__ __forceinline__
+// loop unrolling in host-and-device functions (the host compiler has no such pragma)
+#ifdef __CUDA_ARCH__
+#define MKF_UNROLL _Pragma("unroll")
+#else
+#define MKF_UNROLL
+#endif
 
 namespace mkf {
 
@@ -47,9 +54,7 @@ struct NvtxRange {
 struct u32x4 { uint32_t x, y, z, w; };
 
 MKF_HD u32x4 philox4x32_10(u32x4 c, uint32_t k0, uint32_t k1) {
-#ifdef __CUDA_ARCH__
-#pragma unroll
-#endif
+  MKF_UNROLL
   for (int r = 0; r < 10; ++r) {
     if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
 #ifdef __CUDA_ARCH__
@@ -234,16 +239,6 @@ constexpr int kQBits = 40;
 __device__ __forceinline__ uint64_t quantize_f32(float w, int e) {
   return (w > 0.0f) ? (uint64_t)__float2ull_rz(ldexpf(w, kQBits - e)) : 0ull;
 }
-// quantize_f32(w, 1) for a weight normalised to max 1, without the 64-bit
-// conversion (which runs on GB300's small FP64 pipe): floor(w 2^39) from the
-// float's fields with integer shifts; 0 for zero, negative, NaN and subnormal w
-__device__ __forceinline__ uint64_t quantize39(float w) {
-  const uint32_t b = __float_as_uint(w);
-  const int e = (int)(b >> 23) - 111;
-  const uint64_t m = (uint64_t)((b & 0x7FFFFFu) | 0x800000u);
-  const uint64_t q = e >= 0 ? (m << e) : (e > -24 ? (m >> -e) : 0ull);
-  return (w > 0.0f) ? q : 0ull;
-}
 __device__ __forceinline__ uint64_t quantize_f64(double w, int e) {
   return (w > 0.0) ? (uint64_t)__double2ull_rz(ldexp(w, kQBits - e)) : 0ull;
 }
@@ -318,27 +313,44 @@ MKF_HD uint64_t rs_threshold64(const RsThresh& t, uint32_t i) {
   return (uint64_t)i * t.A + t.C + g + (((h != 0) || (t.low != 0u)) ? 1u : 0u);
 }
 
-#ifdef __CUDACC__
+// quantize_f32(w, 1) (the device's 64-bit conversion path) for a weight
+// normalised to max 1 (w <= 1), without the 64-bit conversion (which runs on
+// GB300's small FP64 pipe): floor(w 2^39) from the float's fields with integer
+// shifts; 0 for zero, negative, NaN and subnormal w
+MKF_HD uint64_t quantize39(float w) {
+#ifdef __CUDA_ARCH__
+  const uint32_t b = __float_as_uint(w);
+#else
+  uint32_t b;
+  memcpy(&b, &w, sizeof(b));
+  if (!(w > 0.0f)) b = 0;   // keeps the host's shifts in range (the device's shl clamps)
+#endif
+  const int e = (int)(b >> 23) - 111;
+  const uint64_t m = (uint64_t)((b & 0x7FFFFFu) | 0x800000u);
+  const uint64_t q = e >= 0 ? (m << e) : (e > -24 ? (m >> -e) : 0ull);
+  return (w > 0.0f) ? q : 0ull;
+}
+
 // First j in [0, n) with Q[j] >= T (Q nondecreasing) for G targets at once: a
 // branch-free lower bound whose halving steps depend on n only, so the G
-// searches run interleaved.  Needs
-// T[g] <= Q[n-1].
+// searches run interleaved.  Needs T[g] <= Q[n-1] (else the result is n).
 template <int G>
-__device__ __forceinline__ void search_u64_multi(const uint64_t* Q, int n, const uint64_t* T, int* out) {
+MKF_HD void search_u64_multi(const uint64_t* Q, int n, const uint64_t* T, int* out) {
   int base[G];
-#pragma unroll
+  MKF_UNROLL
   for (int g = 0; g < G; ++g) base[g] = 0;
   int len = n;
   while (len > 1) {
     const int half = len >> 1;
-#pragma unroll
+    MKF_UNROLL
     for (int g = 0; g < G; ++g) base[g] = (Q[base[g] + half] < T[g]) ? base[g] + half : base[g];
     len -= half;
   }
-#pragma unroll
+  MKF_UNROLL
   for (int g = 0; g < G; ++g) out[g] = base[g] + ((Q[base[g]] < T[g]) ? 1 : 0);
 }
 
+#ifdef __CUDACC__
 // number of targets i in [0, N) with (i 2^32 + U) Qt <= N X 2^32
 __device__ __forceinline__ int count_targets_le(uint64_t X, int N, uint32_t U, uint64_t Qt) {
   const unsigned __int128 lim = ((unsigned __int128)(uint64_t)N * (unsigned __int128)X) << 32;

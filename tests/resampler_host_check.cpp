@@ -1,0 +1,114 @@
+// The integer pieces of the exact resampler, from mkf_common.cuh compiled here
+// for the host, against independent restatements:
+//  - thresholds: rs_thresh_setup with rs_threshold (N <= 65536) and
+//    rs_threshold64 (N <= 2^22) against T_i = ceil((i 2^32 + U) Qt / (N 2^32))
+//    in 128-bit integers; random N, Qt in [1, 2^62) (at most 2^22 weights of
+//    40 bits each), U and i, plus the extremes of each;
+//  - quantize: quantize39(w) against floor(w 2^39) in double (exact: a float
+//    times a power of two) for weights w <= 1 (its domain): random, boundary,
+//    subnormal, zero, negative, -inf and NaN;
+//  - search: search_u64_multi<4> against std::lower_bound on random
+//    nondecreasing prefix arrays (with runs of equal values) of 1 .. 2^22 entries.
+// Prints one "name mismatches cases" line per piece.
+#include "mkf_common.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <limits>
+#include <random>
+#include <vector>
+
+static bool check(uint64_t Qt, int N, uint32_t U, uint32_t i) {
+  const mkf::RsThresh th = mkf::rs_thresh_setup(Qt, N, U);
+  const unsigned __int128 num = ((((unsigned __int128)i) << 32) + U) * (unsigned __int128)Qt;
+  const unsigned __int128 den = ((unsigned __int128)(uint64_t)N) << 32;
+  const unsigned __int128 ref = (num + den - 1) / den;
+  bool ok = mkf::rs_threshold64(th, i) == (uint64_t)ref && ref >> 64 == 0;
+  if (N <= 65536) ok = ok && mkf::rs_threshold(th, i) == (uint64_t)ref;
+  return ok;
+}
+
+static void thresholds(std::mt19937_64& rng) {
+  long long bad = 0, n = 0;
+  for (int it = 0; it < 400000; ++it) {
+    const int N = 1 + (int)(rng() % (it & 1 ? 65536 : 4194304));
+    const uint64_t Qt = 1 + (rng() >> (2 + rng() % 60));
+    const uint32_t U = (uint32_t)rng();
+    const uint32_t i = (uint32_t)(rng() % N);
+    bad += !check(Qt, N, U, i);
+    ++n;
+  }
+  const int Ns[] = {1, 2, 3, 255, 256, 4097, 65535, 65536, 65537, 1048575, 4194303, 4194304};
+  const uint64_t Qs[] = {1, 2, 3, (1ull << 40) - 1, 1ull << 40, (1ull << 62) - 1};
+  const uint32_t Us[] = {0u, 1u, 0x80000000u, 0xFFFFFFFFu};
+  for (int N : Ns)
+    for (uint64_t Qt : Qs)
+      for (uint32_t U : Us)
+        for (uint32_t i : {0u, 1u, (uint32_t)N / 2, (uint32_t)N - 1}) {
+          if (i >= (uint32_t)N) continue;
+          bad += !check(Qt, N, U, i);
+          ++n;
+        }
+  std::printf("thresholds %lld %lld\n", bad, n);
+}
+
+static uint64_t quantize_ref(float w) {
+  if (!(w > 0.0f) || !std::isfinite(w) || w < std::numeric_limits<float>::min()) return 0;
+  return (uint64_t)std::floor(std::ldexp((double)w, 39));
+}
+
+static void quantize(std::mt19937_64& rng) {
+  long long bad = 0, n = 0;
+  std::uniform_real_distribution<float> u01(0.0f, 1.0f);
+  std::vector<float> ws = {0.0f, -0.0f, 1.0f, -1.0f, 0.5f, std::nextafter(1.0f, 0.0f),
+                           std::ldexp(1.0f, -39), std::ldexp(1.0f, -40), std::ldexp(1.5f, -39),
+                           std::ldexp(1.0f, -63), std::ldexp(1.0f, -126), std::ldexp(1.0f, -130),
+                           -std::numeric_limits<float>::infinity(), std::numeric_limits<float>::quiet_NaN()};
+  for (int k = 0; k < 1000000; ++k) {
+    const float w = u01(rng);
+    ws.push_back(k & 1 ? w : std::ldexp(w, -(int)(rng() % 64)));
+  }
+  for (float w : ws) {
+    bad += mkf::quantize39(w) != quantize_ref(w);
+    ++n;
+  }
+  std::printf("quantize %lld %lld\n", bad, n);
+}
+
+static void search(std::mt19937_64& rng) {
+  long long bad = 0, n = 0;
+  for (int it = 0; it < 400; ++it) {
+    const int len = 1 + (int)(rng() % (it < 100 ? 64 : it < 390 ? 65536 : 4194304));
+    std::vector<uint64_t> Q(len);
+    uint64_t acc = 0;
+    for (int j = 0; j < len; ++j) {
+      acc += (rng() % 4 == 0) ? 0 : (rng() >> 30);     // runs of equal prefix values
+      Q[j] = acc;
+    }
+    for (int k = 0; k < 256; ++k) {
+      uint64_t T[4];
+      int out[4];
+      for (int g = 0; g < 4; ++g) {
+        const int pick = (int)(rng() % len);
+        T[g] = (rng() & 1) ? Q[pick] : (Q[pick] == 0 ? 0 : Q[pick] - rng() % (Q[pick] + 1) / 2);
+        if (T[g] > Q[len - 1]) T[g] = Q[len - 1];
+      }
+      mkf::search_u64_multi<4>(Q.data(), len, T, out);
+      for (int g = 0; g < 4; ++g) {
+        const int ref = (int)(std::lower_bound(Q.begin(), Q.end(), T[g]) - Q.begin());
+        bad += out[g] != ref;
+        ++n;
+      }
+    }
+  }
+  std::printf("search %lld %lld\n", bad, n);
+}
+
+int main() {
+  std::mt19937_64 rng(20140601);
+  thresholds(rng);
+  quantize(rng);
+  search(rng);
+  return 0;
+}

@@ -1,0 +1,36 @@
+"""The integer pieces of the exact resampler that every GPU resampling kernel
+shares (64-bit thresholds, weight quantisation by bit fields, the interleaved
+branch-free search), compiled for the host from the kernels' own header and
+checked against independent restatements (tests/resampler_host_check.cpp)."""
+import os
+import shutil
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _cuda_include():
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    inc = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "include")
+    return inc if os.path.exists(os.path.join(inc, "cuda_runtime.h")) else None
+
+
+@pytest.fixture(scope="module")
+def results(tmp_path_factory):
+    inc = _cuda_include()
+    if inc is None or shutil.which("g++") is None:
+        pytest.skip("needs g++ and the CUDA headers")
+    exe = str(tmp_path_factory.mktemp("rh") / "resampler_host_check")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "mkfbodytracker_pdaf_gb300", "csrc"),
+                    "-I", inc, os.path.join(ROOT, "tests", "resampler_host_check.cpp"), "-o", exe], check=True)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+    return {name: (int(bad), int(n)) for name, bad, n in (line.split() for line in out.strip().splitlines())}
+
+
+@pytest.mark.parametrize("piece,min_cases", [("thresholds", 400000), ("quantize", 1000000), ("search", 400000)])
+def test_against_independent_restatement(results, piece, min_cases):
+    bad, n = results[piece]
+    assert n >= min_cases
+    assert bad == 0, "%s: %d of %d cases differ" % (piece, bad, n)
