@@ -94,39 +94,10 @@ struct PView {
   float fx, fy, cx, cy;
 };
 
-// first k with u < cumpi[k] (the last component if none): with cumpi
-// nondecreasing that is the number of c < K-1 with cumpi[c] <= u, counted with
-// independent loads instead of a dependent walk
-__device__ __forceinline__ int pick_component(const float* cumpi, int K, float u) {
-  int k = 0;
-  for (int c = 0; c < K - 1; ++c) k += (u >= cumpi[c]) ? 1 : 0;
-  return k;
-}
-
-// The same count from a table over kPickBins equal bins of [0, 1): entry b holds
-// #{c < K-1 : cumpi[c] <= b / kPickBins} in its low 7 bits and, in bit 7,
-// whether some cumpi[c] falls strictly inside the bin; only then does the count
-// continue past the bin's lower edge.  u is a multiple of 2^-24, so u * kPickBins
-// and its floor are exact.
-constexpr int kPickBins = 1024;
-__device__ __forceinline__ void build_pick_table(const float* cumpi, int K, uint8_t* tab, int tid, int TB) {
-  for (int b = tid; b < kPickBins; b += TB) {
-    const float lo = (float)b * (1.0f / kPickBins), hi = (float)(b + 1) * (1.0f / kPickBins);
-    int s = 0, s2 = 0;
-    for (int c = 0; c < K - 1; ++c) {
-      s += (cumpi[c] <= lo) ? 1 : 0;
-      s2 += (cumpi[c] < hi) ? 1 : 0;
-    }
-    tab[b] = (uint8_t)(s | ((s2 > s) ? 0x80 : 0));
-  }
-}
+// mixture component of a particle-frame (mkf_common.cuh: by count, or through
+// the track's kPickBins table when the view has one)
 __device__ __forceinline__ int pick_component(const PView& p, float u) {
-  if (!p.ktab) return pick_component(p.cumpi, p.K, u);
-  const int e = p.ktab[__float2int_rz(u * (float)kPickBins)];
-  int k = e & 0x7F;
-  if (e & 0x80)
-    while (k < p.K - 1 && u >= p.cumpi[k]) ++k;
-  return k;
+  return p.ktab ? pick_component_table(p.ktab, p.cumpi, p.K, u) : pick_component(p.cumpi, p.K, u);
 }
 
 template <int D>

@@ -89,6 +89,46 @@ MKF_HD uint32_t resample_uniform(uint64_t seed, uint32_t track, uint32_t frame) 
   return draw_block(seed, track, frame, kItemFrame, kStreamResample).x;
 }
 
+// ---------------------------------------------------------------- component pick
+// First k with u < cumpi[k] (the last component if none): with cumpi
+// nondecreasing that is the number of c < K-1 with cumpi[c] <= u, counted with
+// independent loads instead of a dependent walk.
+MKF_HD int pick_component(const float* cumpi, int K, float u) {
+  int k = 0;
+  for (int c = 0; c < K - 1; ++c) k += (u >= cumpi[c]) ? 1 : 0;
+  return k;
+}
+
+// The same count from a table over kPickBins equal bins of [0, 1): entry b holds
+// #{c < K-1 : cumpi[c] <= b / kPickBins} in its low 7 bits (K <= 128) and, in
+// bit 7, whether some cumpi[c] falls strictly inside the bin; only then does the
+// count continue past the bin's lower edge.  u is a multiple of 2^-24 in [0, 1),
+// so u * kPickBins and its floor are exact.  build_pick_table fills entries
+// tid, tid + TB, ... (a block fills it cooperatively).
+constexpr int kPickBins = 1024;
+MKF_HD void build_pick_table(const float* cumpi, int K, uint8_t* tab, int tid, int TB) {
+  for (int b = tid; b < kPickBins; b += TB) {
+    const float lo = (float)b * (1.0f / kPickBins), hi = (float)(b + 1) * (1.0f / kPickBins);
+    int s = 0, s2 = 0;
+    for (int c = 0; c < K - 1; ++c) {
+      s += (cumpi[c] <= lo) ? 1 : 0;
+      s2 += (cumpi[c] < hi) ? 1 : 0;
+    }
+    tab[b] = (uint8_t)(s | ((s2 > s) ? 0x80 : 0));
+  }
+}
+MKF_HD int pick_component_table(const uint8_t* tab, const float* cumpi, int K, float u) {
+#ifdef __CUDA_ARCH__
+  const int e = tab[__float2int_rz(u * (float)kPickBins)];
+#else
+  const int e = tab[(int)(u * (float)kPickBins)];   // truncation, as __float2int_rz
+#endif
+  int k = e & 0x7F;
+  if (e & 0x80)
+    while (k < K - 1 && u >= cumpi[k]) ++k;
+  return k;
+}
+
 #ifdef __CUDACC__
 // ---------------------------------------------------------------- packed FP32 pairs
 // Blackwell f32x2 instructions: one issue for two lanes, each lane rounded as

@@ -1,4 +1,4 @@
-// The integer pieces of the exact resampler, from mkf_common.cuh compiled here
+// The integer paths of the particle kernels, from mkf_common.cuh compiled here
 // for the host, against independent restatements:
 //  - thresholds: rs_thresh_setup with rs_threshold (N <= 65536) and
 //    rs_threshold64 (N <= 2^22) against T_i = ceil((i 2^32 + U) Qt / (N 2^32))
@@ -8,7 +8,13 @@
 //    times a power of two) for weights w <= 1 (its domain): random, boundary,
 //    subnormal, zero, negative, -inf and NaN;
 //  - search: search_u64_multi<4> against std::lower_bound on random
-//    nondecreasing prefix arrays (with runs of equal values) of 1 .. 2^22 entries.
+//    nondecreasing prefix arrays (with runs of equal values) of 1 .. 2^22 entries;
+//  - pick: the particle kernels' component pick through the 1024-bin table
+//    (build_pick_table / pick_component_table) against the direct count, for
+//    K in [1, 32], cumulative weights with zero-weight components, sums short of
+//    or past 1, cumulative values on bin edges, and every uniform u = m 2^-24 of
+//    a sample.  (The weights cover the picks that the random-mixture workloads
+//    and the shipped models make.)
 // Prints one "name mismatches cases" line per piece.
 #include "mkf_common.cuh"
 
@@ -105,10 +111,48 @@ static void search(std::mt19937_64& rng) {
   std::printf("search %lld %lld\n", bad, n);
 }
 
+static void pick(std::mt19937_64& rng) {
+  long long bad = 0, n = 0;
+  std::uniform_real_distribution<float> u01(0.0f, 1.0f);
+  std::vector<uint8_t> tab(mkf::kPickBins);
+  for (int it = 0; it < 3000; ++it) {
+    const int K = 1 + (int)(rng() % 32);
+    std::vector<float> pi(K), cum(K);
+    float tot = 0.0f;
+    for (int k = 0; k < K; ++k) {
+      pi[k] = (rng() % 5 == 0) ? 0.0f : u01(rng);
+      tot += pi[k];
+    }
+    const float scale = (it % 3 == 0) ? 1.0f : (it % 3 == 1 ? 0.999f : 1.001f);
+    float acc = 0.0f;
+    for (int k = 0; k < K; ++k) {
+      acc += tot > 0.0f ? pi[k] / tot * scale : 1.0f / K;
+      cum[k] = acc;
+    }
+    if (it % 7 == 0)   // cumulative values exactly on bin edges
+      for (int k = 0; k + 1 < K; ++k) cum[k] = std::floor(cum[k] * mkf::kPickBins) / mkf::kPickBins;
+    for (int k = 1; k < K; ++k) cum[k] = std::max(cum[k], cum[k - 1]);
+    for (int b = 0; b < mkf::kPickBins; ++b) tab[b] = 0xFF;
+    mkf::build_pick_table(cum.data(), K, tab.data(), 0, 1);
+    for (int q = 0; q < 2000; ++q) {
+      uint32_t m = (uint32_t)(rng() >> 40);                          // 24 bits
+      if (q < 64 && K > 1) {                                         // u on a cumulative value or a bin edge
+        const float c = (q & 1) ? cum[rng() % (K - 1)] : (float)(rng() % mkf::kPickBins) / mkf::kPickBins;
+        m = (uint32_t)std::min(std::max(0.0, std::ldexp((double)c, 24)), 16777215.0);
+      }
+      const float u = (float)m * (1.0f / 16777216.0f);
+      bad += mkf::pick_component_table(tab.data(), cum.data(), K, u) != mkf::pick_component(cum.data(), K, u);
+      ++n;
+    }
+  }
+  std::printf("pick %lld %lld\n", bad, n);
+}
+
 int main() {
   std::mt19937_64 rng(20140601);
   thresholds(rng);
   quantize(rng);
   search(rng);
+  pick(rng);
   return 0;
 }

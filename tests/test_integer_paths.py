@@ -1,7 +1,8 @@
-"""The integer pieces of the exact resampler that every GPU resampling kernel
-shares (64-bit thresholds, weight quantisation by bit fields, the interleaved
-branch-free search), compiled for the host from the kernels' own header and
-checked against independent restatements (tests/resampler_host_check.cpp)."""
+"""The integer paths that the GPU particle kernels share (the exact
+resampler's 64-bit thresholds, weight quantisation by bit fields and
+interleaved branch-free search; the table-driven component pick), compiled for
+the host from the kernels' own header and checked against independent
+restatements (tests/integer_paths_check.cpp)."""
 import os
 import shutil
 import subprocess
@@ -22,14 +23,15 @@ def results(tmp_path_factory):
     inc = _cuda_include()
     if inc is None or shutil.which("g++") is None:
         pytest.skip("needs g++ and the CUDA headers")
-    exe = str(tmp_path_factory.mktemp("rh") / "resampler_host_check")
+    exe = str(tmp_path_factory.mktemp("ip") / "integer_paths_check")
     subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "mkfbodytracker_pdaf_gb300", "csrc"),
-                    "-I", inc, os.path.join(ROOT, "tests", "resampler_host_check.cpp"), "-o", exe], check=True)
+                    "-I", inc, os.path.join(ROOT, "tests", "integer_paths_check.cpp"), "-o", exe], check=True)
     out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
     return {name: (int(bad), int(n)) for name, bad, n in (line.split() for line in out.strip().splitlines())}
 
 
-@pytest.mark.parametrize("piece,min_cases", [("thresholds", 400000), ("quantize", 1000000), ("search", 400000)])
+@pytest.mark.parametrize("piece,min_cases", [("thresholds", 400000), ("quantize", 1000000), ("search", 400000),
+                                             ("pick", 6000000)])
 def test_against_independent_restatement(results, piece, min_cases):
     bad, n = results[piece]
     assert n >= min_cases
