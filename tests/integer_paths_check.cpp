@@ -15,6 +15,8 @@
 //    or past 1, cumulative values on bin edges, and every uniform u = m 2^-24 of
 //    a sample.  (The weights cover the picks that the random-mixture workloads
 //    and the shipped models make.)
+//  - philox: philox4x32_10 (every draw of the kernels) against the Random123
+//    known-answer vectors.
 // Prints one "name mismatches cases" line per piece.
 #include "mkf_common.cuh"
 
@@ -148,8 +150,26 @@ static void pick(std::mt19937_64& rng) {
   std::printf("pick %lld %lld\n", bad, n);
 }
 
+static void philox() {
+  struct Kat { mkf::u32x4 ctr; uint32_t k0, k1; mkf::u32x4 out; };
+  const Kat kats[] = {
+      {{0u, 0u, 0u, 0u}, 0u, 0u, {0x6627e8d5u, 0xe169c58du, 0xbc57ac4cu, 0x9b00dbd8u}},
+      {{0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu}, 0xffffffffu, 0xffffffffu,
+       {0x408f276du, 0x41c83b0eu, 0xa20bc7c6u, 0x6d5451fdu}},
+      {{0x243f6a88u, 0x85a308d3u, 0x13198a2eu, 0x03707344u}, 0xa4093822u, 0x299f31d0u,
+       {0xd16cfe09u, 0x94fdccebu, 0x5001e420u, 0x24126ea1u}}};
+  long long bad = 0, n = 0;
+  for (const Kat& k : kats) {
+    const mkf::u32x4 o = mkf::philox4x32_10(k.ctr, k.k0, k.k1);
+    bad += o.x != k.out.x || o.y != k.out.y || o.z != k.out.z || o.w != k.out.w;
+    ++n;
+  }
+  std::printf("philox %lld %lld\n", bad, n);
+}
+
 int main() {
   std::mt19937_64 rng(20140601);
+  philox();
   thresholds(rng);
   quantize(rng);
   search(rng);
