@@ -283,12 +283,14 @@ __device__ __forceinline__ uint64_t quantize_f64(double w, int e) {
   return (w > 0.0) ? (uint64_t)__double2ull_rz(ldexp(w, kQBits - e)) : 0ull;
 }
 
+#endif  // __CUDACC__
+
 // target of particle i: (i 2^32 + U) * Qt  (128-bit)
-__device__ __forceinline__ unsigned __int128 resample_rhs(int i, uint32_t U, uint64_t Qt) {
+MKF_HD unsigned __int128 resample_rhs(int i, uint32_t U, uint64_t Qt) {
   return (unsigned __int128)((((uint64_t)(uint32_t)i) << 32) | (uint64_t)U) * (unsigned __int128)Qt;
 }
 // first j in [0, n) with N Q[j] 2^32 >= rhs; Q nondecreasing; returns n-1 if none
-__device__ __forceinline__ int resample_search(const uint64_t* Q, int n, int N, unsigned __int128 rhs) {
+MKF_HD int resample_search(const uint64_t* Q, int n, int N, unsigned __int128 rhs) {
   int lo = 0, hi = n - 1;
   while (lo < hi) {
     int mid = (lo + hi) >> 1;
@@ -297,17 +299,51 @@ __device__ __forceinline__ int resample_search(const uint64_t* Q, int n, int N, 
   }
   return lo;
 }
-__device__ __forceinline__ int resample_fallback_index(uint32_t U, int i, int L) {
+MKF_HD int resample_fallback_index(uint32_t U, int i, int L) {
   u32x4 o = philox4x32_10(u32x4{(uint32_t)i, 0u, 0u, 0u}, U, 0x5EEDu);
   return (int)(((uint64_t)o.x * (uint64_t)L) >> 32);
 }
-#endif  // __CUDACC__
+// number of targets i in [0, N) with (i 2^32 + U) Qt <= N X 2^32
+MKF_HD int count_targets_le(uint64_t X, int N, uint32_t U, uint64_t Qt) {
+  const unsigned __int128 lim = ((unsigned __int128)(uint64_t)N * (unsigned __int128)X) << 32;
+  double est = (double)N * ((double)X / (double)Qt);
+  long long i = (long long)est;
+  if (i < 0) i = 0;
+  if (i > N) i = N;
+  for (int it = 0; it < 64 && i < N && resample_rhs((int)i, U, Qt) <= lim; ++it) ++i;
+  for (int it = 0; it < 64 && i > 0 && resample_rhs((int)(i - 1), U, Qt) > lim; ++it) --i;
+  bool ok = (i == N || resample_rhs((int)i, U, Qt) > lim) && (i == 0 || resample_rhs((int)(i - 1), U, Qt) <= lim);
+  if (!ok) {
+    long long lo = 0, hi = N;
+    while (lo < hi) {
+      long long mid = (lo + hi) >> 1;
+      if (resample_rhs((int)mid, U, Qt) <= lim) lo = mid + 1; else hi = mid;
+    }
+    i = lo;
+  }
+  return (int)i;
+}
+
+// Scatter walk of exact systematic resampling for one thread's contiguous chunk
+// [j0, j1) of integer weights q_j (get(j)), whose exclusive prefix is P: emits
+// ancestors j for every target i whose rule "first j with N Q_j 2^32 >=
+// (i 2^32 + U) Qt" lands in the chunk.
+template <typename GetQ>
+MKF_HD void scatter_walk(int j0, int j1, uint64_t P, int N, uint32_t U, uint64_t Qt, GetQ get, int* anc) {
+  if (j0 >= j1) return;
+  int i = (j0 == 0) ? 0 : count_targets_le(P, N, U, Qt);
+  uint64_t Qj = P;
+  for (int j = j0; j < j1; ++j) {
+    Qj += get(j);
+    const unsigned __int128 lim = ((unsigned __int128)(uint64_t)N * (unsigned __int128)Qj) << 32;
+    while (i < N && resample_rhs(i, U, Qt) <= lim) anc[i++] = j;
+  }
+}
 
 // The same rule with 64-bit thresholds (integer only, host and device): target
 // i takes the first j whose inclusive prefix Q_j >= T_i = ceil((i 2^32 + U) Qt /
 // (N 2^32)), the 128-bit comparison N Q_j 2^32 >= (i 2^32 + U) Qt restated
-// exactly.  With
-// Qt = A N + r and floor(U Qt / 2^32) = C N + s, and V_i = i r + s:
+// exactly.  With Qt = A N + r and floor(U Qt / 2^32) = C N + s, and V_i = i r + s:
 //   T_i = i A + C + floor(V_i / N) + [V_i mod N > 0 or (U Qt mod 2^32) > 0].
 // Needs N <= 65536 (V_i < N^2 fits 32 bits) and i A + C < 2^64.
 struct RsThresh {
@@ -389,45 +425,5 @@ MKF_HD void search_u64_multi(const uint64_t* Q, int n, const uint64_t* T, int* o
   MKF_UNROLL
   for (int g = 0; g < G; ++g) out[g] = base[g] + ((Q[base[g]] < T[g]) ? 1 : 0);
 }
-
-#ifdef __CUDACC__
-// number of targets i in [0, N) with (i 2^32 + U) Qt <= N X 2^32
-__device__ __forceinline__ int count_targets_le(uint64_t X, int N, uint32_t U, uint64_t Qt) {
-  const unsigned __int128 lim = ((unsigned __int128)(uint64_t)N * (unsigned __int128)X) << 32;
-  double est = (double)N * ((double)X / (double)Qt);
-  long long i = (long long)est;
-  if (i < 0) i = 0;
-  if (i > N) i = N;
-  for (int it = 0; it < 64 && i < N && resample_rhs((int)i, U, Qt) <= lim; ++it) ++i;
-  for (int it = 0; it < 64 && i > 0 && resample_rhs((int)(i - 1), U, Qt) > lim; ++it) --i;
-  bool ok = (i == N || resample_rhs((int)i, U, Qt) > lim) && (i == 0 || resample_rhs((int)(i - 1), U, Qt) <= lim);
-  if (!ok) {
-    long long lo = 0, hi = N;
-    while (lo < hi) {
-      long long mid = (lo + hi) >> 1;
-      if (resample_rhs((int)mid, U, Qt) <= lim) lo = mid + 1; else hi = mid;
-    }
-    i = lo;
-  }
-  return (int)i;
-}
-
-// Scatter walk of exact systematic resampling for one thread's contiguous chunk
-// [j0, j1) of integer weights q_j (get(j)), whose exclusive prefix is P: emits
-// ancestors j for every target i whose rule "first j with N Q_j 2^32 >=
-// (i 2^32 + U) Qt" lands in the chunk.
-template <typename GetQ>
-__device__ __forceinline__ void scatter_walk(int j0, int j1, uint64_t P, int N, uint32_t U, uint64_t Qt,
-                                             GetQ get, int* anc) {
-  if (j0 >= j1) return;
-  int i = (j0 == 0) ? 0 : count_targets_le(P, N, U, Qt);
-  uint64_t Qj = P;
-  for (int j = j0; j < j1; ++j) {
-    Qj += get(j);
-    const unsigned __int128 lim = ((unsigned __int128)(uint64_t)N * (unsigned __int128)Qj) << 32;
-    while (i < N && resample_rhs(i, U, Qt) <= lim) anc[i++] = j;
-  }
-}
-#endif  // __CUDACC__
 
 }  // namespace mkf

@@ -16,7 +16,12 @@
 //    a sample.  (The weights cover the picks that the random-mixture workloads
 //    and the shipped models make.)
 //  - philox: philox4x32_10 (every draw of the kernels) against the Random123
-//    known-answer vectors.
+//    known-answer vectors;
+//  - walk: the scatter walk over per-thread chunks (scatter_walk with
+//    count_targets_le, the RBPF, PDAF, pf2D and scatter-variant resampler) and
+//    the 128-bit binary search (resample_search) against a direct two-pointer
+//    evaluation of the rule "first j with N Q_j 2^32 >= (i 2^32 + U) Qt", on
+//    random integer weights (with zeros and a dominant weight) and chunkings.
 // Prints one "name mismatches cases" line per piece.
 #include "mkf_common.cuh"
 
@@ -167,9 +172,50 @@ static void philox() {
   std::printf("philox %lld %lld\n", bad, n);
 }
 
+static void walk(std::mt19937_64& rng) {
+  long long bad = 0, n = 0;
+  for (int it = 0; it < 600; ++it) {
+    const int L = 1 + (int)(rng() % 3000), N = 1 + (int)(rng() % 3000);
+    std::vector<uint64_t> q(L), Q(L);
+    uint64_t acc = 0;
+    for (int j = 0; j < L; ++j) {
+      const int kind = (int)(rng() % 8);
+      q[j] = kind == 0 ? 0 : kind == 1 ? (1ull << 40) : (rng() >> (24 + rng() % 30));
+      acc += q[j];
+      Q[j] = acc;
+    }
+    if (acc == 0) { q[L - 1] = 1; Q[L - 1] = acc = 1; }
+    const uint64_t Qt = acc;
+    const uint32_t U = (uint32_t)rng();
+    // direct evaluation of the rule, one pointer per side
+    std::vector<int> ref(N);
+    int j = 0;
+    for (int i = 0; i < N; ++i) {
+      const unsigned __int128 rhs = mkf::resample_rhs(i, U, Qt);
+      while ((((unsigned __int128)(uint64_t)N * (unsigned __int128)Q[j]) << 32) < rhs) ++j;
+      ref[i] = j;
+    }
+    // the scatter walk over chunks of E weights, as the kernels' threads run it
+    const int E = 1 + (int)(rng() % 64);
+    std::vector<int> anc(N, -1);
+    for (int j0 = 0; j0 < L; j0 += E) {
+      const int j1 = std::min(L, j0 + E);
+      const uint64_t P = j0 ? Q[j0 - 1] : 0;
+      mkf::scatter_walk(j0, j1, P, N, U, Qt, [&](int k) { return q[k]; }, anc.data());
+    }
+    for (int i = 0; i < N; ++i) {
+      bad += anc[i] != ref[i];
+      bad += mkf::resample_search(Q.data(), L, N, mkf::resample_rhs(i, U, Qt)) != ref[i];
+      n += 2;
+    }
+  }
+  std::printf("walk %lld %lld\n", bad, n);
+}
+
 int main() {
   std::mt19937_64 rng(20140601);
   philox();
+  walk(rng);
   thresholds(rng);
   quantize(rng);
   search(rng);

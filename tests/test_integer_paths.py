@@ -1,6 +1,7 @@
 """The integer paths that the GPU particle kernels share (Philox4x32-10; the
-exact resampler's 64-bit thresholds, weight quantisation by bit fields and
-interleaved branch-free search; the table-driven component pick), compiled for
+exact resampler's scatter walk, 128-bit search, 64-bit thresholds, weight
+quantisation by bit fields and interleaved branch-free search; the
+table-driven component pick), compiled for
 the host from the kernels' own header and checked against independent
 restatements (tests/integer_paths_check.cpp)."""
 import os
@@ -31,7 +32,7 @@ def results(tmp_path_factory):
 
 
 @pytest.mark.parametrize("piece,min_cases", [("thresholds", 400000), ("quantize", 1000000), ("search", 400000),
-                                             ("pick", 6000000), ("philox", 3)])
+                                             ("pick", 6000000), ("philox", 3), ("walk", 1000000)])
 def test_against_independent_restatement(results, piece, min_cases):
     bad, n = results[piece]
     assert n >= min_cases
