@@ -271,19 +271,28 @@ __device__ __forceinline__ uint64_t block_excl_scan_u64(uint64_t v, uint64_t* re
   return r;
 }
 
+#endif  // __CUDACC__
+
 // ---------------------------------------------------------------- exact resampler
 // Weights -> 64-bit integers with 40 bits below the max (exact power-of-two
-// scaling then truncation); systematic resampling in exact integer arithmetic.
+// scaling then truncation; e is the max weight's binary exponent, frexp
+// convention); systematic resampling in exact integer arithmetic.
 constexpr int kQBits = 40;
 
-__device__ __forceinline__ uint64_t quantize_f32(float w, int e) {
+MKF_HD uint64_t quantize_f32(float w, int e) {
+#ifdef __CUDA_ARCH__
   return (w > 0.0f) ? (uint64_t)__float2ull_rz(ldexpf(w, kQBits - e)) : 0ull;
+#else
+  return (w > 0.0f) ? (uint64_t)ldexpf(w, kQBits - e) : 0ull;   // the cast truncates
+#endif
 }
-__device__ __forceinline__ uint64_t quantize_f64(double w, int e) {
+MKF_HD uint64_t quantize_f64(double w, int e) {
+#ifdef __CUDA_ARCH__
   return (w > 0.0) ? (uint64_t)__double2ull_rz(ldexp(w, kQBits - e)) : 0ull;
+#else
+  return (w > 0.0) ? (uint64_t)ldexp(w, kQBits - e) : 0ull;
+#endif
 }
-
-#endif  // __CUDACC__
 
 // target of particle i: (i 2^32 + U) * Qt  (128-bit)
 MKF_HD unsigned __int128 resample_rhs(int i, uint32_t U, uint64_t Qt) {

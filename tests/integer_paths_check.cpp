@@ -6,7 +6,9 @@
 //    40 bits each), U and i, plus the extremes of each;
 //  - quantize: quantize39(w) against floor(w 2^39) in double (exact: a float
 //    times a power of two) for weights w <= 1 (its domain): random, boundary,
-//    subnormal, zero, negative, -inf and NaN;
+//    subnormal, zero, negative, -inf and NaN; quantize_f32 / quantize_f64 (the
+//    general-exponent forms) against floor(w 2^(40-e)) in long double for
+//    weights up to their max 2^e;
 //  - search: search_u64_multi<4> against std::lower_bound on random
 //    nondecreasing prefix arrays (with runs of equal values) of 1 .. 2^22 entries;
 //  - pick: the particle kernels' component pick through the 1024-bin table
@@ -84,8 +86,22 @@ static void quantize(std::mt19937_64& rng) {
   }
   for (float w : ws) {
     bad += mkf::quantize39(w) != quantize_ref(w);
+    bad += (w <= 1.0f && w > 0.0f) && mkf::quantize_f32(w, 1) != quantize_ref(w);   // the same value
     ++n;
   }
+  // general exponents: w in (0, 2^e), e = max weight's frexp exponent
+  for (int k = 0; k < 200000; ++k) {
+    const int e = (int)(rng() % 200) - 100;
+    const double wd = std::ldexp(std::uniform_real_distribution<double>(0.0, 1.0)(rng), e);
+    const float wf = (float)wd;
+    const long double rf = std::floor(std::ldexp((long double)wf, 40 - e));
+    const long double rd = std::floor(std::ldexp((long double)wd, 40 - e));
+    bad += wf > 0.0f && wf < std::ldexp(1.0f, e) && mkf::quantize_f32(wf, e) != (uint64_t)rf;
+    bad += wd > 0.0 && mkf::quantize_f64(wd, e) != (uint64_t)rd;
+    n += 2;
+  }
+  bad += mkf::quantize_f64(0.0, 1) != 0 || mkf::quantize_f64(-1.0, 1) != 0 || mkf::quantize_f32(-0.5f, 0) != 0;
+  n += 3;
   std::printf("quantize %lld %lld\n", bad, n);
 }
 
