@@ -310,12 +310,14 @@ __host__ __device__ constexpr int params_floats(int K, int J, bool diag) {
   return 2 * K * D + pad4(diag ? K * D : K * D * (D + 1) / 2) + J * 3 * D + pad4(J * 3) + pad4(K);
 }
 
-// Batched persistent kernel.  Shared memory per CTA: W (float, Nmax) holds the
-// frame's log-weights then weights; ANC (int, Nmax) the ancestors; then the
-// track's model.  Particle states live in this CTA's global slot (two SoA
-// buffers of D x Nmax floats, L2-resident).  Per frame: propagate + score,
-// block max, weights/estimate/ESS, exact systematic resampling by a scatter
-// walk over each thread's contiguous chunk of integer weights.
+// Batched persistent kernel: CTAs take tracks from an atomic queue in
+// longest-first order, one track at a time.  Particle states live in this
+// CTA's global slot (two buffers of D/4 float4 planes of Nmax particles,
+// partly L2-resident); per-particle weights, prefix sums and ancestors in
+// shared memory (the layout of each variant below), then the track's model.
+// Per frame: propagate + score (accumulating the estimate sums), block max,
+// weights and ESS, exact systematic resampling, the gather folded into the
+// next frame's propagate.
 // Code variants chosen by the autotuner: VEC (float4 vs scalar parameter loads)
 // and SEARCH (ancestors by binary search over the shared prefix sums, 12 Nmax
 // bytes of shared memory, vs the scatter walk over each thread's chunk, 8 Nmax).
