@@ -11,9 +11,12 @@
 // Launch shape: one CTA per track (static round-robin over a persistent grid,
 // so every reduction has a fixed order), one warp per mixture component.  A
 // warp's predict/update/reverse runs lane-parallel over matrix entries; the
-// collapse and its reverse are CTA-wide.  Per-warp buffers (joint records,
-// component outputs, adjoints) live in the CTA's global scratch slot (L1/L2
-// resident); the collapsed state and its adjoint live in shared memory.
+// collapse and its reverse are CTA-wide.  Each warp's forward scratch (its
+// component state and the joint update being formed) is in shared memory; the
+// per-frame joint records of a backward segment are in the CTA's global slot
+// (sized to stay L2-resident); the per-component adjoint work blocks are in
+// shared memory when they fit (STAGE), else in the slot; the collapsed state
+// and its adjoint are in shared memory.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
