@@ -76,14 +76,29 @@ def tune(n_tracks=8192, reps=2, seed=None, candidates=CANDIDATES):
             "results": res, "best": best}
 
 
+def merge_rankings(new, old):
+    """A partial (--quick) ranking keeps the previous ranking's full table
+    beside it: ``best`` comes from the new run alone (rankings from different
+    runs are not compared), the old results move to ``earlier_results``."""
+    if not old:
+        return new
+    out = dict(new)
+    out["earlier_results"] = {"when": old.get("when"), "results": old.get("results", [])}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--tracks", type=int, default=8192)
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--out", default=TUNING_FILE)
-    ap.add_argument("--quick", action="store_true", help="rank only the usual top candidates")
+    ap.add_argument("--quick", action="store_true",
+                    help="rank only the usual top candidates, keeping the previous table of --out")
     a = ap.parse_args()
     r = tune(a.tracks, a.reps, candidates=QUICK if a.quick else CANDIDATES)
+    if a.quick and os.path.exists(a.out):
+        with open(a.out) as f:
+            r = merge_rankings(r, json.load(f))
     with open(a.out, "w") as f:
         json.dump(r, f, indent=1)
     print(json.dumps(r))

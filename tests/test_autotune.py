@@ -35,3 +35,14 @@ def test_committed_ranking_and_load_tuning():
     assert shape == (best["block_threads"], best["ctas_per_sm"], best["variant"])
     assert _valid(*shape)
     assert shape in autotune.CANDIDATES
+
+
+def test_quick_ranking_keeps_the_previous_table():
+    old = {"when": "t0", "results": [{"block_threads": 256, "ctas_per_sm": 2, "variant": 0, "ms": 9.0}],
+           "best": {"block_threads": 256, "ctas_per_sm": 2, "variant": 0, "ms": 9.0}}
+    new = {"when": "t1", "results": [{"block_threads": 256, "ctas_per_sm": 3, "variant": 11, "ms": 5.0}],
+           "best": {"block_threads": 256, "ctas_per_sm": 3, "variant": 11, "ms": 5.0}}
+    m = autotune.merge_rankings(new, old)
+    assert m["best"] == new["best"] and m["results"] == new["results"]
+    assert m["earlier_results"] == {"when": "t0", "results": old["results"]}
+    assert autotune.merge_rankings(new, None) is new
