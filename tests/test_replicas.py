@@ -95,3 +95,32 @@ def test_reference_arm_nonzero_rank_exits_without_work(monkeypatch, capsys):
     args = bench.parse_args(["--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3"])
     assert bench.run_reference(args) is None
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_json_line_on_cpu(monkeypatch, capsys):
+    """The reference arm (the oracle on the host cores) prints the bench
+    contract's line: impl, metric, value, e2e with zero copies, cpu_baseline."""
+    import importlib.util
+    import json
+    import sys
+    from mkfbodytracker_pdaf_gb300 import synth
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("bench_ref", os.path.join(root, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    sys.modules["bench_ref"] = bench
+    spec.loader.exec_module(bench)
+    for k in ("WORLD_SIZE", "RANK", "LOCAL_RANK"):
+        monkeypatch.delenv(k, raising=False)
+    small = synth.make_bpf_batch(7, [64, 100, 150], [5, 3, 4], [2.0, 3.0, 1.0], [0.9, 0.8, 0.95])
+    monkeypatch.setattr(bench, "workload", lambda rank, n: small)
+    args = bench.parse_args(["--impl", "reference", "--steps", "2", "--warmup", "3", "--ref-sample-tracks", "2"])
+    bench.run_reference(args)
+    lines = [ln for ln in capsys.readouterr().out.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == bench.UNIT
+    assert d["value"] > 0 and d["steps"] == 2 and d["warmup"] == 3 and d["higher_is_better"] is True
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
+    assert d["config"]["tracks_per_step"] == 2
