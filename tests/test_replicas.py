@@ -124,3 +124,19 @@ def test_reference_arm_json_line_on_cpu(monkeypatch, capsys):
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
     assert d["config"]["tracks_per_step"] == 2
+
+
+def test_cpu_baseline_record_on_cpu():
+    """The cpu_baseline object of the GPU arm's line, from the oracle on a fixed sample."""
+    import importlib.util
+    import sys
+    from mkfbodytracker_pdaf_gb300 import synth
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("bench_cb", os.path.join(root, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    sys.modules["bench_cb"] = bench
+    spec.loader.exec_module(bench)
+    small = synth.make_bpf_batch(8, [64, 80, 96, 50], [4, 3, 5, 2], [2.0, 3.0, 1.0, 0.5], [0.9, 0.8, 0.95, 0.9])
+    cb = bench.cpu_baseline(small, 3, 2)
+    assert cb["value"] > 0 and cb["unit"] == bench.UNIT and cb["cores"] == 2 and cb["kind"] == "port"
+    assert cb["sample"].startswith("3 fixed tracks")
