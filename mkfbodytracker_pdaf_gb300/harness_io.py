@@ -5,7 +5,8 @@ ROI) input and its HFPose2DArray / TF output (pfPose.cpp:16-21, 173-208).
 Frame file: b"MKFFRM01", int32 n, then per frame int32 id, int32 has_roi,
 float64 roi[8] (x_offset, y_offset, width, height per arm), int32 M,
 float64 cand[2M].  Version b"MKFFRM02" adds int32 W, H after n and a W x H
-uint8 likelihood image after each frame's candidates (the image path).  Output file: b"MKFOUT01", int32 n, d, F, then per frame
+uint8 likelihood image after each frame's candidates (the image path).
+Output file: b"MKFOUT01", int32 n, d, F, then per frame
 int32 id, int32 valid, float64 est[2][d], e[2][F], points[8][2] (hand1, hand2,
 head, neck, elbow1, elbow2, shoulder1, shoulder2), pos3d[2][3][5]."""
 from __future__ import annotations
