@@ -39,7 +39,6 @@ BYTES_PER_PF = 112          # algorithmic bytes per particle-frame (state in/out
 # dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture on 2048
 # tracks of the same workload (284.7 GB over 4.148e9 particle-frames), scaled
 # to a full launch by particle-frames
-# (profiles/bpf_batched_kernel_uneven_tracks_B8192.md)
 TRAFFIC_BYTES_PER_PF = 68.6
 
 
@@ -119,8 +118,13 @@ def pf_count(batch, ids=None):
 
 
 def sample_ids(batch, n):
+    """n fixed tracks of the batch, longest (particle-frames) first: the CPU
+    runs them with dynamic scheduling over tracks, so that order keeps every
+    host core busy to the end (longest-processing-time-first)."""
     rng = np.random.default_rng(12345)
-    return sorted(rng.choice(batch.n_tracks, size=min(n, batch.n_tracks), replace=False).tolist())
+    ids = rng.choice(batch.n_tracks, size=min(n, batch.n_tracks), replace=False).tolist()
+    cost = lambda b: int(batch.tracks[b]["n_particles"]) * int(batch.tracks[b]["n_frames"])
+    return sorted(ids, key=lambda b: (-cost(b), b))
 
 
 def cpu_run(batch, ids, threads):
@@ -139,8 +143,67 @@ def cpu_baseline(batch, n_sample, threads):
     rate, dt, sub = cpu_run(batch, ids, threads)
     return {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": "%d fixed tracks of the batch (%d track-frames, %.3g particle-frames), "
-                      "FP64 oracle with Philox draws, OpenMP over tracks, %.1f s"
+                      "FP64 oracle with Philox draws, OpenMP over tracks (longest first), %.1f s"
                       % (len(ids), sub.n_frames_total, pf_count(sub), dt)}
+
+
+def accuracy_tracks(batch, ids, n=4):
+    """Tracks of the CPU sample whose full horizon is replayed in FP64: the
+    longest, the one with the most particle-frames, the most particles, and
+    the fewest particles among the longer half."""
+    T = {b: int(batch.tracks[b]["n_frames"]) for b in ids}
+    N = {b: int(batch.tracks[b]["n_particles"]) for b in ids}
+    picks = [max(ids, key=lambda b: (T[b], N[b])), max(ids, key=lambda b: (N[b] * T[b], b)),
+             max(ids, key=lambda b: (N[b], T[b]))]
+    long_half = sorted(ids, key=lambda b: -T[b])[:max(1, len(ids) // 2)]
+    picks.append(min(long_half, key=lambda b: (N[b], -T[b])))
+    out = []
+    for b in picks:
+        if b not in out:
+            out.append(b)
+    return out[:n]
+
+
+def fp64_accuracy(batch, ids, tb, cps, var, full_est=None):
+    """Full-horizon FP32-vs-FP64 error of the batched kernel on tracks ids of
+    the batch: each track's debug dump (weights, ancestors) and outputs are
+    replayed frame by frame in FP64 by the oracle, teacher-forced with the
+    device's draws and ancestors.  The tracks run as a sub-batch; tracks are
+    independent, so their outputs equal the full run's bit for bit, which is
+    checked against full_est (the full run's frame-indexed estimates)."""
+    import torch
+    import oracle
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from bpf_check import check_track_full
+    from mkfbodytracker_pdaf_gb300.filters import BatchedBootstrapPF
+    oracle.build()
+    sub = batch.subset(ids)
+    runner = BatchedBootstrapPF(sub, block_threads=tb, ctas_per_sm=cps, variant=var)
+    det_off, det = runner.device_inputs()
+    t0 = time.perf_counter()
+    rows = []
+    for n, b in enumerate(ids):
+        t = sub.tracks[n]
+        N, T = int(t["n_particles"]), int(t["n_frames"])
+        wd = torch.zeros((T, N), dtype=torch.float32, device="cuda")
+        ad = torch.zeros((T, N), dtype=torch.int32, device="cuda")
+        runner.set_debug(n, wd, ad)
+        est, ll, _, _ = runner.run(det_off, det)
+        torch.cuda.synchronize()
+        est_h = est.cpu().numpy()
+        rep = check_track_full(torch, oracle, sub, n, wd, ad, est_h, ll.cpu().numpy())
+        s = rep.summary()
+        s.update({"track": int(b), "n_particles": N})
+        if full_est is not None:
+            g0, g1 = int(batch.tracks[b]["frame_base"]), int(t["frame_base"])
+            s["same_as_headline_run"] = bool(np.array_equal(full_est[g0:g0 + T], est_h[g1:g1 + T]))
+        rows.append(s)
+        del wd, ad
+    return {"definition": "per frame: posterior mean max_c|est_dev-est_fp64|/max(1,max_c|est_fp64|); "
+                          "log-likelihood increment |ll_dev-ll_fp64|/max(1,|ll_fp64|); teacher-forced FP64 "
+                          "replay of every frame (device draws and ancestors); ancestors bit-exact",
+            "max_rel_err_vs_fp64": max(max(r["max_rel_est"], r["max_rel_loglik"]) for r in rows),
+            "tracks": rows, "seconds": time.perf_counter() - t0}
 
 
 def run_reference(args):
@@ -151,7 +214,7 @@ def run_reference(args):
     batch = workload(0, args.tracks)
     import oracle
     oracle.build()
-    ids = sample_ids(batch, args.ref_sample_tracks)
+    ids = sample_ids(batch, args.cpu_sample_tracks)
     for _ in range(args.warmup):
         cpu_run(batch, ids, threads)
     rates, times = [], []
@@ -165,12 +228,12 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded)",
             "config": {"workload": "batched uneven tracks: B=%d, T~U{50..2000}, N log-uniform "
-                                   "[128,8192], K=15, d=12; CPU sample of %d fixed tracks per step"
-                                   % (args.tracks, len(ids)),
+                                   "[128,8192], K=15, d=12; CPU sample of %d fixed tracks per step "
+                                   "(the GPU line's cpu_baseline sample)" % (args.tracks, len(ids)),
                        "tracks_per_step": len(ids), "track_frames_per_step": sub.n_frames_total},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": "%d fixed tracks per step (%d track-frames), FP64 restatement of "
-                                       "the reference CPU filter, OpenMP over tracks"
+                                       "the reference CPU filter, OpenMP over tracks, longest first"
                                        % (len(ids), sub.n_frames_total)},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
@@ -314,6 +377,17 @@ def run_gb300(args):
                                   "batched_over_plain": value / ws / pr}
         if not args.no_cpu:
             line["cpu_baseline"] = cpu_baseline(batch, args.cpu_sample_tracks, os.cpu_count() or 1)
+            # the metric's error bound, measured on full-length tracks of the same sample
+            acc_ids = accuracy_tracks(batch, sample_ids(batch, args.cpu_sample_tracks), args.accuracy_tracks)
+            line["accuracy"] = fp64_accuracy(batch, acc_ids, runner.block_threads, runner.ctas_per_sm,
+                                             runner.variant, full_est=outs[0].cpu().numpy())
+            line["max_rel_err_vs_fp64"] = line["accuracy"]["max_rel_err_vs_fp64"]
+        if not args.no_sweep:
+            rows = sweep_rows(args.bench_sweep_sizes, args.sweep_frames, 2, 3)
+            line["sweep"] = {"workload": "particle-count sweep, one track, T=%d, plain per-track path "
+                                         "(C-ABI call per frame, and the frame loop as one CUDA graph)"
+                                         % args.sweep_frames,
+                             "unit": "particle-frames/s", "rows": rows}
         if not args.no_adjoint:
             # the metric's "+adjoint" half: the mixture-KF gradient (B=1024, T=1000)
             a = adjoint_result(args)
@@ -336,14 +410,23 @@ def run_sweep(args):
     through the plain per-track C-ABI path (three grid-wide kernels per frame).
     Reports particle-frames/s and the HBM roofline fraction at 112 B per
     particle-frame."""
-    import torch
-    from mkfbodytracker_pdaf_gb300 import build, synth
-    from mkfbodytracker_pdaf_gb300.filters import BootstrapParticleFilter
+    from mkfbodytracker_pdaf_gb300 import build
     build.build()
+    peak, _ = load_peaks()
+    T = args.sweep_frames
+    rows = sweep_rows(args.sweep_sizes or list(range(12, 23, 2)), T, args.steps, args.warmup)
+    print(json.dumps({"workload": "particle-count sweep, one track, T=%d, plain per-track path: "
+                                  "one C-ABI call per frame, and the frame loop captured as one CUDA graph" % T,
+                      "unit": "particle-frames/s", "peak_hbm_GBps": peak, "rows": rows}), flush=True)
+
+
+def sweep_rows(sizes, T, steps, warmup):
+    import torch
+    from mkfbodytracker_pdaf_gb300 import synth
+    from mkfbodytracker_pdaf_gb300.filters import BootstrapParticleFilter
     peak, peak_kind = load_peaks()
     rows = []
-    T = args.sweep_frames
-    for lg in (args.sweep_sizes or list(range(12, 23, 2))):
+    for lg in sizes:
         N = 1 << lg
         batch = synth.sweep_batch(N, n_frames=T)
         t = batch.tracks[0]
@@ -358,16 +441,16 @@ def run_sweep(args):
 
         def timed(frames_fn):
             tot = 0.0
-            for rep in range(args.warmup + args.steps):
+            for rep in range(warmup + steps):
                 pf.reset()
                 e0, e1 = _events(torch)
                 e0.record()
                 frames_fn()
                 e1.record()
                 torch.cuda.synchronize()
-                if rep >= args.warmup:
+                if rep >= warmup:
                     tot += e0.elapsed_time(e1) / 1000
-            return tot / args.steps
+            return tot / steps
 
         def loop():
             for f in range(T):
@@ -386,9 +469,7 @@ def run_sweep(args):
                      "graph_ms_per_track": sec_g * 1e3, "graph_particle_frames_per_s": N * T / sec_g,
                      "graph_us_per_frame": sec_g / T * 1e6, "graph_frac_of_" + peak_kind + "_hbm": ach_g / peak,
                      "l2_resident": N <= (1 << 18)})
-    print(json.dumps({"workload": "particle-count sweep, one track, T=%d, plain per-track path: "
-                                  "one C-ABI call per frame, and the frame loop captured as one CUDA graph" % T,
-                      "unit": "particle-frames/s", "peak_hbm_GBps": peak, "rows": rows}), flush=True)
+    return rows
 
 
 def run_plain0(args):
@@ -600,12 +681,16 @@ def parse_args(argv=None):
     ap.add_argument("--ctas-per-sm", type=int, default=None)
     ap.add_argument("--variant", type=int, default=None, help="bit 0 float4 loads, bit 1 binary-search resampling")
     ap.add_argument("--cpu-sample-tracks", type=int, default=96)
-    ap.add_argument("--ref-sample-tracks", type=int, default=16)
+    ap.add_argument("--accuracy-tracks", type=int, default=4,
+                    help="full-length tracks of the CPU sample replayed in FP64 for the error bound")
     ap.add_argument("--plain-tracks", type=int, default=8)
     ap.add_argument("--plain-frames", type=int, default=300)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the mixture-KF adjoint summary of the default run")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the particle-count sweep rows of the default run")
+    ap.add_argument("--bench-sweep-sizes", type=int, nargs="*", default=[20, 22],
+                    help="log2 particle counts of the default run's sweep rows")
     ap.add_argument("--workload", default="batched", choices=["batched", "sweep", "plain0", "adjoint", "fit"])
     ap.add_argument("--sweep-frames", type=int, default=200)
     ap.add_argument("--sweep-sizes", type=int, nargs="*", default=None,
@@ -613,7 +698,7 @@ def parse_args(argv=None):
     ap.add_argument("--adj-tracks", type=int, default=1024)
     ap.add_argument("--adj-frames", type=int, default=1000)
     ap.add_argument("--adj-check-tracks", type=int, default=8)
-    ap.add_argument("--fd-dirs", type=int, default=16)
+    ap.add_argument("--fd-dirs", type=int, default=64)
     ap.add_argument("--fit-tracks", type=int, default=16384)
     ap.add_argument("--fit-frames", type=int, default=500)
     ap.add_argument("--fit-steps", type=int, default=200)

@@ -4,7 +4,7 @@ timing ones (max of the per-rank elapsed time, sum of the units processed),
 which run on whatever process group the caller initialised (NCCL on GPUs,
 gloo on CPU).
 
-The reference tracks one person per process (handTracker.cpp's ROS node); a
+The reference tracks one person per process (the ROS node of src/pfPoseTracker.cpp); a
 multi-person or multi-camera deployment runs independent trackers, which is
 exactly what a rank here is.
 """

@@ -123,6 +123,8 @@ def _declare(L):
     L.mko_bpf_loglik.restype = D
     L.mko_bpf_run_tracks.argtypes = [I, P, I, I, I, P, P, P, P, P, P, P, P,
                                      F, F, F, F, P, P, P, P, P, I]
+    L.mko_bpf_forced_frames.argtypes = [C.POINTER(BpfParams), I, I, P, P, P, P, P, P, P, P, P, P, P, P, I]
+    L.mko_bpf_prior_set.argtypes = [C.POINTER(BpfParams), I, P, P, P, I]
     L.mko_num_threads.restype = I
     L.mko_gaussian_blur_u8.argtypes = [P, I, I, P]
     L.mko_image_lookup.argtypes = [I, P, P, I, I, P]
@@ -362,6 +364,35 @@ def bpf_run_tracks(batch, track_ids, nthreads=0):
                          *[float(v) for v in m["cam"]], _p(_c(batch.det_off, np.int32)),
                          _p(_c(batch.det, np.float32)), _p(est), _p(ll), _p(ess), int(nthreads))
     return est, ll, ess
+
+
+def bpf_prior_set(params, eps, ucomp, nthreads=0):
+    """FP64 prior set (N, d) from the device's prior draws eps (N, d), ucomp (N)."""
+    eps = _c(eps, np.float32)
+    N = eps.shape[0]
+    x = np.zeros((N, params.d))
+    lib().mko_bpf_prior_set(C.byref(params), N, _p(eps), _p(_c(ucomp, np.float32)), _p(x), int(nthreads))
+    return x
+
+
+def bpf_forced_frames(params, x, anc_prev, eps, ucomp, anc, w_dev, det_off, det, nthreads=0):
+    """Teacher-forced FP64 replay of consecutive frames of one track
+    (mkf_oracle.h: mko_bpf_forced_frames).  x (N, d) is updated in place to
+    the set of the last frame.  eps (nf, N, d), ucomp / anc / w_dev (nf, N),
+    det_off (nf*J + 1) into det.  Returns est (nf, d), loglik, ess, w_err (nf)."""
+    eps = _c(eps, np.float32)
+    nf, N = eps.shape[0], eps.shape[1]
+    assert x.dtype == np.float64 and x.flags.c_contiguous and x.shape == (N, params.d)
+    est = np.zeros((nf, params.d))
+    ll = np.zeros(nf)
+    ess = np.zeros(nf)
+    werr = np.zeros(nf)
+    wd = _c(w_dev, np.float32) if w_dev is not None else None
+    lib().mko_bpf_forced_frames(C.byref(params), N, nf, _p(x), _p(_c(anc_prev, np.int32)), _p(eps),
+                                _p(_c(ucomp, np.float32)), _p(_c(anc, np.int32)), _p(wd),
+                                _p(_c(det_off, np.int32)), _p(_c(det, np.float32)), _p(est), _p(ll),
+                                _p(ess), _p(werr), int(nthreads))
+    return est, ll, ess, werr
 
 
 def num_threads():

@@ -594,6 +594,75 @@ double mko_bpf_loglik(const mko_bpf_params* p, const double* x, const int* det_o
   return ll;
 }
 
+void mko_bpf_prior_set(const mko_bpf_params* p, int N, const float* eps, const float* ucomp, double* x,
+                       int nthreads) {
+  int d = p->d;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+  for (int i = 0; i < N; ++i) {
+    double e[64];
+    for (int c = 0; c < d; ++c) e[c] = (double)eps[(size_t)i * d + c];
+    mko_bpf_prior(p, e, ucomp[i], x + (size_t)i * d);
+  }
+}
+
+void mko_bpf_forced_frames(const mko_bpf_params* p, int N, int nf, double* x, const int* anc_prev,
+                           const float* eps, const float* ucomp, const int* anc, const float* w_dev,
+                           const int* det_off, const float* det, double* est, double* loglik,
+                           double* ess, double* w_err, int nthreads) {
+  int d = p->d, J = p->J;
+#ifdef _OPENMP
+  if (nthreads <= 0) nthreads = omp_get_max_threads();
+#endif
+  double* xb = (double*)malloc(sizeof(double) * (size_t)N * d);
+  double* lw = (double*)malloc(sizeof(double) * (size_t)N);
+  const int* ap = anc_prev;
+  for (int f = 0; f < nf; ++f) {
+    const int* off = det_off + (size_t)f * J;
+    const float* ef = eps + (size_t)f * N * d;
+    const float* uf = ucomp + (size_t)f * N;
+    double mx = -INFINITY;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads) reduction(max : mx)
+#endif
+    for (int i = 0; i < N; ++i) {
+      double e[64];
+      double* xi = xb + (size_t)i * d;
+      memcpy(xi, x + (size_t)ap[i] * d, sizeof(double) * (size_t)d);
+      for (int c = 0; c < d; ++c) e[c] = (double)ef[(size_t)i * d + c];
+      mko_bpf_propagate(p, e, uf[i], xi);
+      lw[i] = mko_bpf_loglik(p, xi, off, det);
+      if (lw[i] > mx) mx = lw[i];
+    }
+    double S = 0.0, S2 = 0.0, werr = 0.0, e[64];
+    int wnan = 0;
+    for (int c = 0; c < d; ++c) e[c] = 0.0;
+    const float* wd = w_dev ? w_dev + (size_t)f * N : NULL;
+    /* fixed-order sums (deterministic for any thread count) */
+    for (int i = 0; i < N; ++i) {
+      double w = exp(lw[i] - mx);
+      S += w;
+      S2 += w * w;
+      for (int c = 0; c < d; ++c) e[c] += w * xb[(size_t)i * d + c];
+      if (wd) {
+        double dw = fabs(w - (double)wd[i]);
+        if (dw != dw) wnan = 1;          /* a NaN device weight reports NaN */
+        else if (dw > werr) werr = dw;
+      }
+    }
+    for (int c = 0; c < d; ++c) est[(size_t)f * d + c] = e[c] / S;
+    loglik[f] = mx + log(S) - log((double)N);
+    ess[f] = S * S / S2;
+    if (w_err) w_err[f] = wd ? (wnan ? NAN : werr) : 0.0;
+    memcpy(x, xb, sizeof(double) * (size_t)N * d);
+    ap = anc + (size_t)f * N;
+  }
+  free(xb);
+  free(lw);
+}
+
 int mko_num_threads(void) {
 #ifdef _OPENMP
   return omp_get_max_threads();

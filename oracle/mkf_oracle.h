@@ -157,6 +157,29 @@ void mko_bpf_run_tracks(int n_tracks, const mko_track* tracks, int d, int K, int
                         const int* det_off, const float* det,
                         float* est, float* loglik, float* ess, int nthreads);
 
+/* Teacher-forced FP64 replay of nf consecutive frames of one track (the loop
+ * of pf2D.cpp:148-210 with my_gmm.cpp:53-58's motion): each frame starts from
+ * this replay's own FP64 particle set, resampled with the ancestors the device
+ * chose, propagated with the device's draws, and scored, weighted and averaged
+ * in FP64.
+ *   x        N*d in/out: the set after the previous frame's propagation (the
+ *            prior set before frame 0); on return, the set of the last frame
+ *   anc_prev N: the ancestors chosen at the frame before the first (identity
+ *            before frame 0)
+ *   eps      nf*N*d, ucomp nf*N: the device's draws of the frames
+ *   anc      nf*N: the device's ancestors of each frame
+ *   w_dev    nf*N: the device's weights (normalised to max 1), or NULL
+ *   det_off  nf*J + 1 offsets of the frames' lists into det (pairs)
+ * Per frame out: est (nf*d), loglik, ess, and w_err = max_i |w_i - w_dev_i|
+ * (w normalised to max 1).  OpenMP over particles. */
+void mko_bpf_forced_frames(const mko_bpf_params* p, int N, int nf, double* x, const int* anc_prev,
+                           const float* eps, const float* ucomp, const int* anc, const float* w_dev,
+                           const int* det_off, const float* det, double* est, double* loglik,
+                           double* ess, double* w_err, int nthreads);
+/* the prior set of N particles from the device's prior draws (eps N*d, ucomp N) */
+void mko_bpf_prior_set(const mko_bpf_params* p, int N, const float* eps, const float* ucomp, double* x,
+                       int nthreads);
+
 int mko_num_threads(void);
 
 /* ---- A11: deterministic mixture KF (GPB1 over the K components) with PDAF

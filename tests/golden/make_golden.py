@@ -15,14 +15,14 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from mkfbodytracker_pdaf_gb300 import cvyaml  # noqa: E402
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-
-
 def main():
-    arms = cvyaml.load_reference_models(os.path.join(REF, "data13D_PCA_100000_15_12.yml"),
-                                        os.path.join(REF, "data23D_PCA_100000_15_12.yml"))
-    raw_left_gamma = cvyaml.load(os.path.join(REF, "data13D_PCA_100000_15_12.yml"))["gamma"].ravel()
-    cal = cvyaml.load(os.path.join(REF, "cal.yml"))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference checkout>")
+    ref = sys.argv[1]
+    arms = cvyaml.load_reference_models(os.path.join(ref, "data13D_PCA_100000_15_12.yml"),
+                                        os.path.join(ref, "data23D_PCA_100000_15_12.yml"))
+    raw_left_gamma = cvyaml.load(os.path.join(ref, "data13D_PCA_100000_15_12.yml"))["gamma"].ravel()
+    cal = cvyaml.load(os.path.join(ref, "cal.yml"))
     out = {}
     for a, arm in enumerate(arms):
         for k, v in arm.items():

@@ -104,3 +104,51 @@ def test_fit_resumes_from_a_saved_state(cuda, olib, tmp_path):
     assert st.step == 2 and st.theta.size == th.size
     resumed, _ = g.fit_adam(None, 2, lr=1e-2, resume=st)
     np.testing.assert_array_equal(resumed.cpu().numpy(), full)
+
+
+def _setup_body8(olib, n_tracks=3, T=40, seed=9):
+    """The motion-model-fitting shape: K=32 components over d=24 (8 joints x 3D,
+    head and both hands measured), lambda=5."""
+    from mkfbodytracker_pdaf_gb300 import mixkf, synth
+    b = synth.make_mix_batch(seed, n_tracks, T, K=32, d=24, lam=5.0, pd=0.9, layout="body8")
+    tt = b.theta_true()
+    om = olib.MixModel(tt["mu"], tt["a"], tt["Lq"], tt["sigma"], tt["pi"], tt["S0"], J=b.J)
+    th = om.theta()
+    g = mixkf.MixtureKF(b, tt["pi"], tt["S0"])
+    return b, om, th, g
+
+
+def test_body8_k32_forward_and_gradient_match_fp64(cuda, olib):
+    """d=24, K=32, J=3: per-track logL against the FP64 forward, the gradient
+    against the FP64 adjoint along random directions, and per parameter block
+    against FP64 central differences (relative step 1e-6)."""
+    b, om, th, g = _setup_body8(olib)
+    g.set_theta(th)
+    g.forward()
+    ll = g.ll.cpu().numpy()
+    grad = g.backward().cpu().numpy()
+    L, ll_ref, gref = olib.mix_batch(om, b, grad=True)
+    np.testing.assert_allclose(ll, ll_ref, rtol=1e-5)
+    assert g.status() == 0
+    rng = np.random.default_rng(11)
+    rel = []
+    for _ in range(16):
+        v = rng.standard_normal(th.size)
+        v /= np.linalg.norm(v)
+        rel.append(abs(v @ grad - v @ gref) / max(abs(v @ gref), 1e-6))
+    print("body8 K32 max rel err vs FP64 adjoint: %.3g" % max(rel))
+    assert max(rel) < 1e-3, max(rel)
+    K, d = 32, 24
+    blocks = {"mu": slice(0, K * d), "a": slice(K * d, 2 * K * d), "Lq": slice(2 * K * d, th.size - 1),
+              "sigma": slice(th.size - 1, th.size)}
+    for name, sl in blocks.items():
+        v = np.zeros(th.size)
+        v[sl] = rng.standard_normal(v[sl].size)
+        v /= np.linalg.norm(v)
+        h = 1e-6 * max(1.0, np.abs(th).max())
+        Lp, _ = olib.mix_batch(om.with_theta(th + h * v), b)
+        Lm, _ = olib.mix_batch(om.with_theta(th - h * v), b)
+        fd = (Lp - Lm) / (2 * h)
+        assert abs(v @ gref - fd) <= 1e-6 * max(1.0, abs(fd)), (name, v @ gref, fd)
+        print("body8 K32 block %s: rel err vs FD %.3g" % (name, abs(v @ grad - fd) / max(1.0, abs(fd))))
+        assert abs(v @ grad - fd) <= 1e-3 * max(1.0, abs(fd)), (name, v @ grad, fd)

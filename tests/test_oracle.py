@@ -241,6 +241,55 @@ def test_bpf_pieces_vs_numpy(olib):
         assert abs(ll - tot) < 1e-6 * max(1, abs(tot))
 
 
+def test_bpf_forced_frames_replays_the_frame_loop(olib):
+    """The C teacher-forced replay (used for the full-horizon GPU check) equals
+    the frame loop of pf2D.cpp:148-210 written out per particle here, when it
+    is given that loop's own draws and ancestors; it also reports the weight
+    error against given weights, split over two calls (chunked replay)."""
+    from mkfbodytracker_pdaf_gb300 import synth
+    b = synth.make_bpf_batch(5, [40], [7], [4.0], [0.9])
+    m, t = b.model, b.tracks[0]
+    prm, keep = olib.bpf_params(m, 0, t)
+    d, J, N, T = m["d"], m["J"], 40, 7
+    seed, trk = int(t["seed"]), int(t["track_id"])
+
+    def draws(f):
+        e, u = zip(*[olib.particle_draws(seed, trk, f, i, d) for i in range(N)])
+        return np.asarray(e, np.float32), np.asarray(u, np.float32)
+
+    e0, u0 = draws(0xFFFFFFFF)
+    x = np.stack([olib.bpf_prior(prm, e0[i].astype(np.float64), u0[i]) for i in range(N)])
+    np.testing.assert_array_equal(olib.bpf_prior_set(prm, e0, u0), x)
+    anc = np.arange(N)
+    eps_all, uc_all, anc_all, w_all, est_ref, ll_ref = [], [], [], [], [], []
+    for f in range(T):
+        eps, uc = draws(f)
+        xn = np.stack([olib.bpf_propagate(prm, x[anc[i]], eps[i].astype(np.float64), uc[i]) for i in range(N)])
+        off = b.det_off[f * J:f * J + J + 1].astype(np.int32)
+        ll = np.array([olib.bpf_loglik(prm, xn[i], off, b.det) for i in range(N)])
+        w = np.exp(ll - ll.max())
+        est_ref.append((w[:, None] * xn).sum(0) / w.sum())
+        ll_ref.append(ll.max() + np.log(w.sum()) - np.log(N))
+        U = int(olib.draw_block(seed, trk, f, 0xFFFFFFFF, 0x100)[0])
+        anc, _ = olib.resample(w, N, U)
+        eps_all.append(eps); uc_all.append(uc); anc_all.append(anc); w_all.append(w.astype(np.float32))
+        x = xn
+    x2 = olib.bpf_prior_set(prm, e0, u0)
+    outs = []
+    for f0, f1 in ((0, 3), (3, T)):       # two chunks: the state carries over
+        prev = np.arange(N, dtype=np.int32) if f0 == 0 else anc_all[f0 - 1]
+        outs.append(olib.bpf_forced_frames(prm, x2, prev, np.stack(eps_all[f0:f1]), np.stack(uc_all[f0:f1]),
+                                           np.stack(anc_all[f0:f1]), np.stack(w_all[f0:f1]),
+                                           b.det_off[f0 * J:f1 * J + 1], b.det))
+    est = np.concatenate([o[0] for o in outs])
+    ll = np.concatenate([o[1] for o in outs])
+    werr = np.concatenate([o[3] for o in outs])
+    np.testing.assert_allclose(est, np.stack(est_ref), rtol=0, atol=1e-12)
+    np.testing.assert_allclose(ll, ll_ref, rtol=1e-13)
+    assert werr.max() <= 2 ** -24 and werr.max() > 0            # float32 rounding of the given weights
+    np.testing.assert_allclose(x2, x, rtol=0, atol=1e-12)
+
+
 # ----------------------------------------------------------------- RBPF update (A8)
 def _numpy_rbpf(model, x, P, z, ind, U_anc, olib):
     """Independent numpy restatement of pf2DRao.cpp:125-158 given the indicators."""

@@ -113,7 +113,7 @@ def test_reference_arm_json_line_on_cpu(monkeypatch, capsys):
         monkeypatch.delenv(k, raising=False)
     small = synth.make_bpf_batch(7, [64, 100, 150], [5, 3, 4], [2.0, 3.0, 1.0], [0.9, 0.8, 0.95])
     monkeypatch.setattr(bench, "workload", lambda rank, n: small)
-    args = bench.parse_args(["--impl", "reference", "--steps", "2", "--warmup", "3", "--ref-sample-tracks", "2"])
+    args = bench.parse_args(["--impl", "reference", "--steps", "2", "--warmup", "3", "--cpu-sample-tracks", "2"])
     bench.run_reference(args)
     lines = [ln for ln in capsys.readouterr().out.splitlines() if ln.startswith("{")]
     assert len(lines) == 1
@@ -140,3 +140,10 @@ def test_cpu_baseline_record_on_cpu():
     cb = bench.cpu_baseline(small, 3, 2)
     assert cb["value"] > 0 and cb["unit"] == bench.UNIT and cb["cores"] == 2 and cb["kind"] == "port"
     assert cb["sample"].startswith("3 fixed tracks")
+    # the sample runs longest first (particle-frames), the same one in both arms
+    ids = bench.sample_ids(small, 3)
+    cost = [small.tracks[b]["n_particles"] * small.tracks[b]["n_frames"] for b in ids]
+    assert cost == sorted(cost, reverse=True)
+    acc = bench.accuracy_tracks(small, bench.sample_ids(small, 4))
+    assert len(acc) == len(set(acc)) and 1 <= len(acc) <= 4
+    assert max(small.tracks[b]["n_frames"] for b in acc) == max(t["n_frames"] for t in small.tracks)
