@@ -393,7 +393,8 @@ def run_gb300(args):
             a = adjoint_result(args)
             line["adjoint"] = {k: a[k] for k in ("workload", "forward_ms", "backward_ms", "backward_over_forward",
                                                  "gradient_evals_per_s", "checkpoint_stride", "fd_directions",
-                                                 "grad_rel_err_vs_fd", "grad_rel_err_vs_cpu_adjoint")}
+                                                 "grad_rel_err_vs_fd", "grad_rel_err_vs_cpu_adjoint",
+                                                 "gradient_accuracy")}
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.barrier()
@@ -567,19 +568,50 @@ def adjoint_result(args):
         bwd.append(e1.elapsed_time(e2))
     L_gpu = g.forward().item()
     grad = g.backward().cpu().numpy()
-    # accuracy on a subset (FP64 CPU adjoint and central differences, 64 directions)
+    # accuracy on a subset (FP64 CPU adjoint and central differences, 64
+    # directions), at the generating parameters and at the fitting start point
+    # (means + N(0, 0.3), covariances x 1.5)
     sub = list(range(min(args.adj_check_tracks, b.n_tracks)))
     sb = synth.MixBatch(b.gmm, [b.tracks[i] for i in sub], b.Bm, b.mm, b.det_off, b.det, b.truth)
     gs = mixkf.MixtureKF(sb, tt["pi"], tt["S0"])
+    K, d = om.K, om.d
+    rng0 = np.random.default_rng(4)
+    th_start = mixkf.theta_from(tt["mu"] + rng0.normal(0, 0.3, tt["mu"].shape), tt["a"], tt["Lq"] * np.sqrt(1.5),
+                                tt["sigma"] * np.sqrt(1.5))
+    points = {}
+    for name, thp in (("at_generating_params", th), ("at_fit_start", th_start)):
+        points[name] = grad_accuracy(oracle, om.with_theta(thp), thp, sb, gs, args.fd_dirs, K, d)
+    tf = float(np.median(fwd))
+    tb = float(np.median(bwd))
+    acc = points["at_generating_params"]
+    return {
+        "workload": "mixture-KF logL and adjoint, B=%d x T=%d, K=15, d=12, PDAF <=16 candidates, FP32 + FP64 sums"
+                    % (b.n_tracks, args.adj_frames),
+        "forward_ms": tf, "backward_ms": tb, "backward_over_forward": tb / tf,
+        "track_frames_per_s_forward": b.n_frames_total / tf * 1e3,
+        "gradient_evals_per_s": 1e3 / (tf + tb), "logL": L_gpu,
+        "checkpoint_stride": g.checkpoint_stride,
+        "check_subset_tracks": len(sub), "logL_rel_err_subset": acc["logL_rel_err"],
+        "fd_directions": args.fd_dirs,
+        "grad_rel_err_vs_fd": acc["rel_err_vs_fd"],
+        "grad_rel_err_vs_cpu_adjoint": acc["rel_err_vs_cpu_adjoint"],
+        "gradient_accuracy": points}
+
+
+def grad_accuracy(oracle, om, th, sb, gs, ndirs, K, d):
+    """GPU gradient on the subset batch sb against the FP64 CPU adjoint and
+    FP64 central differences (relative step 1e-6) along ndirs random unit
+    directions, plus the normwise error per parameter block."""
     gs.set_theta(th)
     gs.forward()
     grad_s = gs.backward().cpu().numpy()
+    L_sub_gpu = float(gs.ll.sum().item())
     t0 = time.perf_counter()
     L_c, _, gref = oracle.mix_batch(om, sb, grad=True)
     cpu_adj_s = time.perf_counter() - t0
     rng = np.random.default_rng(64)
     rel_fd, rel_adj, rel_cpu_fd = [], [], []
-    for _ in range(args.fd_dirs):
+    for _ in range(ndirs):
         v = rng.standard_normal(th.size)
         v /= np.linalg.norm(v)
         h = 1e-6 * max(1.0, np.abs(th).max())
@@ -589,33 +621,37 @@ def adjoint_result(args):
         rel_fd.append(abs(v @ grad_s - fd) / max(abs(fd), 1e-9))
         rel_cpu_fd.append(abs(v @ gref - fd) / max(abs(fd), 1e-9))
         rel_adj.append(abs(v @ grad_s - v @ gref) / max(abs(v @ gref), 1e-9))
-    L_sub_gpu = float(gs.ll.sum().item())
-    tf = float(np.median(fwd))
-    tb = float(np.median(bwd))
-    return {
-        "workload": "mixture-KF logL and adjoint, B=%d x T=%d, K=15, d=12, PDAF <=16 candidates, FP32 + FP64 sums"
-                    % (b.n_tracks, args.adj_frames),
-        "forward_ms": tf, "backward_ms": tb, "backward_over_forward": tb / tf,
-        "track_frames_per_s_forward": b.n_frames_total / tf * 1e3,
-        "gradient_evals_per_s": 1e3 / (tf + tb), "logL": L_gpu,
-        "checkpoint_stride": g.checkpoint_stride,
-        "check_subset_tracks": len(sub), "logL_rel_err_subset": abs(L_sub_gpu - L_c) / abs(L_c),
-        "fd_directions": args.fd_dirs,
-        "grad_rel_err_vs_fd": {"median": float(np.median(rel_fd)), "max": float(np.max(rel_fd))},
-        "grad_rel_err_vs_cpu_adjoint": {"median": float(np.median(rel_adj)), "max": float(np.max(rel_adj))},
-        "cpu_adjoint_rel_err_vs_fd": {"median": float(np.median(rel_cpu_fd)), "max": float(np.max(rel_cpu_fd))},
-        "cpu_adjoint_s_subset": cpu_adj_s}
+    DD = d * (d + 1) // 2
+    blocks = {"mu": slice(0, K * d), "a": slice(K * d, 2 * K * d), "Lq": slice(2 * K * d, 2 * K * d + K * DD),
+              "sigma": slice(th.size - 1, th.size)}
+    normwise = {k: float(np.linalg.norm(grad_s[sl] - gref[sl]) / max(np.linalg.norm(gref[sl]), 1e-300))
+                for k, sl in blocks.items()}
+    med = lambda x: {"median": float(np.median(x)), "max": float(np.max(x))}
+    return {"logL_rel_err": abs(L_sub_gpu - L_c) / abs(L_c), "grad_norm": float(np.linalg.norm(gref)),
+            "rel_err_vs_fd": med(rel_fd), "rel_err_vs_cpu_adjoint": med(rel_adj),
+            "cpu_adjoint_rel_err_vs_fd": med(rel_cpu_fd),
+            "normwise_rel_err_vs_cpu_adjoint": normwise,
+            "normwise_rel_err_total": float(np.linalg.norm(grad_s - gref) / np.linalg.norm(gref)),
+            "cpu_adjoint_s": cpu_adj_s}
 
 
 def run_fit(args):
-    """Motion-model fit: fit the motion model (K=32, d=24) by gradient on the device
-    from data the filter's own generative model produced."""
+    """Motion-model fit: fit the motion model by gradient on the device from
+    data the filter's own generative model produced.  --fit-case config4: K=32,
+    d=24 (8 joints x 3D), lambda=5; --fit-case exact: one component (K=1,
+    d=12), no clutter, detection probability 0.999, where the filter's
+    likelihood is the model's own (an EKF whose linearisation error is small at
+    these depths), so that the fit can be judged by parameter recovery."""
     import torch
     from mkfbodytracker_pdaf_gb300 import build, mixkf, synth
     build.build()
-    b = synth.fit_batch_k32(n_tracks=args.fit_tracks, T=args.fit_frames)
+    if args.fit_case == "exact":
+        K, d = 1, 12
+        b = synth.fit_batch_exact(n_tracks=args.fit_tracks, T=args.fit_frames)
+    else:
+        K, d = 32, 24
+        b = synth.fit_batch_k32(n_tracks=args.fit_tracks, T=args.fit_frames)
     tt = b.theta_true()
-    K, d = 32, 24
     th_true = mixkf.theta_from(tt["mu"], tt["a"], tt["Lq"], tt["sigma"])
     rng = np.random.default_rng(4)
     mu0 = tt["mu"] + rng.normal(0, 0.3, tt["mu"].shape)
@@ -658,10 +694,12 @@ def run_fit(args):
                "a_mae": err(a_f, tt["a"][perm]), "Q_mae": err(Qf, Qt[perm]),
                "components_relabelled": int((perm != np.arange(K)).sum())}
     print(json.dumps({
-        "workload": "motion-model fit: K=32, d=24 from B=%d x T=%d, %d Adam steps (lr %g) on the device"
-                    % (b.n_tracks, args.fit_frames, args.fit_steps, args.fit_lr),
+        "workload": "motion-model fit (%s): K=%d, d=%d from B=%d x T=%d, %d Adam steps (lr %g) on the device"
+                    % (args.fit_case, K, d, b.n_tracks, args.fit_frames, args.fit_steps, args.fit_lr),
         "seconds_total": wall, "seconds_per_gradient_eval": wall / args.fit_steps,
         "logL_init": L0, "logL_final": Lf, "logL_true_params": Ltrue, "logL_history": hist,
+        "logL_final_minus_true": Lf - Ltrue, "n_params": int(th_true.size),
+        "half_n_params": 0.5 * th_true.size,
         "recovery": {"mu_mae_init": err(mu_0, tt["mu"]), "mu_mae_final": err(mu_f, tt["mu"]),
                      "a_mae_init": 0.0, "a_mae_final": err(a_f, tt["a"]),
                      "Q_mae_init": err(Q0, Qt), "Q_mae_final": err(Qf, Qt),
@@ -699,13 +737,18 @@ def parse_args(argv=None):
     ap.add_argument("--adj-frames", type=int, default=1000)
     ap.add_argument("--adj-check-tracks", type=int, default=8)
     ap.add_argument("--fd-dirs", type=int, default=64)
-    ap.add_argument("--fit-tracks", type=int, default=16384)
-    ap.add_argument("--fit-frames", type=int, default=500)
-    ap.add_argument("--fit-steps", type=int, default=200)
+    ap.add_argument("--fit-case", default="config4", choices=["config4", "exact"])
+    ap.add_argument("--fit-tracks", type=int, default=None, help="default: 16384 (config4), 128 (exact)")
+    ap.add_argument("--fit-frames", type=int, default=None, help="default: 500 (config4), 200 (exact)")
+    ap.add_argument("--fit-steps", type=int, default=None, help="default: 200 (config4), 400 (exact)")
     ap.add_argument("--fit-lr", type=float, default=0.02)
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
+    exact = args.fit_case == "exact"
+    args.fit_tracks = args.fit_tracks or (128 if exact else 16384)
+    args.fit_frames = args.fit_frames or (200 if exact else 500)
+    args.fit_steps = args.fit_steps or (400 if exact else 200)
     return args
 
 

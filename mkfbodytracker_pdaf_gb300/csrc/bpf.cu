@@ -598,13 +598,26 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
         if (fb || Qt == 0) {
           for (int i = tid; i < N; i += TB) sA[i] = resample_fallback_index(U, i, N);
         } else {
-          // four targets per thread at a time (i, i + TB, i + 2 TB, i + 3 TB)
+          // four targets per thread at a time (i, i + TB, i + 2 TB, i + 3 TB),
+          // their thresholds walked along the stride (one division per frame);
+          // a target past N - 1 is searched (in bounds) but not stored
           const RsThresh th = rs_thresh_setup(Qt, N, U);
+          const RsStep st4 = rs_step_setup(th, 4u * (uint32_t)TB);
+          RsWalk wk[4];
+          wk[0] = rs_walk_init(th, (uint32_t)tid);
+          {
+            const RsStep st1 = rs_step_setup(th, (uint32_t)TB);
+#pragma unroll
+            for (int g = 1; g < 4; ++g) { wk[g] = wk[g - 1]; rs_walk_next(th, st1, wk[g]); }
+          }
           for (int i0 = tid; i0 < N; i0 += 4 * TB) {
             uint64_t T4[4];
             int r4[4];
 #pragma unroll
-            for (int g = 0; g < 4; ++g) T4[g] = rs_threshold(th, (uint32_t)min(i0 + g * TB, N - 1));
+            for (int g = 0; g < 4; ++g) {
+              T4[g] = rs_walk_threshold(th, wk[g]);
+              rs_walk_next(th, st4, wk[g]);
+            }
             search_u64_multi<4>(sQ, N, T4, r4);
 #pragma unroll
             for (int g = 0; g < 4; ++g)
@@ -981,7 +994,27 @@ constexpr int kTileB = 4096;
 using namespace mkf;
 
 struct mkf_bpf { BpfHandle h; };
+// Host-buffer runs are split into chunks of tracks by frame range, so that
+// the copies of one chunk overlap the kernels of the others: chunk c covers
+// frames [cut[c], cut[c+1]) and holds the tracks inside that range; its
+// tracks run longest-first from order_chunks[ofs[c] .. ofs[c+1]).
+constexpr int kMaxHostChunks = 8;
+struct HostChunks {
+  int n;                                     // 0: not planned yet; 1: one chunk (no overlap)
+  long long cut[kMaxHostChunks + 1];
+  int ofs[kMaxHostChunks + 1];
+  int* order;                                // device, n_tracks entries
+  int* counters;                             // device, kMaxHostChunks work counters
+  cudaStream_t h2d, d2h, comp[2];
+  cudaEvent_t start, copied[kMaxHostChunks], done[kMaxHostChunks], out_done;
+};
+
 struct mkf_bpf_batch {
+  mkf_bpf_batch() : m(), n_tracks(0), Nmax(0), d(0), K(0), J(0), G(0), tb(0), ctas_per_sm(0), meta(nullptr),
+                    fbase(nullptr), seed(nullptr), obs(nullptr), order(nullptr), counter(nullptr), scratch(nullptr),
+                    scratch_slots(0), scratch_sets(1), last_grid(0), variant(0), dbg_track(-1), dbg_w(nullptr),
+                    dbg_anc(nullptr), h_det_off_dev(nullptr), h_det_dev(nullptr), det_cap(0), d_est(nullptr),
+                    d_ll(nullptr), d_ess(nullptr), d_status(nullptr), hc() {}
   DevModels m;
   int n_tracks, Nmax, d, K, J;
   long long G;
@@ -994,6 +1027,7 @@ struct mkf_bpf_batch {
   int* counter;
   float* scratch;
   size_t scratch_slots;
+  int scratch_sets;                          // slot sets of concurrent launches (1, or 2 for chunked runs)
   int last_grid;
   int variant;
   int dbg_track;
@@ -1005,6 +1039,8 @@ struct mkf_bpf_batch {
   size_t det_cap;
   float *d_est, *d_ll, *d_ess;
   int* d_status;
+  HostChunks hc;
+  std::vector<mkf_bpf_track> tracks;         // host copy, for planning the chunks
 };
 
 static PView make_view(const DevModels& m, int mi) {
@@ -1284,14 +1320,15 @@ extern "C" int mkf_bpf_batch_create(const mkf_bpf_models* models, int n_tracks, 
   }
   mkf_bpf_batch* B = new (std::nothrow) mkf_bpf_batch();
   if (!B) return MKF_ERR_NOMEM;
-  memset(B, 0, sizeof(*B));
   int st = build_models(models, B->m);
   if (st) { free_models(B->m); delete B; return st; }
   B->n_tracks = n_tracks; B->Nmax = (Nmax + 31) & ~31; B->d = models->d; B->K = models->K; B->J = models->J;
   B->G = n_frames_total;
   // the fastest shape measured on GB300 for the uneven-track workload
   B->tb = 256; B->ctas_per_sm = 3; B->variant = MKF_BPF_VEC_LOADS | MKF_BPF_SEARCH | MKF_BPF_LOWSMEM;
+  B->scratch_sets = 1;
   B->dbg_track = -1;
+  B->tracks.assign(tracks, tracks + n_tracks);
   std::vector<int4> meta(n_tracks);
   std::vector<long long> fb(n_tracks);
   std::vector<unsigned long long> sd(n_tracks);
@@ -1351,8 +1388,12 @@ extern "C" int mkf_bpf_batch_set_debug(mkf_bpf_batch_t B, int track, float* d_w,
   return MKF_OK;
 }
 
+// One launch of the persistent kernel over a.n_tracks tracks (a.order,
+// a.counter set by the caller).  slot_set selects one of B->scratch_sets
+// disjoint sets of per-CTA slots, so that launches that may overlap on the
+// GPU never share a slot.
 template <int D, bool DIAG, int TBMAX, int MINB, bool VEC, bool SEARCH, bool PAIR, bool LOW>
-static int launch_batched_v(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
+static int launch_batched_v(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s, int slot_set) {
   auto kern = bpf_batched_kernel<D, DIAG, TBMAX, MINB, VEC, SEARCH, PAIR, LOW>;
   size_t smem = batched_smem_bytes(D, B->Nmax, B->K, B->J, DIAG, SEARCH, LOW);
   MKF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1363,10 +1404,11 @@ static int launch_batched_v(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
   MKF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, B->tb, smem));
   if (occ < 1) { set_error("mkf_bpf_batch_run: block shape does not fit on an SM"); return MKF_ERR_ARG; }
   int per_sm = B->ctas_per_sm > 0 ? std::min(B->ctas_per_sm, occ) : occ;
-  long long grid = (long long)num_sms() * per_sm;
-  grid = std::min<long long>(grid, B->n_tracks);
-  // per CTA: two state buffers (2 D Nmax floats); LOW adds Nmax ancestors
-  size_t need = (size_t)grid * (2 * D + (LOW ? 1 : 0)) * B->Nmax;
+  const long long full = (long long)num_sms() * per_sm;
+  // per CTA: two state buffers (2 D Nmax floats); LOW adds Nmax ancestors.
+  // Every set is sized for the full grid of the whole batch.
+  const size_t per_set = (size_t)std::min<long long>(full, B->n_tracks) * (2 * D + (LOW ? 1 : 0)) * B->Nmax;
+  const size_t need = per_set * (size_t)B->scratch_sets;
   if (need > B->scratch_slots) {
     if (B->scratch) cudaFree(B->scratch);
     B->scratch = nullptr;
@@ -1374,10 +1416,13 @@ static int launch_batched_v(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
     MKF_CUDA(cudaMalloc(&B->scratch, need * sizeof(float)));
     B->scratch_slots = need;
   }
-  a.scratch = B->scratch;
-  a.anc = LOW ? reinterpret_cast<int*>(B->scratch + (size_t)grid * 2 * D * B->Nmax) : nullptr;
+  const long long grid = std::min<long long>(full, a.n_tracks);
+  if (grid < 1) return MKF_OK;
+  float* base = B->scratch + (size_t)slot_set * per_set;
+  a.scratch = base;
+  a.anc = LOW ? reinterpret_cast<int*>(base + (size_t)grid * 2 * D * B->Nmax) : nullptr;
   B->last_grid = (int)grid;
-  MKF_CUDA(cudaMemsetAsync(B->counter, 0, sizeof(int), s));
+  MKF_CUDA(cudaMemsetAsync(a.counter, 0, sizeof(int), s));
   kern<<<(int)grid, B->tb, smem, s>>>(a);
   MKF_CHECK_LAUNCH("mkf_bpf_batch_run: batched kernel");
   return MKF_OK;
@@ -1390,32 +1435,50 @@ static int launch_batched_v(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
 // threads at 2 CTAs per SM, up to 512 at 1, which keeps the number of compiled
 // kernels, and the build time, down.
 template <int D, bool DIAG, bool VEC, bool SEARCH, bool PAIR = false, bool LOW = false, bool ALL = false>
-static int launch_shape(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
+static int launch_shape(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s, int set) {
   if constexpr (ALL) {
-    if (B->tb > 384) return launch_batched_v<D, DIAG, 512, 1, VEC, SEARCH, PAIR, LOW>(B, a, s);
-    if (B->tb > 256) return launch_batched_v<D, DIAG, 384, 2, VEC, SEARCH, PAIR, LOW>(B, a, s);
-    if (B->ctas_per_sm >= 3) return launch_batched_v<D, DIAG, 256, 3, VEC, SEARCH, PAIR, LOW>(B, a, s);
-    return launch_batched_v<D, DIAG, 256, 2, VEC, SEARCH, PAIR, LOW>(B, a, s);
+    if (B->tb > 384) return launch_batched_v<D, DIAG, 512, 1, VEC, SEARCH, PAIR, LOW>(B, a, s, set);
+    if (B->tb > 256) return launch_batched_v<D, DIAG, 384, 2, VEC, SEARCH, PAIR, LOW>(B, a, s, set);
+    if (B->ctas_per_sm >= 3) return launch_batched_v<D, DIAG, 256, 3, VEC, SEARCH, PAIR, LOW>(B, a, s, set);
+    return launch_batched_v<D, DIAG, 256, 2, VEC, SEARCH, PAIR, LOW>(B, a, s, set);
   }
-  if (B->tb > 256) return launch_batched_v<D, DIAG, 512, 1, VEC, SEARCH, PAIR, LOW>(B, a, s);
-  return launch_batched_v<D, DIAG, 256, 2, VEC, SEARCH, PAIR, LOW>(B, a, s);
+  if (B->tb > 256) return launch_batched_v<D, DIAG, 512, 1, VEC, SEARCH, PAIR, LOW>(B, a, s, set);
+  return launch_batched_v<D, DIAG, 256, 2, VEC, SEARCH, PAIR, LOW>(B, a, s, set);
 }
 
 // the load-width and resampler variants are compiled for the diagonal-noise
 // d = 12 model only
 template <int D, bool DIAG>
-static int launch_batched(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s) {
+static int launch_batched(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s, int set) {
   if constexpr (D == 12 && DIAG) {
     const bool vec = (B->variant & MKF_BPF_VEC_LOADS) != 0, search = (B->variant & MKF_BPF_SEARCH) != 0;
-    if (B->variant & MKF_BPF_PAIR) return launch_shape<D, DIAG, true, true, true>(B, a, s);
-    if (B->variant & MKF_BPF_LOWSMEM) return launch_shape<D, DIAG, true, true, false, true, true>(B, a, s);
-    if (vec && search) return launch_shape<D, DIAG, true, true, false, false, true>(B, a, s);
-    if (vec) return launch_shape<D, DIAG, true, false>(B, a, s);
-    if (search) return launch_shape<D, DIAG, false, true>(B, a, s);
-    return launch_shape<D, DIAG, false, false>(B, a, s);
+    if (B->variant & MKF_BPF_PAIR) return launch_shape<D, DIAG, true, true, true>(B, a, s, set);
+    if (B->variant & MKF_BPF_LOWSMEM) return launch_shape<D, DIAG, true, true, false, true, true>(B, a, s, set);
+    if (vec && search) return launch_shape<D, DIAG, true, true, false, false, true>(B, a, s, set);
+    if (vec) return launch_shape<D, DIAG, true, false>(B, a, s, set);
+    if (search) return launch_shape<D, DIAG, false, true>(B, a, s, set);
+    return launch_shape<D, DIAG, false, false>(B, a, s, set);
   } else {
-    return launch_shape<D, DIAG, true, false>(B, a, s);
+    return launch_shape<D, DIAG, true, false>(B, a, s, set);
   }
+}
+
+static int launch_any(mkf_bpf_batch* B, BatchArgs& a, cudaStream_t s, int set) {
+  if (B->d == 12) return B->m.diag ? launch_batched<12, true>(B, a, s, set) : launch_batched<12, false>(B, a, s, set);
+  return B->m.diag ? launch_batched<24, true>(B, a, s, set) : launch_batched<24, false>(B, a, s, set);
+}
+
+static BatchArgs batch_args(const mkf_bpf_batch* B, const int* d_det_off, const float* d_det, float* d_est,
+                            float* d_loglik, float* d_ess, int* d_status) {
+  BatchArgs a;
+  memset(&a, 0, sizeof(a));
+  a.n_tracks = B->n_tracks; a.K = B->K; a.J = B->J; a.Nmax = B->Nmax;
+  a.meta = B->meta; a.fbase = B->fbase; a.seed = B->seed; a.obs = B->obs;
+  a.order = B->order; a.counter = B->counter; a.m = B->m;
+  a.det_off = d_det_off; a.det = reinterpret_cast<const float2*>(d_det);
+  a.est = d_est; a.loglik = d_loglik; a.ess = d_ess; a.status = d_status;
+  a.dbg_track = B->dbg_track; a.dbg_w = B->dbg_w; a.dbg_anc = B->dbg_anc;
+  return a;
 }
 
 extern "C" int mkf_bpf_batch_set_variant(mkf_bpf_batch_t B, int flags) {
@@ -1435,17 +1498,85 @@ extern "C" int mkf_bpf_batch_run(mkf_bpf_batch_t B, const int* d_det_off, const 
                                  mkf_stream_t stream) {
   MKF_RANGE("mkf_bpf_batch_run");
   MKF_ARG(B && d_det_off && d_est && d_loglik && d_ess && d_status, "mkf_bpf_batch_run: null argument");
-  BatchArgs a;
-  memset(&a, 0, sizeof(a));
-  a.n_tracks = B->n_tracks; a.K = B->K; a.J = B->J; a.Nmax = B->Nmax;
-  a.meta = B->meta; a.fbase = B->fbase; a.seed = B->seed; a.obs = B->obs;
-  a.order = B->order; a.counter = B->counter; a.m = B->m;
-  a.det_off = d_det_off; a.det = reinterpret_cast<const float2*>(d_det);
-  a.est = d_est; a.loglik = d_loglik; a.ess = d_ess; a.status = d_status;
-  a.dbg_track = B->dbg_track; a.dbg_w = B->dbg_w; a.dbg_anc = B->dbg_anc;
-  cudaStream_t s = (cudaStream_t)stream;
-  if (B->d == 12) return B->m.diag ? launch_batched<12, true>(B, a, s) : launch_batched<12, false>(B, a, s);
-  return B->m.diag ? launch_batched<24, true>(B, a, s) : launch_batched<24, false>(B, a, s);
+  BatchArgs a = batch_args(B, d_det_off, d_det, d_est, d_loglik, d_ess, d_status);
+  return launch_any(B, a, (cudaStream_t)stream, 0);
+}
+
+// Plan the chunks of host-buffer runs (once per handle).  Tracks sorted by
+// first frame must occupy disjoint frame ranges; otherwise (or for tiny
+// batches) one chunk, copied before and after a single launch.
+static int plan_host_chunks(mkf_bpf_batch* B) {
+  HostChunks& c = B->hc;
+  const int n = B->n_tracks;
+  std::vector<int> idx(n);
+  for (int b = 0; b < n; ++b) idx[b] = b;
+  std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return B->tracks[x].frame_base < B->tracks[y].frame_base; });
+  bool disjoint = true;
+  for (int k = 0; k + 1 < n; ++k) {
+    const mkf_bpf_track& t = B->tracks[idx[k]];
+    if (B->tracks[idx[k + 1]].frame_base < t.frame_base + t.n_frames) { disjoint = false; break; }
+  }
+  int nc = disjoint ? std::min(kMaxHostChunks, n / 16) : 1;
+  if (nc < 1) nc = 1;
+  // cut the frame-sorted tracks into nc runs of about equal frame counts
+  long long tot = 0;
+  for (int b = 0; b < n; ++b) tot += B->tracks[b].n_frames;
+  std::vector<int> ord;
+  ord.reserve(n);
+  c.cut[0] = 0;
+  c.ofs[0] = 0;
+  int k = 0;
+  long long acc = 0;
+  for (int ci = 0; ci < nc; ++ci) {
+    const int first = k;
+    const long long target = (ci == nc - 1) ? tot : tot * (ci + 1) / nc;
+    while (k < n && (acc < target || k == first)) acc += B->tracks[idx[k++]].n_frames;
+    if (ci == nc - 1) k = n;
+    std::vector<int> seg(idx.begin() + first, idx.begin() + k);
+    std::stable_sort(seg.begin(), seg.end(), [&](int x, int y) {
+      return (long long)B->tracks[x].n_particles * B->tracks[x].n_frames >
+             (long long)B->tracks[y].n_particles * B->tracks[y].n_frames;
+    });
+    ord.insert(ord.end(), seg.begin(), seg.end());
+    c.ofs[ci + 1] = k;
+    // frame cut: the end of this chunk's last track (the whole range for one chunk)
+    if (nc == 1) c.cut[ci + 1] = B->G;
+    else if (ci == nc - 1) c.cut[ci + 1] = B->G;
+    else {
+      const mkf_bpf_track& t = B->tracks[idx[k - 1]];
+      c.cut[ci + 1] = t.frame_base + t.n_frames;
+    }
+  }
+  c.n = nc;
+  MKF_CUDA(cudaMalloc(&c.order, std::max(1, n) * sizeof(int)));
+  MKF_CUDA(cudaMemcpy(c.order, ord.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+  MKF_CUDA(cudaMalloc(&c.counters, kMaxHostChunks * sizeof(int)));
+  MKF_CUDA(cudaStreamCreateWithFlags(&c.h2d, cudaStreamNonBlocking));
+  MKF_CUDA(cudaStreamCreateWithFlags(&c.d2h, cudaStreamNonBlocking));
+  MKF_CUDA(cudaStreamCreateWithFlags(&c.comp[0], cudaStreamNonBlocking));
+  MKF_CUDA(cudaStreamCreateWithFlags(&c.comp[1], cudaStreamNonBlocking));
+  MKF_CUDA(cudaEventCreateWithFlags(&c.start, cudaEventDisableTiming));
+  MKF_CUDA(cudaEventCreateWithFlags(&c.out_done, cudaEventDisableTiming));
+  for (int i = 0; i < kMaxHostChunks; ++i) {
+    MKF_CUDA(cudaEventCreateWithFlags(&c.copied[i], cudaEventDisableTiming));
+    MKF_CUDA(cudaEventCreateWithFlags(&c.done[i], cudaEventDisableTiming));
+  }
+  if (nc > 1) B->scratch_sets = 2;
+  return MKF_OK;
+}
+
+static void free_host_chunks(HostChunks& c) {
+  if (c.order) cudaFree(c.order);
+  if (c.counters) cudaFree(c.counters);
+  cudaStream_t ss[] = {c.h2d, c.d2h, c.comp[0], c.comp[1]};
+  for (cudaStream_t x : ss) if (x) cudaStreamDestroy(x);
+  if (c.start) cudaEventDestroy(c.start);
+  if (c.out_done) cudaEventDestroy(c.out_done);
+  for (int i = 0; i < kMaxHostChunks; ++i) {
+    if (c.copied[i]) cudaEventDestroy(c.copied[i]);
+    if (c.done[i]) cudaEventDestroy(c.done[i]);
+  }
+  c = HostChunks();
 }
 
 extern "C" int mkf_bpf_batch_run_host(mkf_bpf_batch_t B, const int* det_off, const float* det, int64_t n_det,
@@ -1456,6 +1587,7 @@ extern "C" int mkf_bpf_batch_run_host(mkf_bpf_batch_t B, const int* det_off, con
   MKF_ARG(n_det <= 0x7FFFFFFFLL, "mkf_bpf_batch_run_host: more than 2^31 - 1 detections (int32 offsets)");
   cudaStream_t s = (cudaStream_t)stream;
   const size_t G = (size_t)B->G, J = (size_t)B->J, d = (size_t)B->d;
+  MKF_ARG(det_off[0] >= 0 && (int64_t)det_off[G * J] <= n_det, "mkf_bpf_batch_run_host: det_off outside [0, n_det]");
   if (!B->h_det_off_dev) {
     MKF_CUDA(cudaMalloc(&B->h_det_off_dev, (G * J + 1) * sizeof(int)));
     MKF_CUDA(cudaMalloc(&B->d_est, G * d * sizeof(float)));
@@ -1469,14 +1601,55 @@ extern "C" int mkf_bpf_batch_run_host(mkf_bpf_batch_t B, const int* det_off, con
     MKF_CUDA(cudaMalloc(&B->h_det_dev, std::max<size_t>(1, (size_t)n_det) * 2 * sizeof(float)));
     B->det_cap = (size_t)n_det;
   }
-  MKF_CUDA(cudaMemcpyAsync(B->h_det_off_dev, det_off, (G * J + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
-  MKF_CUDA(cudaMemcpyAsync(B->h_det_dev, det, (size_t)n_det * 2 * sizeof(float), cudaMemcpyHostToDevice, s));
-  int st = mkf_bpf_batch_run(B, B->h_det_off_dev, B->h_det_dev, B->d_est, B->d_ll, B->d_ess, B->d_status, stream);
-  if (st) return st;
-  MKF_CUDA(cudaMemcpyAsync(est, B->d_est, G * d * sizeof(float), cudaMemcpyDeviceToHost, s));
-  MKF_CUDA(cudaMemcpyAsync(loglik, B->d_ll, G * sizeof(float), cudaMemcpyDeviceToHost, s));
-  MKF_CUDA(cudaMemcpyAsync(ess, B->d_ess, G * sizeof(float), cudaMemcpyDeviceToHost, s));
-  MKF_CUDA(cudaMemcpyAsync(status, B->d_status, B->n_tracks * sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (B->hc.n == 0) {
+    int st = plan_host_chunks(B);
+    if (st) { free_host_chunks(B->hc); return st; }
+  }
+  HostChunks& c = B->hc;
+  // Chunk ci: copy its frames' lists in (h2d stream), run its tracks (compute
+  // streams alternate, so a chunk's launch can fill the SMs that the previous
+  // chunk's last tracks leave idle), copy its frames' outputs out (d2h stream).
+  // Every track of chunk ci lies in frames [cut[ci], cut[ci+1]) and the copies
+  // complete in order, so the launch waits on its own chunk's copy event only.
+  MKF_CUDA(cudaEventRecord(c.start, s));
+  MKF_CUDA(cudaStreamWaitEvent(c.h2d, c.start, 0));
+  MKF_CUDA(cudaStreamWaitEvent(c.comp[0], c.start, 0));
+  MKF_CUDA(cudaStreamWaitEvent(c.comp[1], c.start, 0));
+  MKF_CUDA(cudaStreamWaitEvent(c.d2h, c.start, 0));
+  for (int ci = 0; ci < c.n; ++ci) {
+    const size_t g0 = (size_t)c.cut[ci], g1 = (size_t)c.cut[ci + 1];
+    const size_t o0 = (size_t)det_off[g0 * J], o1 = (size_t)det_off[g1 * J];
+    // offsets (g0 J, g1 J] (from 0 for the first chunk): a frame's lists end
+    // at the next frame's first offset, so each chunk also takes its end entry
+    const size_t e0 = ci == 0 ? 0 : g0 * J + 1, e1 = g1 * J + 1;
+    if (e1 > e0)
+      MKF_CUDA(cudaMemcpyAsync(B->h_det_off_dev + e0, det_off + e0, (e1 - e0) * sizeof(int), cudaMemcpyHostToDevice, c.h2d));
+    if (o1 > o0)
+      MKF_CUDA(cudaMemcpyAsync(B->h_det_dev + 2 * o0, det + 2 * o0, (o1 - o0) * 2 * sizeof(float), cudaMemcpyHostToDevice,
+                               c.h2d));
+    MKF_CUDA(cudaEventRecord(c.copied[ci], c.h2d));
+  }
+  for (int ci = 0; ci < c.n; ++ci) {
+    cudaStream_t cs = c.comp[ci & 1];
+    MKF_CUDA(cudaStreamWaitEvent(cs, c.copied[ci], 0));
+    BatchArgs a = batch_args(B, B->h_det_off_dev, B->h_det_dev, B->d_est, B->d_ll, B->d_ess, B->d_status);
+    a.order = c.order + c.ofs[ci];
+    a.n_tracks = c.ofs[ci + 1] - c.ofs[ci];
+    a.counter = c.counters + ci;
+    int st = launch_any(B, a, cs, ci & 1);
+    if (st) return st;
+    MKF_CUDA(cudaEventRecord(c.done[ci], cs));
+    const size_t g0 = (size_t)c.cut[ci], g1 = (size_t)c.cut[ci + 1];
+    MKF_CUDA(cudaStreamWaitEvent(c.d2h, c.done[ci], 0));
+    if (g1 > g0) {
+      MKF_CUDA(cudaMemcpyAsync(est + g0 * d, B->d_est + g0 * d, (g1 - g0) * d * sizeof(float), cudaMemcpyDeviceToHost, c.d2h));
+      MKF_CUDA(cudaMemcpyAsync(loglik + g0, B->d_ll + g0, (g1 - g0) * sizeof(float), cudaMemcpyDeviceToHost, c.d2h));
+      MKF_CUDA(cudaMemcpyAsync(ess + g0, B->d_ess + g0, (g1 - g0) * sizeof(float), cudaMemcpyDeviceToHost, c.d2h));
+    }
+  }
+  MKF_CUDA(cudaMemcpyAsync(status, B->d_status, B->n_tracks * sizeof(int), cudaMemcpyDeviceToHost, c.d2h));
+  MKF_CUDA(cudaEventRecord(c.out_done, c.d2h));
+  MKF_CUDA(cudaStreamWaitEvent(s, c.out_done, 0));
   MKF_CUDA(cudaStreamSynchronize(s));
   return MKF_OK;
 }
@@ -1486,6 +1659,7 @@ extern "C" int mkf_bpf_batch_destroy(mkf_bpf_batch_t B) {
   void* ps[] = {B->meta, B->fbase, B->seed, B->obs, B->order, B->counter, B->scratch,
                 B->h_det_off_dev, B->h_det_dev, B->d_est, B->d_ll, B->d_ess, B->d_status};
   for (void* p : ps) if (p) cudaFree(p);
+  free_host_chunks(B->hc);
   free_models(B->m);
   delete B;
   return MKF_OK;

@@ -378,6 +378,45 @@ MKF_HD uint64_t rs_threshold(const RsThresh& t, uint32_t i) {
   const uint32_t g = V / t.N, h = V - g * t.N;
   return (uint64_t)i * t.A + t.C + g + (((h | t.low) != 0u) ? 1u : 0u);
 }
+// rs_threshold along a stride of targets i, i + S, i + 2S, ... without a
+// division per target: with S r = dq N + dr, V_{i+S} = V_i + S r, so
+// floor(V / N) grows by dq plus the carry of (V_i mod N) + dr.  The walk keeps
+// base = i A + C + floor(V_i / N) and h = V_i mod N (< N), so any target index
+// (also past N - 1) stays in 32-bit arithmetic; needs S r < 2^32 and N <= 65536.
+struct RsStep {
+  uint64_t dA;
+  uint32_t dq, dr;
+};
+struct RsWalk {
+  uint64_t base;
+  uint32_t h;
+};
+MKF_HD RsStep rs_step_setup(const RsThresh& t, uint32_t S) {
+  RsStep st;
+  const uint32_t v = S * t.r;
+  st.dq = v / t.N;
+  st.dr = v - st.dq * t.N;
+  st.dA = (uint64_t)S * t.A;
+  return st;
+}
+MKF_HD RsWalk rs_walk_init(const RsThresh& t, uint32_t i) {
+  const uint32_t V = i * t.r + t.s;
+  const uint32_t g = V / t.N;
+  RsWalk w;
+  w.h = V - g * t.N;
+  w.base = (uint64_t)i * t.A + t.C + g;
+  return w;
+}
+MKF_HD uint64_t rs_walk_threshold(const RsThresh& t, const RsWalk& w) {
+  return w.base + (((w.h | t.low) != 0u) ? 1u : 0u);
+}
+MKF_HD void rs_walk_next(const RsThresh& t, const RsStep& st, RsWalk& w) {
+  uint32_t h = w.h + st.dr;
+  const uint32_t c = (h >= t.N) ? 1u : 0u;
+  w.h = h - (c ? t.N : 0u);
+  w.base += st.dA + st.dq + c;
+}
+
 // The same threshold for any N <= 2^22 (V_i < 2^45): floor(V_i / N) from a
 // float estimate (relative error <= 4 2^-24, so within one of the truth) and
 // exact integer correction.

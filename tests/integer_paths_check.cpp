@@ -4,6 +4,8 @@
 //    rs_threshold64 (N <= 2^22) against T_i = ceil((i 2^32 + U) Qt / (N 2^32))
 //    in 128-bit integers; random N, Qt in [1, 2^62) (at most 2^22 weights of
 //    40 bits each), U and i, plus the extremes of each;
+//  - stride: the division-free walk of those thresholds along a stride of
+//    targets (rs_walk_*) against the same 128-bit T_i, past N - 1 included;
 //  - quantize: quantize39(w) against floor(w 2^39) in double (exact: a float
 //    times a power of two) for weights w <= 1 (its domain): random, boundary,
 //    subnormal, zero, negative, -inf and NaN; quantize_f32 / quantize_f64 (the
@@ -66,6 +68,31 @@ static void thresholds(std::mt19937_64& rng) {
           ++n;
         }
   std::printf("thresholds %lld %lld\n", bad, n);
+}
+
+// the strided walk (rs_walk_*) against T_i at every target of the stride,
+// including targets past N - 1 (they are formed, then left unused, by the kernels)
+static void stride_walk(std::mt19937_64& rng) {
+  long long bad = 0, n = 0;
+  for (int it = 0; it < 3000; ++it) {
+    const int N = 1 + (int)(rng() % (it % 3 == 0 ? 65536 : 8192));
+    const uint64_t Qt = 1 + (rng() >> (2 + rng() % 60));
+    const uint32_t U = (uint32_t)rng();
+    const uint32_t S = 32u * (1u + (uint32_t)(rng() % 64));       // 32 .. 2048
+    const uint32_t i0 = (uint32_t)(rng() % S);
+    const mkf::RsThresh th = mkf::rs_thresh_setup(Qt, N, U);
+    const mkf::RsStep st = mkf::rs_step_setup(th, S);
+    mkf::RsWalk w = mkf::rs_walk_init(th, i0);
+    for (uint32_t i = i0; i < (uint32_t)N + 4 * S; i += S) {
+      const unsigned __int128 num = ((((unsigned __int128)i) << 32) + U) * (unsigned __int128)Qt;
+      const unsigned __int128 den = ((unsigned __int128)(uint64_t)N) << 32;
+      const unsigned __int128 ref = (num + den - 1) / den;
+      bad += mkf::rs_walk_threshold(th, w) != (uint64_t)ref;
+      ++n;
+      mkf::rs_walk_next(th, st, w);
+    }
+  }
+  std::printf("stride %lld %lld\n", bad, n);
 }
 
 static uint64_t quantize_ref(float w) {
@@ -233,6 +260,7 @@ int main() {
   philox();
   walk(rng);
   thresholds(rng);
+  stride_walk(rng);
   quantize(rng);
   search(rng);
   pick(rng);

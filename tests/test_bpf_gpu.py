@@ -196,6 +196,30 @@ def test_batched_host_buffers_match_device_run(cuda):
     assert err < 0.6, err
 
 
+def test_batched_host_run_chunks_in_any_track_order(cuda):
+    """The host-buffer run copies and launches per chunk of frames (tracks
+    grouped by frame range); with the tracks listed out of frame order the
+    outputs still equal the single device-resident launch bit for bit, on
+    repeated calls."""
+    from mkfbodytracker_pdaf_gb300 import synth
+    from mkfbodytracker_pdaf_gb300.filters import BatchedBootstrapPF
+    torch = cuda
+    base = synth.uneven_tracks_batch(n_tracks=96, t_range=(5, 60), n_range=(64, 2048))
+    perm = np.random.default_rng(5).permutation(base.n_tracks)
+    batch = synth.BpfBatch(base.model, [base.tracks[b] for b in perm], base.det_off, base.det, base.truth)
+    runner = BatchedBootstrapPF(batch)
+    est, ll, ess, st = runner.run(*runner.device_inputs())
+    G = batch.n_frames_total
+    for _ in range(2):
+        outs = (np.full((G, 12), np.nan, np.float32), np.zeros(G, np.float32), np.zeros(G, np.float32),
+                np.zeros(batch.n_tracks, np.int32))
+        runner.run_host(batch.det_off.astype(np.int32), batch.det.astype(np.float32), outs)
+        np.testing.assert_array_equal(outs[0], est.cpu().numpy())
+        np.testing.assert_array_equal(outs[1], ll.cpu().numpy())
+        np.testing.assert_array_equal(outs[2], ess.cpu().numpy())
+        np.testing.assert_array_equal(outs[3], st.cpu().numpy())
+
+
 def test_batched_variant_flags_checked(cuda):
     """The search with global ancestors needs float4 loads and the search, not pairs."""
     from mkfbodytracker_pdaf_gb300 import _native as N, synth

@@ -31,7 +31,7 @@ def results(tmp_path_factory):
     return {name: (int(bad), int(n)) for name, bad, n in (line.split() for line in out.strip().splitlines())}
 
 
-@pytest.mark.parametrize("piece,min_cases", [("thresholds", 400000), ("quantize", 1000000), ("search", 400000),
+@pytest.mark.parametrize("piece,min_cases", [("thresholds", 400000), ("stride", 100000), ("quantize", 1000000), ("search", 400000),
                                              ("pick", 6000000), ("philox", 3), ("walk", 1000000)])
 def test_against_independent_restatement(results, piece, min_cases):
     bad, n = results[piece]

@@ -152,3 +152,35 @@ def test_body8_k32_forward_and_gradient_match_fp64(cuda, olib):
         assert abs(v @ gref - fd) <= 1e-6 * max(1.0, abs(fd)), (name, v @ gref, fd)
         print("body8 K32 block %s: rel err vs FD %.3g" % (name, abs(v @ grad - fd) / max(1.0, abs(fd))))
         assert abs(v @ grad - fd) <= 1e-3 * max(1.0, abs(fd)), (name, v @ grad, fd)
+
+
+def test_fit_recovers_the_model_when_the_likelihood_is_exact(cuda, olib):
+    """One component, no clutter, detection probability 0.999: the filter's
+    likelihood is the model's own (up to the EKF linearisation), so fitting by
+    the device adjoint from the config-4-style start (means + N(0, 0.3),
+    covariances x 1.5) must recover the parameters to their statistical
+    precision, and the fitted logL must exceed the generating parameters' by
+    about half the parameter count (the maximum-likelihood excess), not more."""
+    from mkfbodytracker_pdaf_gb300 import mixkf, synth
+    b = synth.fit_batch_exact(n_tracks=64, T=150)
+    tt = b.theta_true()
+    K, d = 1, 12
+    th_true = mixkf.theta_from(tt["mu"], tt["a"], tt["Lq"], tt["sigma"])
+    rng = np.random.default_rng(4)
+    th0 = mixkf.theta_from(tt["mu"] + rng.normal(0, 0.3, tt["mu"].shape), tt["a"], tt["Lq"] * np.sqrt(1.5),
+                           tt["sigma"] * np.sqrt(1.5))
+    g = mixkf.MixtureKF(b, tt["pi"], tt["S0"])
+    g.set_theta(th_true)
+    L_true = g.forward().item()
+    th, _ = g.fit_adam(th0, 200, lr=0.02)
+    thf = th.cpu().numpy()
+    g.set_theta(thf)
+    L_fit = g.forward().item()
+    mu0 = mixkf.theta_split(th0, K, d)[0]
+    mu_f, a_f, _, s_f = mixkf.theta_split(thf, K, d)
+    mae0, mae = np.abs(mu0 - tt["mu"]).mean(), np.abs(mu_f - tt["mu"]).mean()
+    print("exact-case fit: mu MAE %.4f -> %.4f, sigma %.3f, a MAE %.4f, logL fit - true %.1f (half the parameters %.1f)"
+          % (mae0, mae, s_f, np.abs(a_f - tt["a"]).mean(), L_fit - L_true, 0.5 * th_true.size))
+    assert mae < 0.4 * mae0
+    assert abs(s_f - tt["sigma"]) < 0.2
+    assert 0.0 < L_fit - L_true < th_true.size
