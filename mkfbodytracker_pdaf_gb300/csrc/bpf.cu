@@ -994,27 +994,28 @@ constexpr int kTileB = 4096;
 using namespace mkf;
 
 struct mkf_bpf { BpfHandle h; };
-// Host-buffer runs are split into chunks of tracks by frame range, so that
-// the copies of one chunk overlap the kernels of the others: chunk c covers
-// frames [cut[c], cut[c+1]) and holds the tracks inside that range; its
-// tracks run longest-first from order_chunks[ofs[c] .. ofs[c+1]).
-constexpr int kMaxHostChunks = 8;
-struct HostChunks {
-  int n;                                     // 0: not planned yet; 1: one chunk (no overlap)
-  long long cut[kMaxHostChunks + 1];
-  int ofs[kMaxHostChunks + 1];
-  int* order;                                // device, n_tracks entries
-  int* counters;                             // device, kMaxHostChunks work counters
-  cudaStream_t h2d, d2h, comp[2];
-  cudaEvent_t start, copied[kMaxHostChunks], done[kMaxHostChunks], out_done;
+// Host-buffer runs keep the device run's longest-first track order and split it
+// in two launches: the head (the first grid-size tracks of that order, one per
+// persistent CTA) starts as soon as its own tracks' lists are copied (one small
+// copy per track, into buffer 0), while the whole input is copied in bulk
+// (buffer 1) for the tail launch, whose CTAs take the SMs that head CTAs free.
+struct HostRun {
+  bool ready;
+  int head;                                  // tracks in the head launch
+  int* counters;                             // device, 2 work counters
+  int* h_det_off_dev[2];
+  float* h_det_dev[2];
+  size_t det_cap;
+  cudaStream_t copy, comp[2];
+  cudaEvent_t start, copied[2], done[2];
 };
 
 struct mkf_bpf_batch {
   mkf_bpf_batch() : m(), n_tracks(0), Nmax(0), d(0), K(0), J(0), G(0), tb(0), ctas_per_sm(0), meta(nullptr),
                     fbase(nullptr), seed(nullptr), obs(nullptr), order(nullptr), counter(nullptr), scratch(nullptr),
                     scratch_slots(0), scratch_sets(1), last_grid(0), variant(0), dbg_track(-1), dbg_w(nullptr),
-                    dbg_anc(nullptr), h_det_off_dev(nullptr), h_det_dev(nullptr), det_cap(0), d_est(nullptr),
-                    d_ll(nullptr), d_ess(nullptr), d_status(nullptr), hc() {}
+                    dbg_anc(nullptr), d_est(nullptr),
+                    d_ll(nullptr), d_ess(nullptr), d_status(nullptr), hr() {}
   DevModels m;
   int n_tracks, Nmax, d, K, J;
   long long G;
@@ -1027,20 +1028,18 @@ struct mkf_bpf_batch {
   int* counter;
   float* scratch;
   size_t scratch_slots;
-  int scratch_sets;                          // slot sets of concurrent launches (1, or 2 for chunked runs)
+  int scratch_sets;                          // slot sets of concurrent launches (1, or 2 for host-buffer runs)
   int last_grid;
   int variant;
   int dbg_track;
   float* dbg_w;
   int* dbg_anc;
-  // host-run staging
-  int* h_det_off_dev;
-  float* h_det_dev;
-  size_t det_cap;
+  // host-run staging of outputs (when the caller's buffers are not mapped)
   float *d_est, *d_ll, *d_ess;
   int* d_status;
-  HostChunks hc;
-  std::vector<mkf_bpf_track> tracks;         // host copy, for planning the chunks
+  HostRun hr;
+  std::vector<mkf_bpf_track> tracks;         // host copy: the head tracks' frame ranges
+  std::vector<int> order_h;                  // host copy of order
 };
 
 static PView make_view(const DevModels& m, int mi) {
@@ -1357,6 +1356,7 @@ extern "C" int mkf_bpf_batch_create(const mkf_bpf_models* models, int n_tracks, 
   if (e == cudaSuccess) e = cudaMemcpy(B->seed, sd.data(), n_tracks * sizeof(unsigned long long), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(B->obs, ob.data(), n_tracks * sizeof(float4), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(B->order, order.data(), n_tracks * sizeof(int), cudaMemcpyHostToDevice);
+  B->order_h = order;
   if (e != cudaSuccess) {
     mkf_bpf_batch_destroy(B);
     return cuda_fail(e, "mkf_bpf_batch_create: allocation", __FILE__, __LINE__);
@@ -1502,81 +1502,45 @@ extern "C" int mkf_bpf_batch_run(mkf_bpf_batch_t B, const int* d_det_off, const 
   return launch_any(B, a, (cudaStream_t)stream, 0);
 }
 
-// Plan the chunks of host-buffer runs (once per handle).  Tracks sorted by
-// first frame must occupy disjoint frame ranges; otherwise (or for tiny
-// batches) one chunk, copied before and after a single launch.
-static int plan_host_chunks(mkf_bpf_batch* B) {
-  HostChunks& c = B->hc;
-  const int n = B->n_tracks;
-  std::vector<int> idx(n);
-  for (int b = 0; b < n; ++b) idx[b] = b;
-  std::stable_sort(idx.begin(), idx.end(), [&](int x, int y) { return B->tracks[x].frame_base < B->tracks[y].frame_base; });
-  bool disjoint = true;
-  for (int k = 0; k + 1 < n; ++k) {
-    const mkf_bpf_track& t = B->tracks[idx[k]];
-    if (B->tracks[idx[k + 1]].frame_base < t.frame_base + t.n_frames) { disjoint = false; break; }
+static void free_host_run(HostRun& r) {
+  void* ps[] = {r.counters, r.h_det_off_dev[0], r.h_det_off_dev[1], r.h_det_dev[0], r.h_det_dev[1]};
+  for (void* p : ps) if (p) cudaFree(p);
+  cudaStream_t ss[] = {r.copy, r.comp[0], r.comp[1]};
+  for (cudaStream_t x : ss) if (x) cudaStreamDestroy(x);
+  cudaEvent_t es[] = {r.start, r.copied[0], r.copied[1], r.done[0], r.done[1]};
+  for (cudaEvent_t x : es) if (x) cudaEventDestroy(x);
+  r = HostRun();
+}
+
+static int setup_host_run(mkf_bpf_batch* B) {
+  HostRun& r = B->hr;
+  const size_t G = (size_t)B->G, J = (size_t)B->J, d = (size_t)B->d;
+  MKF_CUDA(cudaMalloc(&r.counters, 2 * sizeof(int)));
+  for (int k = 0; k < 2; ++k) MKF_CUDA(cudaMalloc(&r.h_det_off_dev[k], (G * J + 1) * sizeof(int)));
+  if (!B->d_est) MKF_CUDA(cudaMalloc(&B->d_est, G * d * sizeof(float)));
+  if (!B->d_ll) MKF_CUDA(cudaMalloc(&B->d_ll, G * sizeof(float)));
+  if (!B->d_ess) MKF_CUDA(cudaMalloc(&B->d_ess, G * sizeof(float)));
+  if (!B->d_status) MKF_CUDA(cudaMalloc(&B->d_status, B->n_tracks * sizeof(int)));
+  MKF_CUDA(cudaStreamCreateWithFlags(&r.copy, cudaStreamNonBlocking));
+  for (int k = 0; k < 2; ++k) {
+    MKF_CUDA(cudaStreamCreateWithFlags(&r.comp[k], cudaStreamNonBlocking));
+    MKF_CUDA(cudaEventCreateWithFlags(&r.copied[k], cudaEventDisableTiming));
+    MKF_CUDA(cudaEventCreateWithFlags(&r.done[k], cudaEventDisableTiming));
   }
-  int nc = disjoint ? std::min(kMaxHostChunks, n / 16) : 1;
-  if (nc < 1) nc = 1;
-  // cut the frame-sorted tracks into nc runs of about equal frame counts
-  long long tot = 0;
-  for (int b = 0; b < n; ++b) tot += B->tracks[b].n_frames;
-  std::vector<int> ord;
-  ord.reserve(n);
-  c.cut[0] = 0;
-  c.ofs[0] = 0;
-  int k = 0;
-  long long acc = 0;
-  for (int ci = 0; ci < nc; ++ci) {
-    const int first = k;
-    const long long target = (ci == nc - 1) ? tot : tot * (ci + 1) / nc;
-    while (k < n && (acc < target || k == first)) acc += B->tracks[idx[k++]].n_frames;
-    if (ci == nc - 1) k = n;
-    std::vector<int> seg(idx.begin() + first, idx.begin() + k);
-    std::stable_sort(seg.begin(), seg.end(), [&](int x, int y) {
-      return (long long)B->tracks[x].n_particles * B->tracks[x].n_frames >
-             (long long)B->tracks[y].n_particles * B->tracks[y].n_frames;
-    });
-    ord.insert(ord.end(), seg.begin(), seg.end());
-    c.ofs[ci + 1] = k;
-    // frame cut: the end of this chunk's last track (the whole range for one chunk)
-    if (nc == 1) c.cut[ci + 1] = B->G;
-    else if (ci == nc - 1) c.cut[ci + 1] = B->G;
-    else {
-      const mkf_bpf_track& t = B->tracks[idx[k - 1]];
-      c.cut[ci + 1] = t.frame_base + t.n_frames;
-    }
-  }
-  c.n = nc;
-  MKF_CUDA(cudaMalloc(&c.order, std::max(1, n) * sizeof(int)));
-  MKF_CUDA(cudaMemcpy(c.order, ord.data(), n * sizeof(int), cudaMemcpyHostToDevice));
-  MKF_CUDA(cudaMalloc(&c.counters, kMaxHostChunks * sizeof(int)));
-  MKF_CUDA(cudaStreamCreateWithFlags(&c.h2d, cudaStreamNonBlocking));
-  MKF_CUDA(cudaStreamCreateWithFlags(&c.d2h, cudaStreamNonBlocking));
-  MKF_CUDA(cudaStreamCreateWithFlags(&c.comp[0], cudaStreamNonBlocking));
-  MKF_CUDA(cudaStreamCreateWithFlags(&c.comp[1], cudaStreamNonBlocking));
-  MKF_CUDA(cudaEventCreateWithFlags(&c.start, cudaEventDisableTiming));
-  MKF_CUDA(cudaEventCreateWithFlags(&c.out_done, cudaEventDisableTiming));
-  for (int i = 0; i < kMaxHostChunks; ++i) {
-    MKF_CUDA(cudaEventCreateWithFlags(&c.copied[i], cudaEventDisableTiming));
-    MKF_CUDA(cudaEventCreateWithFlags(&c.done[i], cudaEventDisableTiming));
-  }
-  if (nc > 1) B->scratch_sets = 2;
+  MKF_CUDA(cudaEventCreateWithFlags(&r.start, cudaEventDisableTiming));
+  // the head: one track per CTA of the persistent grid (an upper bound of it)
+  r.head = std::min(B->n_tracks, num_sms() * std::max(1, B->ctas_per_sm > 0 ? B->ctas_per_sm : 3));
+  B->scratch_sets = 2;
+  r.ready = true;
   return MKF_OK;
 }
 
-static void free_host_chunks(HostChunks& c) {
-  if (c.order) cudaFree(c.order);
-  if (c.counters) cudaFree(c.counters);
-  cudaStream_t ss[] = {c.h2d, c.d2h, c.comp[0], c.comp[1]};
-  for (cudaStream_t x : ss) if (x) cudaStreamDestroy(x);
-  if (c.start) cudaEventDestroy(c.start);
-  if (c.out_done) cudaEventDestroy(c.out_done);
-  for (int i = 0; i < kMaxHostChunks; ++i) {
-    if (c.copied[i]) cudaEventDestroy(c.copied[i]);
-    if (c.done[i]) cudaEventDestroy(c.done[i]);
-  }
-  c = HostChunks();
+// device address of a host buffer that the GPU can write directly (pinned and
+// mapped), or null
+static void* mapped_device_ptr(void* host) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, host) != cudaSuccess) { cudaGetLastError(); return nullptr; }
+  return (at.type == cudaMemoryTypeHost) ? at.devicePointer : nullptr;
 }
 
 extern "C" int mkf_bpf_batch_run_host(mkf_bpf_batch_t B, const int* det_off, const float* det, int64_t n_det,
@@ -1588,68 +1552,71 @@ extern "C" int mkf_bpf_batch_run_host(mkf_bpf_batch_t B, const int* det_off, con
   cudaStream_t s = (cudaStream_t)stream;
   const size_t G = (size_t)B->G, J = (size_t)B->J, d = (size_t)B->d;
   MKF_ARG(det_off[0] >= 0 && (int64_t)det_off[G * J] <= n_det, "mkf_bpf_batch_run_host: det_off outside [0, n_det]");
-  if (!B->h_det_off_dev) {
-    MKF_CUDA(cudaMalloc(&B->h_det_off_dev, (G * J + 1) * sizeof(int)));
-    MKF_CUDA(cudaMalloc(&B->d_est, G * d * sizeof(float)));
-    MKF_CUDA(cudaMalloc(&B->d_ll, G * sizeof(float)));
-    MKF_CUDA(cudaMalloc(&B->d_ess, G * sizeof(float)));
-    MKF_CUDA(cudaMalloc(&B->d_status, B->n_tracks * sizeof(int)));
+  HostRun& r = B->hr;
+  if (!r.ready) {
+    int st = setup_host_run(B);
+    if (st) { free_host_run(r); return st; }
   }
-  if ((size_t)n_det > B->det_cap || !B->h_det_dev) {
-    if (B->h_det_dev) cudaFree(B->h_det_dev);
-    B->h_det_dev = nullptr;
-    MKF_CUDA(cudaMalloc(&B->h_det_dev, std::max<size_t>(1, (size_t)n_det) * 2 * sizeof(float)));
-    B->det_cap = (size_t)n_det;
-  }
-  if (B->hc.n == 0) {
-    int st = plan_host_chunks(B);
-    if (st) { free_host_chunks(B->hc); return st; }
-  }
-  HostChunks& c = B->hc;
-  // Chunk ci: copy its frames' lists in (h2d stream), run its tracks (compute
-  // streams alternate, so a chunk's launch can fill the SMs that the previous
-  // chunk's last tracks leave idle), copy its frames' outputs out (d2h stream).
-  // Every track of chunk ci lies in frames [cut[ci], cut[ci+1]) and the copies
-  // complete in order, so the launch waits on its own chunk's copy event only.
-  MKF_CUDA(cudaEventRecord(c.start, s));
-  MKF_CUDA(cudaStreamWaitEvent(c.h2d, c.start, 0));
-  MKF_CUDA(cudaStreamWaitEvent(c.comp[0], c.start, 0));
-  MKF_CUDA(cudaStreamWaitEvent(c.comp[1], c.start, 0));
-  MKF_CUDA(cudaStreamWaitEvent(c.d2h, c.start, 0));
-  for (int ci = 0; ci < c.n; ++ci) {
-    const size_t g0 = (size_t)c.cut[ci], g1 = (size_t)c.cut[ci + 1];
-    const size_t o0 = (size_t)det_off[g0 * J], o1 = (size_t)det_off[g1 * J];
-    // offsets (g0 J, g1 J] (from 0 for the first chunk): a frame's lists end
-    // at the next frame's first offset, so each chunk also takes its end entry
-    const size_t e0 = ci == 0 ? 0 : g0 * J + 1, e1 = g1 * J + 1;
-    if (e1 > e0)
-      MKF_CUDA(cudaMemcpyAsync(B->h_det_off_dev + e0, det_off + e0, (e1 - e0) * sizeof(int), cudaMemcpyHostToDevice, c.h2d));
-    if (o1 > o0)
-      MKF_CUDA(cudaMemcpyAsync(B->h_det_dev + 2 * o0, det + 2 * o0, (o1 - o0) * 2 * sizeof(float), cudaMemcpyHostToDevice,
-                               c.h2d));
-    MKF_CUDA(cudaEventRecord(c.copied[ci], c.h2d));
-  }
-  for (int ci = 0; ci < c.n; ++ci) {
-    cudaStream_t cs = c.comp[ci & 1];
-    MKF_CUDA(cudaStreamWaitEvent(cs, c.copied[ci], 0));
-    BatchArgs a = batch_args(B, B->h_det_off_dev, B->h_det_dev, B->d_est, B->d_ll, B->d_ess, B->d_status);
-    a.order = c.order + c.ofs[ci];
-    a.n_tracks = c.ofs[ci + 1] - c.ofs[ci];
-    a.counter = c.counters + ci;
-    int st = launch_any(B, a, cs, ci & 1);
-    if (st) return st;
-    MKF_CUDA(cudaEventRecord(c.done[ci], cs));
-    const size_t g0 = (size_t)c.cut[ci], g1 = (size_t)c.cut[ci + 1];
-    MKF_CUDA(cudaStreamWaitEvent(c.d2h, c.done[ci], 0));
-    if (g1 > g0) {
-      MKF_CUDA(cudaMemcpyAsync(est + g0 * d, B->d_est + g0 * d, (g1 - g0) * d * sizeof(float), cudaMemcpyDeviceToHost, c.d2h));
-      MKF_CUDA(cudaMemcpyAsync(loglik + g0, B->d_ll + g0, (g1 - g0) * sizeof(float), cudaMemcpyDeviceToHost, c.d2h));
-      MKF_CUDA(cudaMemcpyAsync(ess + g0, B->d_ess + g0, (g1 - g0) * sizeof(float), cudaMemcpyDeviceToHost, c.d2h));
+  if ((size_t)n_det > r.det_cap || !r.h_det_dev[0]) {
+    for (int k = 0; k < 2; ++k) {
+      if (r.h_det_dev[k]) cudaFree(r.h_det_dev[k]);
+      r.h_det_dev[k] = nullptr;
     }
+    r.det_cap = 0;
+    for (int k = 0; k < 2; ++k)
+      MKF_CUDA(cudaMalloc(&r.h_det_dev[k], std::max<size_t>(1, (size_t)n_det) * 2 * sizeof(float)));
+    r.det_cap = (size_t)n_det;
   }
-  MKF_CUDA(cudaMemcpyAsync(status, B->d_status, B->n_tracks * sizeof(int), cudaMemcpyDeviceToHost, c.d2h));
-  MKF_CUDA(cudaEventRecord(c.out_done, c.d2h));
-  MKF_CUDA(cudaStreamWaitEvent(s, c.out_done, 0));
+  // outputs: written by the kernels straight into the caller's buffers when
+  // those are pinned and mapped, else staged on the device and copied after
+  float* o_est = static_cast<float*>(mapped_device_ptr(est));
+  float* o_ll = static_cast<float*>(mapped_device_ptr(loglik));
+  float* o_ess = static_cast<float*>(mapped_device_ptr(ess));
+  int* o_st = static_cast<int*>(mapped_device_ptr(status));
+  const bool direct = o_est && o_ll && o_ess && o_st;
+  if (!direct) { o_est = B->d_est; o_ll = B->d_ll; o_ess = B->d_ess; o_st = B->d_status; }
+
+  MKF_CUDA(cudaEventRecord(r.start, s));
+  for (cudaStream_t x : {r.copy, r.comp[0], r.comp[1]}) MKF_CUDA(cudaStreamWaitEvent(x, r.start, 0));
+  // head tracks' lists into buffer 0, track by track
+  for (int q = 0; q < r.head; ++q) {
+    const mkf_bpf_track& t = B->tracks[B->order_h[q]];
+    if (t.n_frames <= 0) continue;
+    const size_t e0 = (size_t)t.frame_base * J, e1 = (size_t)(t.frame_base + t.n_frames) * J + 1;
+    MKF_CUDA(cudaMemcpyAsync(r.h_det_off_dev[0] + e0, det_off + e0, (e1 - e0) * sizeof(int), cudaMemcpyHostToDevice, r.copy));
+    const size_t o0 = (size_t)det_off[e0], o1 = (size_t)det_off[e1 - 1];
+    if (o1 > o0)
+      MKF_CUDA(cudaMemcpyAsync(r.h_det_dev[0] + 2 * o0, det + 2 * o0, (o1 - o0) * 2 * sizeof(float),
+                               cudaMemcpyHostToDevice, r.copy));
+  }
+  MKF_CUDA(cudaEventRecord(r.copied[0], r.copy));
+  // everything into buffer 1, for the tail
+  if (r.head < B->n_tracks) {
+    MKF_CUDA(cudaMemcpyAsync(r.h_det_off_dev[1], det_off, (G * J + 1) * sizeof(int), cudaMemcpyHostToDevice, r.copy));
+    MKF_CUDA(cudaMemcpyAsync(r.h_det_dev[1], det, (size_t)n_det * 2 * sizeof(float), cudaMemcpyHostToDevice, r.copy));
+  }
+  MKF_CUDA(cudaEventRecord(r.copied[1], r.copy));
+  for (int k = 0; k < 2; ++k) {
+    const int n = k == 0 ? r.head : B->n_tracks - r.head;
+    cudaStream_t cs = r.comp[k];
+    MKF_CUDA(cudaStreamWaitEvent(cs, r.copied[k], 0));
+    if (n > 0) {
+      BatchArgs a = batch_args(B, r.h_det_off_dev[k], r.h_det_dev[k], o_est, o_ll, o_ess, o_st);
+      a.order = B->order + (k == 0 ? 0 : r.head);
+      a.n_tracks = n;
+      a.counter = r.counters + k;
+      int st = launch_any(B, a, cs, k);
+      if (st) return st;
+    }
+    MKF_CUDA(cudaEventRecord(r.done[k], cs));
+    MKF_CUDA(cudaStreamWaitEvent(s, r.done[k], 0));
+  }
+  if (!direct) {
+    MKF_CUDA(cudaMemcpyAsync(est, B->d_est, G * d * sizeof(float), cudaMemcpyDeviceToHost, s));
+    MKF_CUDA(cudaMemcpyAsync(loglik, B->d_ll, G * sizeof(float), cudaMemcpyDeviceToHost, s));
+    MKF_CUDA(cudaMemcpyAsync(ess, B->d_ess, G * sizeof(float), cudaMemcpyDeviceToHost, s));
+    MKF_CUDA(cudaMemcpyAsync(status, B->d_status, B->n_tracks * sizeof(int), cudaMemcpyDeviceToHost, s));
+  }
   MKF_CUDA(cudaStreamSynchronize(s));
   return MKF_OK;
 }
@@ -1657,9 +1624,9 @@ extern "C" int mkf_bpf_batch_run_host(mkf_bpf_batch_t B, const int* det_off, con
 extern "C" int mkf_bpf_batch_destroy(mkf_bpf_batch_t B) {
   if (!B) return MKF_OK;
   void* ps[] = {B->meta, B->fbase, B->seed, B->obs, B->order, B->counter, B->scratch,
-                B->h_det_off_dev, B->h_det_dev, B->d_est, B->d_ll, B->d_ess, B->d_status};
+                B->d_est, B->d_ll, B->d_ess, B->d_status};
   for (void* p : ps) if (p) cudaFree(p);
-  free_host_chunks(B->hc);
+  free_host_run(B->hr);
   free_models(B->m);
   delete B;
   return MKF_OK;

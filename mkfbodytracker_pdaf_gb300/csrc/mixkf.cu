@@ -594,7 +594,8 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
   const float* a = M.a + k * d;
   const float* mu = M.mu + k * d;
   const float* Lk = M.Lq + k * DD;
-  float sbl = 0.0f;                                         // sigma adjoint, per lane
+  float sbl = 0.0f;                                         // sigma adjoint of this segment (lane 0)
+  double sbd = 0.0;                                         // and its FP64 running sum
   for (int i = lane; i < 2 * d + d * d; i += 32) wb[WL.gmu + i] = 0.0f;   // gmu, ga, Sq
   // stage frame record fr's input state, mixture weights and collapsed mean
   auto stage_frame = [&](const float* fr) {
@@ -761,6 +762,8 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
           gacc[2 * K * d + k * DD + i] += (double)g;
         }
       }
+      sbd += (double)sbl;
+      sbl = 0.0f;
       __syncwarp();
       for (int i = lane; i < 2 * d + d * d; i += 32) wb[WL.gmu + i] = 0.0f;
       __syncthreads();
@@ -788,7 +791,7 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
     __syncthreads();
   }
   // sigma: per-warp lane 0 partials, fixed-order sum
-  if (lane == 0) s.dred[k] = (double)sbl;
+  if (lane == 0) s.dred[k] = sbd;
   __syncthreads();
   if (tid == 0) {
     double v = 0.0;

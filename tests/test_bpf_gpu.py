@@ -196,28 +196,32 @@ def test_batched_host_buffers_match_device_run(cuda):
     assert err < 0.6, err
 
 
-def test_batched_host_run_chunks_in_any_track_order(cuda):
-    """The host-buffer run copies and launches per chunk of frames (tracks
-    grouped by frame range); with the tracks listed out of frame order the
-    outputs still equal the single device-resident launch bit for bit, on
-    repeated calls."""
+def test_batched_host_run_head_and_tail_in_any_track_order(cuda):
+    """The host-buffer run launches the first grid-size tracks of the
+    longest-first order as soon as their own lists are copied, and the rest
+    after the bulk copy; outputs go straight into pinned caller buffers or
+    through device staging for pageable ones.  With more tracks than the head
+    and the tracks listed out of frame order, both forms equal the single
+    device-resident launch bit for bit, on repeated calls."""
     from mkfbodytracker_pdaf_gb300 import synth
     from mkfbodytracker_pdaf_gb300.filters import BatchedBootstrapPF
     torch = cuda
-    base = synth.uneven_tracks_batch(n_tracks=96, t_range=(5, 60), n_range=(64, 2048))
+    base = synth.uneven_tracks_batch(n_tracks=600, t_range=(3, 30), n_range=(64, 1024))
     perm = np.random.default_rng(5).permutation(base.n_tracks)
     batch = synth.BpfBatch(base.model, [base.tracks[b] for b in perm], base.det_off, base.det, base.truth)
     runner = BatchedBootstrapPF(batch)
     est, ll, ess, st = runner.run(*runner.device_inputs())
+    ref = [x.cpu().numpy() for x in (est, ll, ess, st)]
     G = batch.n_frames_total
-    for _ in range(2):
-        outs = (np.full((G, 12), np.nan, np.float32), np.zeros(G, np.float32), np.zeros(G, np.float32),
-                np.zeros(batch.n_tracks, np.int32))
+    for pinned in (False, True, True):
+        outs = [torch.full((G, 12), float("nan")), torch.zeros(G), torch.zeros(G),
+                torch.zeros(batch.n_tracks, dtype=torch.int32)]
+        if pinned:
+            outs = [o.pin_memory() for o in outs]
+        outs = [o.numpy() for o in outs]
         runner.run_host(batch.det_off.astype(np.int32), batch.det.astype(np.float32), outs)
-        np.testing.assert_array_equal(outs[0], est.cpu().numpy())
-        np.testing.assert_array_equal(outs[1], ll.cpu().numpy())
-        np.testing.assert_array_equal(outs[2], ess.cpu().numpy())
-        np.testing.assert_array_equal(outs[3], st.cpu().numpy())
+        for o, r in zip(outs, ref):
+            np.testing.assert_array_equal(o, r)
 
 
 def test_batched_variant_flags_checked(cuda):
