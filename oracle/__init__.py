@@ -6,11 +6,15 @@ association), used by the tests as the parity reference, by ``__graft_entry__.sm
 and by ``bench.py``'s CPU-baseline and reference legs.  The product package
 (``mkfbodytracker_pdaf_gb300``) never imports it.
 
-Parity against the reference's own outputs is UNPINNED: the reference has no
-tests or golden vectors and cannot be built here (ROS and OpenCV are absent).
-Pinned instead: Philox4x32-10 against the published Random123 known-answer
-vectors, the exact resampler against the literal wheel on dyadic weights, and
-the KF/Gaussian pieces against independent closed forms (tests/).
+Pinned to the reference's own code: the reference's KF_model.cpp, my_gmm.cpp
+and pf2DRao.cpp, compiled unmodified against stand-in OpenCV/ROS headers
+(oracle/refpin/Makefile), produced tests/golden/refpin.npz, against which
+tests/test_refpin.py checks the KF predict/update, loadGaussian, the literal
+resampling wheel, the chol/mvnpdf quirk modes and the literal RBPF update
+(including its shared-buffer effect).  Also pinned: Philox4x32-10 against the
+published Random123 known-answer vectors, the exact resampler against the
+literal wheel on dyadic weights, and the KF/Gaussian pieces against closed
+forms.
 """
 from __future__ import annotations
 
@@ -113,6 +117,8 @@ def _declare(L):
     L.mko_measure.argtypes = [C.POINTER(Model), I, P, P, P]
     L.mko_rbpf_update.argtypes = [C.POINTER(Model), I, P, P, P, C.c_uint, U32, U32, P, P, P, P, P]
     L.mko_rbpf_update.restype = I
+    L.mko_rbpf_update_literal.argtypes = [C.POINTER(Model), I, P, P, P, C.c_uint, D, P, D, P, I, P, P, P, P, P]
+    L.mko_rbpf_update_literal.restype = I
     L.mko_rbpf_estimate.argtypes = [I, I, P, P]
     L.mko_pdaf_weights.argtypes = [I, P, P, P, P, I, D, D, D, P]
     L.mko_pick_component.argtypes = [P, I, F]
@@ -292,6 +298,27 @@ class RbpfModel:
         fb = lib().mko_rbpf_update(C.byref(self.s), N, _p(x), _p(Pm), _p(_c(z, np.float64)),
                                    mask, U_ind, U_anc, _p(pa), _p(out["ind"]), _p(out["logw"]),
                                    _p(out["wn"]), _p(out["anc"]))
+        out.update(x=x, P=Pm, fallback=bool(fb))
+        return out
+
+    def update_literal(self, x, Pm, z, u_ind, u_anc, mvn_mode, mask=None, alias_prev_anc=None,
+                       fb_ind=None, fb_anc=None):
+        """The update with the reference's literal pieces (the wheel on double
+        uniforms, the Gaussian in mvn_mode, linear-domain weights):
+        mko_rbpf_update_literal."""
+        x = _c(x, np.float64).copy()
+        Pm = _c(Pm, np.float64).copy()
+        N = x.shape[0]
+        if mask is None:
+            mask = (1 << self.m) - 1
+        out = dict(ind=np.zeros(N, np.int32), logw=np.zeros(N), wn=np.zeros(N),
+                   anc=np.zeros(N, np.int32))
+        pa = _c(alias_prev_anc, np.int32) if alias_prev_anc is not None else None
+        fi = _c(fb_ind, np.int32) if fb_ind is not None else None
+        fa = _c(fb_anc, np.int32) if fb_anc is not None else None
+        fb = lib().mko_rbpf_update_literal(C.byref(self.s), N, _p(x), _p(Pm), _p(_c(z, np.float64)), mask,
+                                           float(u_ind), _p(fi), float(u_anc), _p(fa), int(mvn_mode), _p(pa),
+                                           _p(out["ind"]), _p(out["logw"]), _p(out["wn"]), _p(out["anc"]))
         out.update(x=x, P=Pm, fallback=bool(fb))
         return out
 

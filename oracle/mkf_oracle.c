@@ -1,9 +1,8 @@
 /*
  * mkf_oracle.c -- FP64 CPU restatement of the mkfbodytracker_pdaf filtering
  * hot path.  TEST INFRASTRUCTURE ONLY (the parity reference of the tests and the timed CPU baseline);
- * the CUDA product never links or calls it.  Parity against the reference's
- * own outputs is unpinned (the reference has no tests and cannot be built
- * here); see mkf_oracle.h for what is pinned.
+ * the CUDA product never links or calls it.  mkf_oracle.h says how it is
+ * pinned to the reference's own code.
  *
  * Compiled with -ffp-contract=off so that the integer/FP steps that must be
  * bit-identical with the GPU (quantisation, component pick) are not fused.
@@ -429,9 +428,16 @@ void mko_measure(const mko_model* M, int k, const double* x, double* zhat, doubl
 /* ------------------------------------------------------------------------ */
 /* A8: ParticleFilter::update (pf2DRao.cpp:125-158)                          */
 /* ------------------------------------------------------------------------ */
-int mko_rbpf_update(const mko_model* M, int N, double* x, double* P, const double* z,
-                    unsigned mask, uint32_t U_ind, uint32_t U_anc, const int* alias_prev_anc,
-                    int* ind_out, double* logw_out, double* wn_out, int* anc_out) {
+/* The update of pf2DRao.cpp:125-158.  lit == 0: the exact quantised
+ * resampler on 32-bit uniforms U_ind / U_anc, the exact Gaussian, weights
+ * normalised after a max shift.  lit == 1: the reference's literal wheel
+ * (pf2DRao.cpp:175-210) on the double uniforms u_ind / u_anc (fb_ind / fb_anc:
+ * the indices its all-zero branch draws), the Gaussian in mvn_mode, and the
+ * weights normalised in the linear domain as pf2DRao.cpp:138-148 does. */
+static int rbpf_update_impl(const mko_model* M, int N, double* x, double* P, const double* z, unsigned mask,
+                            int lit, uint32_t U_ind, uint32_t U_anc, double u_ind, const int* fb_ind,
+                            double u_anc, const int* fb_anc, int mvn_mode, const int* alias_prev_anc,
+                            int* ind_out, double* logw_out, double* wn_out, int* anc_out) {
   int d = M->d, m = M->m, K = M->K;
   int* ind = (int*)malloc(sizeof(int) * (size_t)N);
   int* anc = (int*)malloc(sizeof(int) * (size_t)N);
@@ -445,7 +451,8 @@ int mko_rbpf_update(const mko_model* M, int N, double* x, double* P, const doubl
     for (int j = 0; j < N; ++j) last_owner[j] = -1;
   }
   /* Propose indicators: systematic resampling of the mixture weights (128) */
-  mko_resample_f64(M->weight, K, N, U_ind, ind);
+  if (lit) mko_resample_wheel(M->weight, K, N, u_ind, fb_ind, ind);
+  else mko_resample_f64(M->weight, K, N, U_ind, ind);
   for (int j = 0; j < N; ++j) {
     int k = ind[j];
     double* xs = x + (size_t)j * d;
@@ -481,18 +488,30 @@ int mko_rbpf_update(const mko_model* M, int N, double* x, double* P, const doubl
         S[a * mm + b] = s + R[rows[a] * m + rows[b]];
       }
     }
-    lw[j] = mm ? mko_mvn_logpdf(mm, zz, zh, S, 0) : 0.0;
+    lw[j] = mm ? mko_mvn_logpdf(mm, zz, zh, S, lit ? mvn_mode : 0) : 0.0;
     kf_update_generic(d, m, Hx, zhat, R, z + (size_t)j * m, mask, xs, Ps);   /* (140) */
     memcpy(tx + (size_t)j * d, xs, sizeof(double) * (size_t)d);               /* temp.push_back */
     memcpy(tP + (size_t)j * d * d, Ps, sizeof(double) * (size_t)d * d);
   }
-  /* normalise (145-148), max-shifted so that underflow cannot zero every weight */
-  double mx = -INFINITY;
-  for (int j = 0; j < N; ++j) if (lw[j] > mx) mx = lw[j];
-  double sum = 0.0;
-  for (int j = 0; j < N; ++j) { wn[j] = isfinite(mx) ? exp(lw[j] - mx) : 0.0; sum += wn[j]; }
-  for (int j = 0; j < N; ++j) wn[j] = wn[j] / sum;
-  int fb = mko_resample_f64(wn, N, N, U_anc, anc);                          /* (152) */
+  int fb;
+  if (lit) {
+    /* linear-domain weights and their sum (138-139), normalised (145-148) */
+    double sum = 0.0;
+    for (int j = 0; j < N; ++j) { wn[j] = exp(lw[j]); sum += wn[j]; }
+    for (int j = 0; j < N; ++j) wn[j] = wn[j] / sum;
+    double mw = 0.0;
+    for (int j = 0; j < N; ++j) if (wn[j] > mw) mw = wn[j];
+    fb = !(mw > 0.0);
+    mko_resample_wheel(wn, N, N, u_anc, fb_anc, anc);                          /* (152) */
+  } else {
+    /* normalise (145-148), max-shifted so that underflow cannot zero every weight */
+    double mx = -INFINITY;
+    for (int j = 0; j < N; ++j) if (lw[j] > mx) mx = lw[j];
+    double sum = 0.0;
+    for (int j = 0; j < N; ++j) { wn[j] = isfinite(mx) ? exp(lw[j] - mx) : 0.0; sum += wn[j]; }
+    for (int j = 0; j < N; ++j) wn[j] = wn[j] / sum;
+    fb = mko_resample_f64(wn, N, N, U_anc, anc);                              /* (152) */
+  }
   for (int j = 0; j < N; ++j) {                                              /* (153-156) */
     memcpy(x + (size_t)j * d, tx + (size_t)anc[j] * d, sizeof(double) * (size_t)d);
     memcpy(P + (size_t)j * d * d, tP + (size_t)anc[j] * d * d, sizeof(double) * (size_t)d * d);
@@ -503,6 +522,21 @@ int mko_rbpf_update(const mko_model* M, int N, double* x, double* P, const doubl
   if (anc_out) memcpy(anc_out, anc, sizeof(int) * (size_t)N);
   free(ind); free(anc); free(lw); free(wn); free(tx); free(tP); free(last_owner);
   return fb;
+}
+
+int mko_rbpf_update(const mko_model* M, int N, double* x, double* P, const double* z,
+                    unsigned mask, uint32_t U_ind, uint32_t U_anc, const int* alias_prev_anc,
+                    int* ind_out, double* logw_out, double* wn_out, int* anc_out) {
+  return rbpf_update_impl(M, N, x, P, z, mask, 0, U_ind, U_anc, 0.0, NULL, 0.0, NULL, 0, alias_prev_anc,
+                          ind_out, logw_out, wn_out, anc_out);
+}
+
+int mko_rbpf_update_literal(const mko_model* M, int N, double* x, double* P, const double* z, unsigned mask,
+                            double u_ind, const int* fb_ind, double u_anc, const int* fb_anc, int mvn_mode,
+                            const int* alias_prev_anc, int* ind_out, double* logw_out, double* wn_out,
+                            int* anc_out) {
+  return rbpf_update_impl(M, N, x, P, z, mask, 1, 0u, 0u, u_ind, fb_ind, u_anc, fb_anc, mvn_mode,
+                          alias_prev_anc, ind_out, logw_out, wn_out, anc_out);
 }
 
 void mko_rbpf_estimate(int N, int d, const double* x, double* est) {

@@ -6,12 +6,15 @@
  * product never links, loads or calls it.
  *
  * Parity status: the reference (ROS + OpenCV, rosbuild) has no tests, golden
- * vectors or fixtures for this path and cannot be built here (no ROS, no
- * OpenCV), so parity against the reference's own outputs is UNPINNED.  What is
- * pinned: Philox4x32-10 against the published Random123 known-answer vectors,
- * the exact systematic resampler against the reference's literal wheel on
- * dyadic weights (where the wheel's FP arithmetic is exact), and the KF /
- * Gaussian restatements against independent closed forms in the tests.
+ * vectors or fixtures for this path, and its build needs ROS and OpenCV, which
+ * are absent.  Its filter sources (KF_model.cpp, my_gmm.cpp, pf2DRao.cpp) are
+ * compiled unmodified against stand-in OpenCV/ROS headers (oracle/refpin), and
+ * their outputs (tests/golden/refpin.npz) pin the KF predict/update,
+ * loadGaussian, the literal resampling wheel, the chol/mvnpdf quirk modes and
+ * the literal RBPF update with its shared-buffer effect (tests/test_refpin.py).
+ * Also pinned: Philox4x32-10 against the published Random123 known-answer
+ * vectors, the exact systematic resampler against the literal wheel on dyadic
+ * weights, and the KF / Gaussian restatements against closed forms.
  *
  * Every function cites the reference file:line it restates.
  */
@@ -102,6 +105,17 @@ void mko_measure(const mko_model* M, int k, const double* x, double* zhat, doubl
 int mko_rbpf_update(const mko_model* M, int N, double* x, double* P, const double* z,
                     unsigned mask, uint32_t U_ind, uint32_t U_anc, const int* alias_prev_anc,
                     int* ind, double* logw, double* wn, int* anc);
+/* The same update with the reference's literal pieces, for pinning the oracle
+ * against the reference's own update: the resampling wheel (pf2DRao.cpp:175-210)
+ * on double uniforms u_ind / u_anc in [0, 1) (fb_ind / fb_anc: the indices of
+ * its all-zero branch, or NULL), the Gaussian density in mvn_mode
+ * (mko_mvn_logpdf), and weights normalised in the linear domain
+ * (pf2DRao.cpp:138-148).  logw_out gets the log density, wn_out the
+ * normalised weights. */
+int mko_rbpf_update_literal(const mko_model* M, int N, double* x, double* P, const double* z, unsigned mask,
+                            double u_ind, const int* fb_ind, double u_anc, const int* fb_anc, int mvn_mode,
+                            const int* alias_prev_anc, int* ind_out, double* logw_out, double* wn_out,
+                            int* anc_out);
 /* getEstimator (pf2DRao.cpp:23-31): uniform mean of track states. */
 void mko_rbpf_estimate(int N, int d, const double* x, double* est);
 
