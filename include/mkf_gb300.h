@@ -17,8 +17,10 @@
  * Philox4x32-10 keyed by (seed, track) and counted by (frame, item, stream),
  * or an explicit uniform passed by the caller, so CPU and GPU see the same
  * draws.  Layout of one particle-frame's draws: ceil(d/4) Philox blocks at
- * streams 0..; words 2p,2p+1 give Box-Muller pair p (top 24 bits); the
- * component uniform is the low bytes of words 0..2.  Resampling uniform of
+ * streams 0..; words 2p,2p+1 give Box-Muller pair p from their top 23 bits
+ * (u1 = 1 - (w0 >> 9) 2^-23, u2 = (w1 >> 9) 2^-23); the component uniform is
+ * the 24-bit value of the low bytes of words 0..2, shifted right by one, times
+ * 2^-23.  Resampling uniform of
  * frame f: word 0 of block (f, 0xFFFFFFFF, 0x100).  Prior draws use frame
  * 0xFFFFFFFF.
  */
@@ -195,7 +197,12 @@ int mkf_bpf_batch_run(mkf_bpf_batch_t h, const int* d_det_off, const float* d_de
                       float* d_est, float* d_loglik, float* d_ess, int* d_status,
                       mkf_stream_t stream);
 /* host-buffer run: copies detections in, runs, copies outputs out, synchronises.
- * n_det = number of (x,y) pairs in det. */
+ * n_det = number of (x,y) pairs in det.  The tracks run in the same
+ * longest-first order as mkf_bpf_batch_run, in two launches: the first
+ * grid-size tracks start once their own lists are copied, the rest after the
+ * bulk copy.  Output buffers that are pinned and mapped (cudaHostAlloc, or
+ * cudaHostRegister with cudaHostRegisterMapped) are written by the kernels
+ * directly; others are staged on the device and copied after the run. */
 int mkf_bpf_batch_run_host(mkf_bpf_batch_t h, const int* det_off, const float* det, int64_t n_det,
                            float* est, float* loglik, float* ess, int* status,
                            mkf_stream_t stream);

@@ -190,6 +190,14 @@ __device__ __forceinline__ void stage_det(float* dj, int i, float2 z, float k) {
   dj[(i >> 1) * 4 + 2 + (i & 1)] = z.y * k;
 }
 
+// Stage slot i of joint j's list for a frame whose list has n entries (clamped
+// to MKF_MAX_DET): the detection, scaled by k, or for n <= i < n rounded up to
+// a multiple of 4, a +inf padding entry.
+__device__ __forceinline__ void stage_list_slot(float* dj, int i, int n, const float2* det, int lo, float k) {
+  if (i < n) stage_det(dj, i, det[lo + i], k);
+  else if (i < ((n + 3) & ~3)) stage_det(dj, i, make_float2(INFINITY, INFINITY), 1.0f);
+}
+
 // log[(1-P_D) kappa + P_D sum_i N(z_i; pi(x), sigma^2 I)] summed over measured
 // joints; det holds each joint's detections in the stage_det layout
 template <int D, bool VEC = true>
@@ -234,24 +242,21 @@ __device__ __forceinline__ float loglik(const PView& p, const float* x, const in
     if (!(q2 > kZMin)) { ll = __fadd_rn(ll, L.log_kappa); continue; }
     const float iz = __fdividef(1.0f, q2);
     const float u = fmaf(L.fxk * q0, iz, L.cxk), v = fmaf(L.fyk * q1, iz, L.cyk);
-    // four partial sums (detection i into sum i mod 4, the remainder into sum 0)
-    // so the exponentials of a list overlap; sums (0, 1) and (2, 3) are packed pairs
+    // four partial sums (detection i into sum i mod 4) so the exponentials of
+    // a list overlap; sums (0, 1) and (2, 3) are packed pairs.  The list is
+    // padded with +inf detections to a multiple of four (stage_list): their
+    // terms are 2^-inf = +0 exactly, so every group runs the same code.
     float2 accA = make_float2(0.0f, 0.0f), accB = make_float2(0.0f, 0.0f);
     const float* dj = det + j * 2 * MKF_MAX_DET;
     const float2 uu = make_float2(u, u), vv = make_float2(v, v);
-    const int n = cnt[j];
-    int i = 0;
-    for (; i + 4 <= n; i += 4) {
+    const int n = (cnt[j] + 3) & ~3;
+    for (int i = 0; i < n; i += 4) {
       const float4 g0 = ld4(dj + 2 * i), g1 = ld4(dj + 2 * i + 4);
       const float2 dxA = pk_sub(make_float2(g0.x, g0.y), uu), dyA = pk_sub(make_float2(g0.z, g0.w), vv);
       const float2 dxB = pk_sub(make_float2(g1.x, g1.y), uu), dyB = pk_sub(make_float2(g1.z, g1.w), vv);
       const float2 sA = pk_fma(dyA, dyA, pk_mul(dxA, dxA)), sB = pk_fma(dyB, dyB, pk_mul(dxB, dxB));
       accA = pk_add(accA, make_float2(ex2_neg(sA.x), ex2_neg(sA.y)));
       accB = pk_add(accB, make_float2(ex2_neg(sB.x), ex2_neg(sB.y)));
-    }
-    for (; i < n; ++i) {
-      const float dx = dj[(i >> 1) * 4 + (i & 1)] - u, dy = dj[(i >> 1) * 4 + 2 + (i & 1)] - v;
-      accA.x += ex2_neg(fmaf(dy, dy, dx * dx));
     }
     const float acc = (accA.x + accA.y) + (accB.x + accB.y);
     // __fadd_rn: never merged with the multiply inside __logf, so every kernel
@@ -422,11 +427,12 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       for (int q = tid; q < J * MKF_MAX_DET; q += TB) {
         const int j = q / MKF_MAX_DET, i = q - j * MKF_MAX_DET;
         const int lo = A.det_off[g * J + j], n = A.det_off[g * J + j + 1] - lo;
+        const int nc = min(max(n, 0), MKF_MAX_DET);
         if (i == 0) {
           if (n > MKF_MAX_DET) atomicOr(&s_flag, MKF_ST_TRUNC);
-          s_cnt[j] = min(max(n, 0), MKF_MAX_DET);
+          s_cnt[j] = nc;
         }
-        if (i < n) stage_det(s_det + j * 2 * MKF_MAX_DET, i, A.det[lo + i], LK.k);
+        stage_list_slot(s_det + j * 2 * MKF_MAX_DET, i, nc, A.det, lo, LK.k);
       }
       __syncthreads();
 
@@ -783,11 +789,12 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
     for (int q = tid; q < J * MKF_MAX_DET; q += TB) {
       const int j = q / MKF_MAX_DET, i = q - j * MKF_MAX_DET;
       const int lo = A.det_off[j], n = A.det_off[j + 1] - lo;
+      const int nc = min(max(n, 0), MKF_MAX_DET);
       if (i == 0) {
         if (n > MKF_MAX_DET && blockIdx.x == 0) atomicOr(&A.fs->status, MKF_ST_TRUNC);
-        s_cnt[j] = min(max(n, 0), MKF_MAX_DET);
+        s_cnt[j] = nc;
       }
-      if (i < n) stage_det(s_det + j * 2 * MKF_MAX_DET, i, A.det[lo + i], LK.k);
+      stage_list_slot(s_det + j * 2 * MKF_MAX_DET, i, nc, A.det, lo, LK.k);
     }
     __syncthreads();
   }

@@ -108,6 +108,39 @@ struct MixArgs {
 
 __device__ __forceinline__ float wsum(float v) { return warp_sum(v); }
 
+// N warp sums at once (N = 2, 4 or 8), every lane getting all N totals.
+// Recursive halving: at each xor step a lane keeps half of its current values
+// and adds its partner's copy of that half, so the N sums need N - 1 + 5 - log2 N
+// exchanges instead of 5 N; lane (i << (5 - log2 N)) ends with total i, which is
+// then broadcast.  The order of the additions is fixed (deterministic).
+template <int N>
+__device__ __forceinline__ void wsum_multi(float (&v)[N], int lane) {
+  constexpr int LG = N == 2 ? 1 : N == 4 ? 2 : 3;
+  static_assert(N == 2 || N == 4 || N == 8, "wsum_multi: N must be 2, 4 or 8");
+  float c[N];
+#pragma unroll
+  for (int i = 0; i < N; ++i) c[i] = v[i];
+  int n = N;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    if (n > 1) {
+      const int h = n / 2;
+      const bool upper = (lane & o) != 0;
+#pragma unroll
+      for (int i = 0; i < h; ++i) {
+        const float send = upper ? c[i] : c[i + h];
+        const float keep = upper ? c[i + h] : c[i];
+        c[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+      }
+      n = h;
+    } else {
+      c[0] += __shfl_xor_sync(0xffffffffu, c[0], o);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < N; ++i) v[i] = __shfl_sync(0xffffffffu, c[0], i << (5 - LG));
+}
+
 // ---------------------------------------------------------------- forward pieces
 // sequential PDAF/EKF update of one joint for one component (whole warp)
 // R: this warp's scratch record (shared memory, R_H + 8d floats, 16-byte
@@ -244,9 +277,10 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
   const float beta0 = R[R_B0], ell = R[R_ELL];
   const float b = (1.0f - pd) * kappa;
   // x' = x + Kg nb
-  float t0 = 0.0f, t1 = 0.0f;
-  if (lane < d) { t0 = Kg[lane * 2] * xb[lane]; t1 = Kg[lane * 2 + 1] * xb[lane]; }
-  float nbb0 = wsum(t0), nbb1 = wsum(t1);
+  float t2[2] = {0.0f, 0.0f};
+  if (lane < d) { t2[0] = Kg[lane * 2] * xb[lane]; t2[1] = Kg[lane * 2 + 1] * xb[lane]; }
+  wsum_multi<2>(t2, lane);
+  float nbb0 = t2[0], nbb1 = t2[1];
   // P' = P - W Kg^T
   for (int i = lane; i < 2 * d; i += 32) {
     const int r = i >> 1, a = i & 1;
@@ -259,17 +293,25 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
     Kgb[i] = xb[r] * (a ? nb1 : nb0) - t;
   }
   __syncwarp();
-  // W = Kg M
-  float m00 = 0.0f, m01 = 0.0f, m10 = 0.0f, m11 = 0.0f;
+  // W = Kg M: the M adjoint (partials), and the Kg adjoint's W term; the
+  // S^-1 adjoint of Kg = U Si (partials, from the finished Kg adjoint) is
+  // reduced together with the M adjoint
+  float r8[8] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
   if (lane < d) {
-    m00 = Kg[lane * 2] * Wb[lane * 2]; m01 = Kg[lane * 2] * Wb[lane * 2 + 1];
-    m10 = Kg[lane * 2 + 1] * Wb[lane * 2]; m11 = Kg[lane * 2 + 1] * Wb[lane * 2 + 1];
+    r8[0] = Kg[lane * 2] * Wb[lane * 2]; r8[1] = Kg[lane * 2] * Wb[lane * 2 + 1];
+    r8[2] = Kg[lane * 2 + 1] * Wb[lane * 2]; r8[3] = Kg[lane * 2 + 1] * Wb[lane * 2 + 1];
   }
-  const float Mb[4] = {wsum(m00), wsum(m01), wsum(m10), wsum(m11)};
   for (int i = lane; i < 2 * d; i += 32) {
     const int r = i >> 1, a = i & 1;
     Kgb[i] += Wb[r * 2] * Mm[a * 2] + Wb[r * 2 + 1] * Mm[a * 2 + 1];
   }
+  __syncwarp();
+  if (lane < d) {
+    r8[4] = U[lane * 2] * Kgb[lane * 2]; r8[5] = U[lane * 2] * Kgb[lane * 2 + 1];
+    r8[6] = U[lane * 2 + 1] * Kgb[lane * 2]; r8[7] = U[lane * 2 + 1] * Kgb[lane * 2 + 1];
+  }
+  wsum_multi<8>(r8, lane);
+  const float Mb[4] = {r8[0], r8[1], r8[2], r8[3]};
   // M = (1 - beta0) S - Cn
   float Sb[4], Cnb[4];
   float b0b = 0.0f;
@@ -290,12 +332,7 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
     const int r = i >> 1, a = i & 1;
     Ub[i] = Kgb[r * 2] * Si[a * 2] + Kgb[r * 2 + 1] * Si[a * 2 + 1];
   }
-  float s00 = 0.0f, s01 = 0.0f, s10 = 0.0f, s11 = 0.0f;
-  if (lane < d) {
-    s00 = U[lane * 2] * Kgb[lane * 2]; s01 = U[lane * 2] * Kgb[lane * 2 + 1];
-    s10 = U[lane * 2 + 1] * Kgb[lane * 2]; s11 = U[lane * 2 + 1] * Kgb[lane * 2 + 1];
-  }
-  float Sib[4] = {wsum(s00), wsum(s01), wsum(s10), wsum(s11)};
+  float Sib[4] = {r8[4], r8[5], r8[6], r8[7]};
   // nb = sum beta nu
   if (lane < n) {
     betab += n0 * nbb0 + n1 * nbb1;
@@ -314,12 +351,13 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
     nub1 += qb * ((Si[2] + Si[1]) * n0 + 2.0f * Si[3] * n1);
     q00 = qb * n0 * n0; q01 = qb * n0 * n1; q11 = qb * n1 * n1;
   }
-  const float ldb = wsum(ldp);
-  Sib[0] += wsum(q00);
-  const float q01s = wsum(q01);
-  Sib[1] += q01s; Sib[2] += q01s;
-  Sib[3] += wsum(q11);
-  const float zhb0 = -wsum(nub0), zhb1 = -wsum(nub1);
+  float r6[8] = {ldp, q00, q01, q11, nub0, nub1, 0.0f, 0.0f};
+  wsum_multi<8>(r6, lane);
+  const float ldb = r6[0];
+  Sib[0] += r6[1];
+  Sib[1] += r6[2]; Sib[2] += r6[2];
+  Sib[3] += r6[3];
+  const float zhb0 = -r6[4], zhb1 = -r6[5];
   // ld = log det S ; Si = S^-1
   Sb[0] += ldb * Si[0]; Sb[1] += ldb * Si[2]; Sb[2] += ldb * Si[1]; Sb[3] += ldb * Si[3];
   {

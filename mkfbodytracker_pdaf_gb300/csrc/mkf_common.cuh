@@ -102,7 +102,7 @@ MKF_HD int pick_component(const float* cumpi, int K, float u) {
 // The same count from a table over kPickBins equal bins of [0, 1): entry b holds
 // #{c < K-1 : cumpi[c] <= b / kPickBins} in its low 7 bits (K <= 128) and, in
 // bit 7, whether some cumpi[c] falls strictly inside the bin; only then does the
-// count continue past the bin's lower edge.  u is a multiple of 2^-24 in [0, 1),
+// count continue past the bin's lower edge.  u is a multiple of 2^-23 in [0, 1),
 // so u * kPickBins and its floor are exact.  build_pick_table fills entries
 // tid, tid + TB, ... (a block fills it cooperatively).
 constexpr int kPickBins = 1024;
@@ -179,14 +179,18 @@ __device__ __forceinline__ float lg2_approx(float x) {
   return r;
 }
 
+// A float in [1, 2) whose 23 mantissa bits are the word's top 23 bits (no
+// integer-to-float conversion, which runs at a fraction of the FP32 rate).
+__device__ __forceinline__ float unit_bits(uint32_t w) { return __uint_as_float(0x3F800000u | (w >> 9)); }
+
 // Both Box-Muller pairs of one Philox block, (w.x, w.y) -> z[0], z[1] and
 // (w.z, w.w) -> z[2], z[3], with the two pairs' arithmetic in packed f32x2
-// instructions: r = sqrt(-2 ln u1) with -2 ln u1 = lg2(u1) (-2 ln 2), angle
-// pi (2 u2 - 1) as fma(2 pi, u2, -pi) (the same single rounding), z = r (cos, sin).
+// instructions.  Uniforms of 23 bits: u1 = 2 - [1, 2) in (0, 1], u2 = [1, 2) - 1
+// in [0, 1), both exact.  r = sqrt(-2 ln u1) with -2 ln u1 = lg2(u1) (-2 ln 2),
+// angle pi (2 u2 - 1) as fma(2 pi, u2, -pi) (the same single rounding), z = r (cos, sin).
 __device__ __forceinline__ void box_muller2(u32x4 w, float* z) {
-  const float2 s24 = make_float2(1.0f / 16777216.0f, 1.0f / 16777216.0f);
-  const float2 u1 = pk_mul(make_float2((float)((w.x >> 8) + 1u), (float)((w.z >> 8) + 1u)), s24);
-  const float2 u2 = pk_mul(make_float2((float)(w.y >> 8), (float)(w.w >> 8)), s24);
+  const float2 u1 = pk_sub(make_float2(2.0f, 2.0f), make_float2(unit_bits(w.x), unit_bits(w.z)));
+  const float2 u2 = pk_sub(make_float2(unit_bits(w.y), unit_bits(w.w)), make_float2(1.0f, 1.0f));
   const float2 y = pk_mul(make_float2(lg2_approx(u1.x), lg2_approx(u1.y)),
                           make_float2(-1.3862943611198906f, -1.3862943611198906f));
   const float2 r = pk_mul(y, make_float2(rsqrtf(fmaxf(y.x, 1e-30f)), rsqrtf(fmaxf(y.y, 1e-30f))));
@@ -200,7 +204,9 @@ __device__ __forceinline__ void box_muller2(u32x4 w, float* z) {
   z[0] = z01.x; z[1] = z01.y; z[2] = z23.x; z[3] = z23.y;
 }
 
-// All draws of one particle-frame.
+// All draws of one particle-frame: D normals (D / 4 Philox blocks at streams
+// 0, 1, ...) and the component uniform, 23 bits from the low bytes of words
+// 0..2 of block 0 ((24-bit value) >> 1, times 2^-23).
 template <int D>
 __device__ __forceinline__ float particle_draws(uint64_t seed, uint32_t track, uint32_t frame,
                                                 uint32_t item, float* eps) {
@@ -212,7 +218,7 @@ __device__ __forceinline__ float particle_draws(uint64_t seed, uint32_t track, u
     if (b == 0) lowb = (w.x & 0xFFu) | ((w.y & 0xFFu) << 8) | ((w.z & 0xFFu) << 16);
     box_muller2(w, eps + 4 * b);
   }
-  return (float)lowb * (1.0f / 16777216.0f);
+  return unit_bits(lowb << 8) - 1.0f;
 }
 
 // ---------------------------------------------------------------- block helpers

@@ -54,16 +54,18 @@ void mko_draw_block(uint64_t seed, uint32_t track, uint32_t frame, uint32_t item
 float mko_u01_f32(uint32_t w) { return (float)(w >> 8) * (1.0f / 16777216.0f); }
 
 /* Draw layout for one particle-frame: ceil(d/4) Philox blocks at streams
- * 0,1,..; words 2p,2p+1 feed Box-Muller pair p (24-bit uniforms from the top
- * bits); the component uniform is assembled from the low bytes of words 0..2. */
+ * 0,1,..; words 2p,2p+1 feed Box-Muller pair p with 23-bit uniforms from the
+ * top bits, u1 = 1 - (w >> 9) 2^-23 in (0,1] and u2 = (w >> 9) 2^-23 in [0,1);
+ * the component uniform is the 24-bit value of the low bytes of words 0..2,
+ * shifted right by one, times 2^-23. */
 void mko_particle_draws(uint64_t seed, uint32_t track, uint32_t frame, uint32_t item,
                         int d, double* eps, float* ucomp) {
   uint32_t W[32];
   int nblk = (d + 3) / 4;
   for (int b = 0; b < nblk; ++b) mko_draw_block(seed, track, frame, item, (uint32_t)b, W + 4 * b);
   for (int p = 0; p < d / 2; ++p) {
-    double u1 = ((double)(W[2 * p] >> 8) + 1.0) * (1.0 / 16777216.0);
-    double u2 = (double)(W[2 * p + 1] >> 8) * (1.0 / 16777216.0);
+    double u1 = 1.0 - (double)(W[2 * p] >> 9) * (1.0 / 8388608.0);
+    double u2 = (double)(W[2 * p + 1] >> 9) * (1.0 / 8388608.0);
     double r = sqrt(-2.0 * log(u1));
     double th = M_PI * (2.0 * u2 - 1.0);
     eps[2 * p] = r * cos(th);
@@ -71,7 +73,7 @@ void mko_particle_draws(uint64_t seed, uint32_t track, uint32_t frame, uint32_t 
   }
   if (ucomp) {
     uint32_t c = (W[0] & 0xFFu) | ((W[1] & 0xFFu) << 8) | ((W[2] & 0xFFu) << 16);
-    *ucomp = (float)c * (1.0f / 16777216.0f);
+    *ucomp = (float)(c >> 1) * (1.0f / 8388608.0f);
   }
 }
 

@@ -34,9 +34,10 @@ void mko_draw_block(uint64_t seed, uint32_t track, uint32_t frame, uint32_t item
 float mko_u01_f32(uint32_t w);
 /* Box-Muller normals for one particle-frame, d (even, <= 24) normals + 1
  * component uniform.  Layout: ceil(d/4) blocks at streams 0..; words 2p,2p+1
- * feed pair p; the component uniform is the low bytes of words 0..2
- * (libm; the GPU uses its own intrinsics, so parity tests feed GPU-dumped
- * normals to the oracle instead of these). */
+ * feed pair p with 23-bit uniforms u1 = 1 - (w >> 9) 2^-23, u2 = (w >> 9) 2^-23;
+ * the component uniform is the 24-bit value of the low bytes of words 0..2,
+ * shifted right by one, times 2^-23 (libm; the GPU uses its own intrinsics, so
+ * parity tests feed GPU-dumped normals to the oracle instead of these). */
 void mko_particle_draws(uint64_t seed, uint32_t track, uint32_t frame, uint32_t item,
                         int d, double* eps, float* ucomp);
 

@@ -40,7 +40,11 @@ def test_gradient_matches_fp64_adjoint_and_fd(cuda, olib):
         v = rng.standard_normal(th.size)
         v /= np.linalg.norm(v)
         rel.append(abs(v @ grad - v @ gref) / max(abs(v @ gref), 1e-6))
-    assert max(rel) < 1e-3, max(rel)
+    assert max(rel) < 1e-3, max(rel)          # random projections: ill-conditioned where v.grad ~ 0
+    # normwise: the whole FP32 gradient against the FP64 adjoint
+    nw = np.linalg.norm(grad - gref) / np.linalg.norm(gref)
+    print("d12 K6 normwise rel err vs FP64 adjoint: %.3g" % nw)
+    assert nw < 5e-5, nw
     # per-block agreement with FP64 central differences (relative step 1e-6)
     K, d = 6, 12
     blocks = {"mu": slice(0, K * d), "a": slice(K * d, 2 * K * d), "Lq": slice(2 * K * d, th.size - 1),
@@ -54,7 +58,8 @@ def test_gradient_matches_fp64_adjoint_and_fd(cuda, olib):
         Lm, _ = olib.mix_batch(om.with_theta(th - h * v), b)
         fd = (Lp - Lm) / (2 * h)
         assert abs(v @ gref - fd) <= 1e-6 * max(1.0, abs(fd)), (name, v @ gref, fd)
-        assert abs(v @ grad - fd) <= 1e-3 * max(1.0, abs(fd)), (name, v @ grad, fd)
+        print("d12 K6 block %s: rel err vs FD %.3g" % (name, abs(v @ grad - fd) / max(1.0, abs(fd))))
+        assert abs(v @ grad - fd) <= 1e-4 * max(1.0, abs(fd)), (name, v @ grad, fd)
 
 
 def test_gradient_deterministic(cuda, olib):
@@ -138,6 +143,9 @@ def test_body8_k32_forward_and_gradient_match_fp64(cuda, olib):
         rel.append(abs(v @ grad - v @ gref) / max(abs(v @ gref), 1e-6))
     print("body8 K32 max rel err vs FP64 adjoint: %.3g" % max(rel))
     assert max(rel) < 1e-3, max(rel)
+    nw = np.linalg.norm(grad - gref) / np.linalg.norm(gref)
+    print("body8 K32 normwise rel err vs FP64 adjoint: %.3g" % nw)
+    assert nw < 5e-5, nw
     K, d = 32, 24
     blocks = {"mu": slice(0, K * d), "a": slice(K * d, 2 * K * d), "Lq": slice(2 * K * d, th.size - 1),
               "sigma": slice(th.size - 1, th.size)}
@@ -151,7 +159,7 @@ def test_body8_k32_forward_and_gradient_match_fp64(cuda, olib):
         fd = (Lp - Lm) / (2 * h)
         assert abs(v @ gref - fd) <= 1e-6 * max(1.0, abs(fd)), (name, v @ gref, fd)
         print("body8 K32 block %s: rel err vs FD %.3g" % (name, abs(v @ grad - fd) / max(1.0, abs(fd))))
-        assert abs(v @ grad - fd) <= 1e-3 * max(1.0, abs(fd)), (name, v @ grad, fd)
+        assert abs(v @ grad - fd) <= 1e-4 * max(1.0, abs(fd)), (name, v @ grad, fd)
 
 
 def test_fit_recovers_the_model_when_the_likelihood_is_exact(cuda, olib):
