@@ -693,13 +693,24 @@ def run_fit(args):
     matched = {"mu_mae": err(mu_f, tt["mu"][perm]),
                "a_mae": err(a_f, tt["a"][perm]), "Q_mae": err(Qf, Qt[perm]),
                "components_relabelled": int((perm != np.arange(K)).sum())}
+    # per parameter block: the fitted parameters with one block put back to the
+    # truth; logL(fit) - logL(that) is the block's share of the fit's excess
+    DD = d * (d + 1) // 2
+    blocks = {"mu": slice(0, K * d), "a": slice(K * d, 2 * K * d), "Lq": slice(2 * K * d, 2 * K * d + K * DD),
+              "sigma": slice(th_true.size - 1, th_true.size)}
+    per_block = {}
+    for name, sl in blocks.items():
+        hyb = thf.copy()
+        hyb[sl] = th_true[sl]
+        g.set_theta(hyb)
+        per_block[name] = {"n_params": int(sl.stop - sl.start), "logL_fit_minus_with_true_block": Lf - g.forward().item()}
     print(json.dumps({
         "workload": "motion-model fit (%s): K=%d, d=%d from B=%d x T=%d, %d Adam steps (lr %g) on the device"
                     % (args.fit_case, K, d, b.n_tracks, args.fit_frames, args.fit_steps, args.fit_lr),
         "seconds_total": wall, "seconds_per_gradient_eval": wall / args.fit_steps,
         "logL_init": L0, "logL_final": Lf, "logL_true_params": Ltrue, "logL_history": hist,
         "logL_final_minus_true": Lf - Ltrue, "n_params": int(th_true.size),
-        "half_n_params": 0.5 * th_true.size,
+        "half_n_params": 0.5 * th_true.size, "per_block": per_block,
         "recovery": {"mu_mae_init": err(mu_0, tt["mu"]), "mu_mae_final": err(mu_f, tt["mu"]),
                      "a_mae_init": 0.0, "a_mae_final": err(a_f, tt["a"]),
                      "Q_mae_init": err(Q0, Qt), "Q_mae_final": err(Qf, Qt),
