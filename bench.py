@@ -37,9 +37,14 @@ BYTES_PER_PF = 112          # algorithmic bytes per particle-frame (state in/out
 # DRAM bytes per particle-frame of bpf_batched_kernel (autotuned shape: 256
 # threads x 3 CTAs/SM, float4 loads + search with ancestors in global memory):
 # dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture on 2048
-# tracks of the same workload (284.7 GB over 4.148e9 particle-frames), scaled
+# tracks of the same workload (286.7 GB over 4.148e9 particle-frames), scaled
 # to a full launch by particle-frames
-TRAFFIC_BYTES_PER_PF = 68.6
+TRAFFIC_BYTES_PER_PF = 69.1
+# warp instructions issued per particle-frame by the same kernel (smsp__inst_executed.sum
+# of the same capture: 1.2312e11 over 4.148e9 particle-frames); with the SM count, the
+# four schedulers of an SM and the sampled SM clock it gives the issue roofline, the
+# bound this kernel actually meets
+WARP_INST_PER_PF = 29.68
 
 
 def load_peaks():
@@ -369,6 +374,16 @@ def run_gb300(args):
             "clocks": clocks,
             "status_ok": bool(((st & ~8) == 0).all()) and est_ok,
         }
+        sms = torch.cuda.get_device_properties(local).multi_processor_count
+        mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz")
+        if mhz:
+            peak_issue = sms * 4 * mhz * 1e6
+            ach_issue = WARP_INST_PER_PF * PF / (ms / 1000.0)
+            line["roofline"]["issue"] = {
+                "bound": "instruction issue (one warp instruction per scheduler per cycle)",
+                "warp_inst_per_particle_frame": WARP_INST_PER_PF, "achieved": ach_issue, "peak": peak_issue,
+                "unit": "warp-instructions/s", "frac": ach_issue / peak_issue,
+                "peak_from": "%d SMs x 4 schedulers x %.0f MHz (median sampled SM clock)" % (sms, mhz)}
         if not args.no_plain:
             pr = plain_rate(batch, args.plain_tracks, args.plain_frames)
             line["plain_path"] = {"value": pr, "unit": UNIT,
@@ -712,6 +727,9 @@ def run_fit(args):
         "logL_final_minus_true": Lf - Ltrue, "n_params": int(th_true.size),
         "half_n_params": 0.5 * th_true.size, "per_block": per_block,
         "recovery": {"mu_mae_init": err(mu_0, tt["mu"]), "mu_mae_final": err(mu_f, tt["mu"]),
+                     # the drift (1 - a_k) mu_k is what a frame's transition uses
+                     "drift_mae_init": err((1 - tt["a"]) * mu_0, (1 - tt["a"]) * tt["mu"]),
+                     "drift_mae_final": err((1 - a_f) * mu_f, (1 - tt["a"]) * tt["mu"]),
                      "a_mae_init": 0.0, "a_mae_final": err(a_f, tt["a"]),
                      "Q_mae_init": err(Q0, Qt), "Q_mae_final": err(Qf, Qt),
                      "sigma_init": float(th0[-1]), "sigma_final": s_f, "sigma_true": float(tt["sigma"]),
