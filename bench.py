@@ -403,6 +403,9 @@ def run_gb300(args):
                                          "(C-ABI call per frame, and the frame loop as one CUDA graph)"
                                          % args.sweep_frames,
                              "unit": "particle-frames/s", "rows": rows}
+        if not args.no_plain0:
+            # the reference's own CPU-runnable case: the two-arm RBPF + PDAF tracker (FP64)
+            line["plain0"] = plain0_result(args)
         if not args.no_adjoint:
             # the metric's "+adjoint" half: the mixture-KF gradient (B=1024, T=1000)
             a = adjoint_result(args)
@@ -489,6 +492,10 @@ def sweep_rows(sizes, T, steps, warmup):
 
 
 def run_plain0(args):
+    print(json.dumps(plain0_result(args)), flush=True)
+
+
+def plain0_result(args):
     """Two-arm pose tracking: two arms, K=15, d=12, N=1000 particles per arm, T=500, FP64
     Rao-Blackwellised filters + PDAF association through PoseTracker, against
     the CPU restatement of the reference frame loop."""
@@ -539,11 +546,11 @@ def run_plain0(args):
     ok = ~skipped
     rel = float(np.abs(est[:, ok] - est_c[:, ok]).max() / np.abs(est_c[:, ok]).max())
     err = float(np.abs(est_c[:, ok] - sc.truth[:, ok]).mean())
-    print(json.dumps({"workload": "two-arm pose tracking: 2 arms x T=%d, N=%d, K=15, d=12, FP64 RBPF + PDAF" % (T, N),
-                      "gpu_track_frames_per_s": 2 * T / gpu_s, "gpu_s": gpu_s,
-                      "cpu_track_frames_per_s": 2 * T / cpu_s, "cpu_s": cpu_s, "cpu_threads": 1,
-                      "max_rel_est_err_vs_cpu": rel, "mean_abs_latent_err_vs_truth": err,
-                      "frames_skipped": int(skipped.sum())}), flush=True)
+    return {"workload": "two-arm pose tracking: 2 arms x T=%d, N=%d, K=15, d=12, FP64 RBPF + PDAF" % (T, N),
+            "gpu_track_frames_per_s": 2 * T / gpu_s, "gpu_s": gpu_s,
+            "cpu_track_frames_per_s": 2 * T / cpu_s, "cpu_s": cpu_s, "cpu_threads": 1,
+            "max_rel_est_err_vs_cpu": rel, "mean_abs_latent_err_vs_truth": err,
+            "frames_skipped": int(skipped.sum())}
 
 
 def run_adjoint(args):
@@ -661,8 +668,8 @@ def run_fit(args):
     from mkfbodytracker_pdaf_gb300 import build, mixkf, synth
     build.build()
     if args.fit_case == "exact":
-        K, d = 1, 12
-        b = synth.fit_batch_exact(n_tracks=args.fit_tracks, T=args.fit_frames)
+        K, d = args.fit_components, 12
+        b = synth.fit_batch_exact(n_tracks=args.fit_tracks, T=args.fit_frames, K=K)
     else:
         K, d = 32, 24
         b = synth.fit_batch_k32(n_tracks=args.fit_tracks, T=args.fit_frames)
@@ -756,6 +763,7 @@ def parse_args(argv=None):
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true", help="skip the mixture-KF adjoint summary of the default run")
     ap.add_argument("--no-sweep", action="store_true", help="skip the particle-count sweep rows of the default run")
+    ap.add_argument("--no-plain0", action="store_true", help="skip the two-arm pose-tracking case of the default run")
     ap.add_argument("--bench-sweep-sizes", type=int, nargs="*", default=[20, 22],
                     help="log2 particle counts of the default run's sweep rows")
     ap.add_argument("--workload", default="batched", choices=["batched", "sweep", "plain0", "adjoint", "fit"])
@@ -767,6 +775,8 @@ def parse_args(argv=None):
     ap.add_argument("--adj-check-tracks", type=int, default=8)
     ap.add_argument("--fd-dirs", type=int, default=64)
     ap.add_argument("--fit-case", default="config4", choices=["config4", "exact"])
+    ap.add_argument("--fit-components", type=int, default=1,
+                    help="components of the clutter-free control case (1: the filter's likelihood is exact)")
     ap.add_argument("--fit-tracks", type=int, default=None, help="default: 16384 (config4), 128 (exact)")
     ap.add_argument("--fit-frames", type=int, default=None, help="default: 500 (config4), 200 (exact)")
     ap.add_argument("--fit-steps", type=int, default=None, help="default: 200 (config4), 400 (exact)")

@@ -424,11 +424,13 @@ def fit_batch_k32(n_tracks=16384, T=500, seed=MASTER_SEED + 4):
     return make_mix_batch(seed, n_tracks, T, K=32, d=24, lam=5.0, pd=0.9, layout="body8")
 
 
-def fit_batch_exact(n_tracks=128, T=200, seed=MASTER_SEED + 5):
-    """Fitting control case: one component (K=1, d=12, arm layout), no clutter
-    and detection probability 0.999, so that the mixture-KF likelihood is the
-    model's own up to the EKF linearisation of the projection."""
-    return make_mix_batch(seed, n_tracks, T, K=1, d=12, lam=0.0, pd=0.999, layout="arm4")
+def fit_batch_exact(n_tracks=128, T=200, seed=MASTER_SEED + 5, K=1):
+    """Fitting control case: d=12, arm layout, no clutter and detection
+    probability 0.999.  With one component (the default) the mixture-KF
+    likelihood is the model's own up to the EKF linearisation of the
+    projection; with more, the filter's per-frame collapse of the mixture makes
+    it an approximation."""
+    return make_mix_batch(seed, n_tracks, T, K=K, d=12, lam=0.0, pd=0.999, layout="arm4")
 
 
 # ------------------------------------------------- reference-model (LINEAR) scene
