@@ -624,7 +624,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
               T4[g] = rs_walk_threshold(th, wk[g]);
               rs_walk_next(th, st4, wk[g]);
             }
-            search_u64_multi<4>(sQ, N, T4, r4);
+            search_u64_pow2<4>(sQ, N, T4, r4);
 #pragma unroll
             for (int g = 0; g < 4; ++g)
               if (i0 + g * TB < N) sA[i0 + g * TB] = r4[g];
@@ -766,22 +766,62 @@ __device__ void block_merge(float& m, float& s, float& s2, float* v, float* red)
   }
 }
 
+// 16-byte global -> shared copies that complete asynchronously (cp.async, no
+// registers held while in flight), one commit group per particle step
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Dynamic shared memory of bpf_stream_a: the model's parameter block
+// (params_floats: a | mb | L | Bm | mm | cumpi) and a two-slot ring holding
+// each thread's next ancestor state (slot r, plane g at (r D/4 + g) TB + tid).
+template <int D>
+__host__ __device__ constexpr size_t stream_a_smem_floats(int K, int J, bool diag, int TB) {
+  return (size_t)params_floats<D>(K, J, diag) + 2 * (size_t)TB * D;
+}
+
+// the float4 planes of ancestor an's state into ring slot r of this thread
+template <int D>
+__device__ __forceinline__ void gather_state_async(float4* ring, int r, int tid, int TB, const float* xa, int N,
+                                                   int an) {
+  const float4* src = reinterpret_cast<const float4*>(xa);
+#pragma unroll
+  for (int g = 0; g < D / 4; ++g) cp_async16(ring + (size_t)(r * (D / 4) + g) * TB + tid, src + (size_t)g * N + an);
+}
+
 template <int D, bool DIAG>
 __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
+  extern __shared__ __align__(16) float s_dyn[];
   __shared__ __align__(16) float s_det[MKF_MAX_J * 2 * MKF_MAX_DET];
   __shared__ int s_cnt[MKF_MAX_J];
   __shared__ float s_red[32 * (D + 3)];
   __shared__ bool s_last;
-  __shared__ float s_cum[MKF_MAX_K];
   __shared__ uint8_t s_ktab[kPickBins];
   const int tid = threadIdx.x, TB = blockDim.x;
-  const int J = A.pv.J;
+  const int K = A.pv.K, J = A.pv.J;
   const LikConst LK = lik_const(A.pv, A.kappa, A.pd, A.sigma);
-  // this block's copy of the cumulative mixture weights and their pick table
+  // this block's copy of the model (the propagate and likelihood read it per
+  // particle) and its component pick table; the prior's mu and S0c stay global
+  const int Lsz = pad4(DIAG ? K * D : K * D * (D + 1) / 2);
+  float* s_a = s_dyn;
+  float* s_mb = s_a + K * D;
+  float* s_L = s_mb + K * D;
+  float* s_Bm = s_L + Lsz;
+  float* s_mm = s_Bm + J * 3 * D;
+  float* s_cum = s_mm + pad4(J * 3);
+  float4* ring = reinterpret_cast<float4*>(s_dyn + params_floats<D>(K, J, DIAG));
   PView pv = A.pv;
-  for (int q = tid; q < pv.K; q += TB) s_cum[q] = pv.cumpi[q];
+  for (int q = tid; q < K * D; q += TB) { s_a[q] = pv.a[q]; s_mb[q] = pv.mb[q]; }
+  for (int q = tid; q < (DIAG ? K * D : K * D * (D + 1) / 2); q += TB) s_L[q] = DIAG ? pv.Ld[q] : pv.Lq[q];
+  for (int q = tid; q < J * 3 * D; q += TB) s_Bm[q] = pv.Bm[q];
+  for (int q = tid; q < J * 3; q += TB) s_mm[q] = pv.mm[q];
+  for (int q = tid; q < K; q += TB) s_cum[q] = pv.cumpi[q];
   __syncthreads();
-  build_pick_table(s_cum, pv.K, s_ktab, tid, TB);
+  build_pick_table(s_cum, K, s_ktab, tid, TB);
+  pv.a = s_a; pv.mb = s_mb; pv.Lq = s_L; pv.Ld = s_L; pv.Bm = s_Bm; pv.mm = s_mm;
   pv.cumpi = s_cum;
   pv.ktab = s_ktab;
   __syncthreads();
@@ -804,16 +844,37 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
   const int base = blockIdx.x * A.tile_a;
   const int end = min(A.N, base + A.tile_a);
   const uint32_t frame = step_frame(A);
-  for (int i = base + tid; i < end; i += TB) {
-    float x[D], eps[D];
-    if (A.prior) {
+  if (A.prior) {
+    for (int i = base + tid; i < end; i += TB) {
+      float x[D], eps[D];
       float uc = particle_draws<D>(A.seed, A.track, kFramePrior, (uint32_t)i, eps);
       prior_sample<D>(pv, eps, uc, x);
       store_state<D>(A.xb, A.N, i, x);
-      continue;
     }
-    const int an = A.anc[i];
-    load_state<D>(A.xa, A.N, an, x);
+    return;
+  }
+  // software pipeline over this thread's particles i, i + TB, ...: the state
+  // of the next particle's ancestor is copied into the ring while this one is
+  // computed, and the ancestor index after that is loaded a step ahead
+  int an_next = 0;
+  if (base + tid < end) {
+    gather_state_async<D>(ring, 0, tid, TB, A.xa, A.N, A.anc[base + tid]);
+    if (base + tid + TB < end) an_next = A.anc[base + tid + TB];
+  }
+  cp_async_commit();
+  int slot = 0;
+  for (int i = base + tid; i < end; i += TB) {
+    float x[D], eps[D];
+    cp_async_wait_all();
+#pragma unroll
+    for (int g = 0; g < D / 4; ++g) {
+      const float4 q = ring[(size_t)(slot * (D / 4) + g) * TB + tid];
+      x[4 * g] = q.x; x[4 * g + 1] = q.y; x[4 * g + 2] = q.z; x[4 * g + 3] = q.w;
+    }
+    slot ^= 1;
+    if (i + TB < end) gather_state_async<D>(ring, slot, tid, TB, A.xa, A.N, an_next);
+    cp_async_commit();
+    if (i + 2 * TB < end) an_next = A.anc[i + 2 * TB];
     float uc = particle_draws<D>(A.seed, A.track, frame, (uint32_t)i, eps);
     propagate<D, DIAG>(pv, eps, uc, x);
     store_state<D>(A.xb, A.N, i, x);
@@ -835,7 +896,6 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
       for (int r = 0; r < D; ++r) v[r] = fmaf(w, x[r], v[r]);
     }
   }
-  if (A.prior) return;
   block_merge<D>(m, s, s2, v, s_red);
   constexpr int NV = D + 3;
   if (tid == 0) {
@@ -888,9 +948,20 @@ __global__ void __launch_bounds__(256) bpf_stream_b(StreamArgs A) {
   const float M = A.fs->M;
   const int fb = A.fs->fb;
   const int base = blockIdx.x * A.tile_b, end = min(A.N, base + A.tile_b);
-  // integer sums are order-free: coalesced striped reads
+  // integer sums are order-free: coalesced 16-byte reads, four in flight per
+  // thread (base is a multiple of 4: tile_b is a multiple of the block size)
   uint64_t cs = 0;
-  for (int j = base + tid; j < end; j += TB) {
+  const int n4 = (end - base) >> 2;
+  const float4* l4 = reinterpret_cast<const float4*>(A.logw + base);
+#pragma unroll 4
+  for (int q = tid; q < n4; q += TB) {
+    const float4 lw = l4[q];
+    const float w0 = stream_weight(lw.x, M, fb), w1 = stream_weight(lw.y, M, fb);
+    const float w2 = stream_weight(lw.z, M, fb), w3 = stream_weight(lw.w, M, fb);
+    if (A.dbg_w) reinterpret_cast<float4*>(A.dbg_w + base)[q] = make_float4(w0, w1, w2, w3);
+    cs += quantize39(w0) + quantize39(w1) + quantize39(w2) + quantize39(w3);
+  }
+  for (int j = base + 4 * n4 + tid; j < end; j += TB) {
     float w = stream_weight(A.logw[j], M, fb);
     if (A.dbg_w) A.dbg_w[j] = w;
     cs += quantize39(w);
@@ -944,7 +1015,18 @@ __global__ void __launch_bounds__(256) bpf_stream_c(StreamArgs A, int tile_c) {
   }
   // the tile's integer weights, read coalesced, then prefix sums over
   // contiguous chunks of an odd length (distinct banks across a warp)
-  for (int j = tid; j < n; j += TB) sQ[j] = quantize39(stream_weight(A.logw[base + j], M, fb));
+  {
+    const int n4 = n >> 2;
+    const float4* l4 = reinterpret_cast<const float4*>(A.logw + base);
+#pragma unroll 4
+    for (int q = tid; q < n4; q += TB) {
+      const float4 lw = l4[q];
+      ulonglong2* d2 = reinterpret_cast<ulonglong2*>(sQ) + 2 * q;
+      d2[0] = make_ulonglong2(quantize39(stream_weight(lw.x, M, fb)), quantize39(stream_weight(lw.y, M, fb)));
+      d2[1] = make_ulonglong2(quantize39(stream_weight(lw.z, M, fb)), quantize39(stream_weight(lw.w, M, fb)));
+    }
+    for (int j = 4 * n4 + tid; j < n; j += TB) sQ[j] = quantize39(stream_weight(A.logw[base + j], M, fb));
+  }
   __syncthreads();
   int E = (n + TB - 1) / TB;
   if (E > 1 && !(E & 1)) ++E;
@@ -963,15 +1045,25 @@ __global__ void __launch_bounds__(256) bpf_stream_c(StreamArgs A, int tile_c) {
     s_hi = (blockIdx.x == gridDim.x - 1) ? A.N : count_targets_le(Xprev + tot, A.N, U, Qt);
   }
   __syncthreads();
-  // targets of this tile by 64-bit thresholds, four interleaved searches per thread
+  // targets of this tile by 64-bit thresholds walked along each thread's
+  // stride (one division estimate per thread, not per target), four
+  // interleaved searches per thread; targets past hi are formed and dropped
   const RsThresh th = rs_thresh_setup(Qt, A.N, U);
   const int lo = s_lo, hi = s_hi;
+  const RsStep st1 = rs_step_setup(th, (uint32_t)TB), st4 = rs_step_setup(th, 4u * (uint32_t)TB);
+  RsWalk wk[4];
+  wk[0] = rs_walk_init64(th, (uint32_t)(lo + tid));
+#pragma unroll
+  for (int g = 1; g < 4; ++g) { wk[g] = wk[g - 1]; rs_walk_next(th, st1, wk[g]); }
   for (int i0 = lo + tid; i0 < hi; i0 += 4 * TB) {
     uint64_t T4[4];
     int r4[4];
 #pragma unroll
-    for (int g = 0; g < 4; ++g) T4[g] = rs_threshold64(th, (uint32_t)min(i0 + g * TB, hi - 1));
-    search_u64_multi<4>(sQ, n, T4, r4);
+    for (int g = 0; g < 4; ++g) {
+      T4[g] = rs_walk_threshold(th, wk[g]);
+      rs_walk_next(th, st4, wk[g]);
+    }
+    search_u64_pow2<4>(sQ, n, T4, r4);
 #pragma unroll
     for (int g = 0; g < 4; ++g)
       if (i0 + g * TB < hi) A.anc_out[i0 + g * TB] = base + r4[g];
@@ -1061,6 +1153,36 @@ static PView make_view(const DevModels& m, int mi) {
   return p;
 }
 
+template <int D, bool DIAG>
+static size_t stream_a_smem_bytes(const DevModels& m) {
+  return stream_a_smem_floats<D>(m.K, m.J, DIAG, kStreamTB) * sizeof(float);
+}
+static size_t stream_a_smem(const DevModels& m) {
+  if (m.d == 12) return m.diag ? stream_a_smem_bytes<12, true>(m) : stream_a_smem_bytes<12, false>(m);
+  return m.diag ? stream_a_smem_bytes<24, true>(m) : stream_a_smem_bytes<24, false>(m);
+}
+// opt the instance this model launches into its dynamic shared memory size
+// (above the default 48 KB only for d = 24 with a full noise factor)
+static cudaError_t stream_a_attr(const DevModels& m) {
+  const int bytes = (int)stream_a_smem(m);
+  if (m.d == 12)
+    return m.diag ? cudaFuncSetAttribute(bpf_stream_a<12, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
+                  : cudaFuncSetAttribute(bpf_stream_a<12, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  return m.diag ? cudaFuncSetAttribute(bpf_stream_a<24, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
+                : cudaFuncSetAttribute(bpf_stream_a<24, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+static void stream_a(const DevModels& m, const StreamArgs& a, int nb, cudaStream_t s) {
+  const size_t smem = stream_a_smem(m);
+  if (m.d == 12) {
+    if (m.diag) bpf_stream_a<12, true><<<nb, kStreamTB, smem, s>>>(a);
+    else bpf_stream_a<12, false><<<nb, kStreamTB, smem, s>>>(a);
+  } else {
+    if (m.diag) bpf_stream_a<24, true><<<nb, kStreamTB, smem, s>>>(a);
+    else bpf_stream_a<24, false><<<nb, kStreamTB, smem, s>>>(a);
+  }
+}
+
 extern "C" int mkf_bpf_create(const mkf_bpf_models* models, const mkf_bpf_track* track, mkf_bpf_t* out) {
   MKF_ARG(models && track && out, "mkf_bpf_create: null argument");
   MKF_ARG(track->n_particles >= 1 && track->n_particles <= (1 << 22), "mkf_bpf_create: n_particles out of range");
@@ -1099,22 +1221,13 @@ extern "C" int mkf_bpf_create(const mkf_bpf_models* models, const mkf_bpf_track*
   if (e == cudaSuccess) e = cudaMalloc(&h.bsum, (size_t)h.nb_b * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMalloc(&h.fs, sizeof(FrameScalars));
   if (e == cudaSuccess) e = cudaMemset(h.fs, 0, sizeof(FrameScalars));
+  if (e == cudaSuccess) e = stream_a_attr(h.m);
   if (e != cudaSuccess) {
     mkf_bpf_destroy(H);
     return cuda_fail(e, "mkf_bpf_create: allocation", __FILE__, __LINE__);
   }
   *out = H;
   return MKF_OK;
-}
-
-template <int D, bool DIAG>
-static void launch_stream_a(const StreamArgs& a, int nb, cudaStream_t s) {
-  bpf_stream_a<D, DIAG><<<nb, kStreamTB, 0, s>>>(a);
-}
-
-static void stream_a(int d, bool diag, const StreamArgs& a, int nb, cudaStream_t s) {
-  if (d == 12) { if (diag) launch_stream_a<12, true>(a, nb, s); else launch_stream_a<12, false>(a, nb, s); }
-  else { if (diag) launch_stream_a<24, true>(a, nb, s); else launch_stream_a<24, false>(a, nb, s); }
 }
 
 static StreamArgs stream_args(BpfHandle& h) {
@@ -1136,7 +1249,7 @@ extern "C" int mkf_bpf_reset(mkf_bpf_t H, mkf_stream_t stream) {
   StreamArgs a = stream_args(h);
   a.prior = true;
   a.xb = h.xa;
-  stream_a(h.d, h.m.diag, a, h.nb_a, s);
+  stream_a(h.m, a, h.nb_a, s);
   MKF_CHECK_LAUNCH("mkf_bpf_reset: prior kernel");
   // identity ancestry: sequence 0..N-1
   std::vector<int> iota(h.N);
@@ -1161,7 +1274,7 @@ static int enqueue_update(BpfHandle& h, uint32_t frame, const uint32_t* frame_ba
   a.est = d_est; a.out_loglik = d_loglik; a.out_ess = d_ess;
   a.dbg_w = h.debug ? h.w : nullptr;
   a.anc_out = h.anc;
-  stream_a(h.d, h.m.diag, a, h.nb_a, s);
+  stream_a(h.m, a, h.nb_a, s);
   MKF_CHECK_LAUNCH("mkf_bpf_update: propagate/score kernel");
   bpf_stream_b<<<h.nb_b, kStreamTB, 0, s>>>(a);
   MKF_CHECK_LAUNCH("mkf_bpf_update: block-sum kernel");

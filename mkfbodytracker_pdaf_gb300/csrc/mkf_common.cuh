@@ -423,24 +423,40 @@ MKF_HD void rs_walk_next(const RsThresh& t, const RsStep& st, RsWalk& w) {
   w.base += st.dA + st.dq + c;
 }
 
-// The same threshold for any N <= 2^22 (V_i < 2^45): floor(V_i / N) from a
-// float estimate (relative error <= 4 2^-24, so within one of the truth) and
-// exact integer correction.
-MKF_HD uint64_t rs_threshold64(const RsThresh& t, uint32_t i) {
+// floor(V_i / N) and V_i mod N for any N <= 2^22 and i < 2^23 (V_i < 2^45):
+// a float estimate (relative error <= 4 2^-24, so within one of the truth)
+// and exact integer correction.
+MKF_HD void rs_divmod64(const RsThresh& t, uint32_t i, uint32_t& g, uint32_t& hq) {
   const uint64_t V = (uint64_t)i * t.r + t.s;
   // float(V) from two 32-bit conversions (V < 2^45); the 64-bit one runs on the FP64 pipe
   const float vf = fmaf((float)(uint32_t)(V >> 20), 1048576.0f, (float)(uint32_t)(V & 0xFFFFFu));
 #ifdef __CUDA_ARCH__
-  uint32_t g = __float2uint_rz(vf * t.invN);
+  g = __float2uint_rz(vf * t.invN);
 #else
-  uint32_t g = (uint32_t)(vf * t.invN);   // truncation, as __float2uint_rz
+  g = (uint32_t)(vf * t.invN);   // truncation, as __float2uint_rz
 #endif
   long long h = (long long)V - (long long)g * (long long)t.N;
   for (int k = 0; k < 2; ++k)
     if (h < 0) { --g; h += t.N; }
   for (int k = 0; k < 2; ++k)
     if (h >= (long long)t.N) { ++g; h -= t.N; }
-  return (uint64_t)i * t.A + t.C + g + (((h != 0) || (t.low != 0u)) ? 1u : 0u);
+  hq = (uint32_t)h;
+}
+// The threshold T_i for any N <= 2^22.
+MKF_HD uint64_t rs_threshold64(const RsThresh& t, uint32_t i) {
+  uint32_t g, h;
+  rs_divmod64(t, i, g, h);
+  return (uint64_t)i * t.A + t.C + g + (((h | t.low) != 0u) ? 1u : 0u);
+}
+// Start of a strided walk (rs_walk_next) for any N <= 2^22 and i < 2^23; the
+// walk itself stays exact while S r < 2^32 (S <= 1024 for every such N).
+MKF_HD RsWalk rs_walk_init64(const RsThresh& t, uint32_t i) {
+  uint32_t g, h;
+  rs_divmod64(t, i, g, h);
+  RsWalk w;
+  w.h = h;
+  w.base = (uint64_t)i * t.A + t.C + g;
+  return w;
 }
 
 // quantize_f32(w, 1) (the device's 64-bit conversion path) for a weight
@@ -478,6 +494,30 @@ MKF_HD void search_u64_multi(const uint64_t* Q, int n, const uint64_t* T, int* o
   }
   MKF_UNROLL
   for (int g = 0; g < G; ++g) out[g] = base[g] + ((Q[base[g]] < T[g]) ? 1 : 0);
+}
+
+// The same lower bound by power-of-two steps (Shar's form of binary search):
+// with p the largest power of two <= n, one compare at n - p - 1 places the
+// answer in a window of p entries starting at 0 or n - p, and log2(p) steps of
+// h = p/2 .. 1 ("base += h if Q[base + h - 1] < T") finish it, with no final
+// compare.  Every index read is < n.  Needs T[g] <= Q[n-1], else the result is
+// some j < n (which callers discard).
+template <int G>
+MKF_HD void search_u64_pow2(const uint64_t* Q, int n, const uint64_t* T, int* out) {
+#ifdef __CUDA_ARCH__
+  const int p = 1 << (31 - __clz(n));
+#else
+  const int p = 1 << (31 - __builtin_clz((unsigned)n));
+#endif
+  int base[G];
+  MKF_UNROLL
+  for (int g = 0; g < G; ++g) base[g] = (p != n && Q[n - p - 1] < T[g]) ? n - p : 0;
+  for (int h = p >> 1; h; h >>= 1) {
+    MKF_UNROLL
+    for (int g = 0; g < G; ++g) base[g] += (Q[base[g] + h - 1] < T[g]) ? h : 0;
+  }
+  MKF_UNROLL
+  for (int g = 0; g < G; ++g) out[g] = base[g];
 }
 
 }  // namespace mkf

@@ -5,13 +5,15 @@
 //    in 128-bit integers; random N, Qt in [1, 2^62) (at most 2^22 weights of
 //    40 bits each), U and i, plus the extremes of each;
 //  - stride: the division-free walk of those thresholds along a stride of
-//    targets (rs_walk_*) against the same 128-bit T_i, past N - 1 included;
+//    targets (rs_walk_*, started by rs_walk_init for N <= 65536 and by
+//    rs_walk_init64 for N <= 2^22) against the same 128-bit T_i, past N - 1
+//    included;
 //  - quantize: quantize39(w) against floor(w 2^39) in double (exact: a float
 //    times a power of two) for weights w <= 1 (its domain): random, boundary,
 //    subnormal, zero, negative, -inf and NaN; quantize_f32 / quantize_f64 (the
 //    general-exponent forms) against floor(w 2^(40-e)) in long double for
 //    weights up to their max 2^e;
-//  - search: search_u64_multi<4> against std::lower_bound on random
+//  - search: search_u64_multi<4> and search_u64_pow2<4> against std::lower_bound on random
 //    nondecreasing prefix arrays (with runs of equal values) of 1 .. 2^22 entries;
 //  - pick: the particle kernels' component pick through the 1024-bin table
 //    (build_pick_table / pick_component_table) against the direct count, for
@@ -92,6 +94,27 @@ static void stride_walk(std::mt19937_64& rng) {
       mkf::rs_walk_next(th, st, w);
     }
   }
+  // the 64-bit start (rs_walk_init64) for N up to 2^22, with S r < 2^32
+  for (int it = 0; it < 3000; ++it) {
+    const int N = 1 + (int)(rng() % (it % 2 == 0 ? (1 << 22) : 70000));
+    const uint64_t Qt = 1 + (rng() >> (2 + rng() % 60));
+    const uint32_t U = (uint32_t)rng();
+    const uint32_t S = 32u * (1u + (uint32_t)(rng() % 32));       // 32 .. 1024
+    const uint32_t i0 = (uint32_t)(rng() % (uint64_t)(N + S));
+    const mkf::RsThresh th = mkf::rs_thresh_setup(Qt, N, U);
+    const mkf::RsStep st = mkf::rs_step_setup(th, S);
+    mkf::RsWalk w = mkf::rs_walk_init64(th, i0);
+    int steps = 0;
+    for (uint32_t i = i0; i < (uint32_t)N + 4 * S && steps < 64; i += S, ++steps) {
+      const unsigned __int128 num = ((((unsigned __int128)i) << 32) + U) * (unsigned __int128)Qt;
+      const unsigned __int128 den = ((unsigned __int128)(uint64_t)N) << 32;
+      const unsigned __int128 ref = (num + den - 1) / den;
+      bad += mkf::rs_walk_threshold(th, w) != (uint64_t)ref;
+      bad += i < (uint32_t)N && mkf::rs_threshold64(th, i) != (uint64_t)ref;
+      n += 2;
+      mkf::rs_walk_next(th, st, w);
+    }
+  }
   std::printf("stride %lld %lld\n", bad, n);
 }
 
@@ -151,10 +174,13 @@ static void search(std::mt19937_64& rng) {
         if (T[g] > Q[len - 1]) T[g] = Q[len - 1];
       }
       mkf::search_u64_multi<4>(Q.data(), len, T, out);
+      int out2[4];
+      mkf::search_u64_pow2<4>(Q.data(), len, T, out2);
       for (int g = 0; g < 4; ++g) {
         const int ref = (int)(std::lower_bound(Q.begin(), Q.end(), T[g]) - Q.begin());
         bad += out[g] != ref;
-        ++n;
+        bad += out2[g] != ref;
+        n += 2;
       }
     }
   }
