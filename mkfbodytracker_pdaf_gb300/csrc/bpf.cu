@@ -11,7 +11,10 @@
 //    runs all its frames with the weights, scan and ancestors in shared
 //    memory (particle states in a per-CTA global slot, L2-resident);
 //  * streaming: one track with up to 2^22 particles, three grid-wide kernels
-//    per frame (propagate+score+partials, quantised block sums, search).
+//    per frame: propagate+score+estimate partials (one wave of resident
+//    blocks over contiguous tiles, the model in shared memory, the next
+//    ancestor state prefetched with cp.async), quantised tile sums, and the
+//    per-tile prefix plus threshold search (tiles in whole waves).
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -668,10 +671,8 @@ static size_t batched_smem_bytes(int D, int Nmax, int K, int J, bool diag, bool 
 struct FrameScalars {
   float M;
   int fb;
-  unsigned long long Qt;
-  unsigned int ticket_a, ticket_b;
+  unsigned int ticket_a;
   int status;
-  int pad;
 };
 
 struct StreamArgs {
@@ -943,7 +944,6 @@ __device__ __forceinline__ float stream_weight(float ll, float M, int fb) {
 // block sums of quantised weights; the last block scans them (exclusive)
 __global__ void __launch_bounds__(256) bpf_stream_b(StreamArgs A) {
   __shared__ uint64_t s_red64[34];
-  __shared__ bool s_last;
   const int tid = threadIdx.x, TB = blockDim.x;
   const float M = A.fs->M;
   const int fb = A.fs->fb;
@@ -968,50 +968,59 @@ __global__ void __launch_bounds__(256) bpf_stream_b(StreamArgs A) {
   }
   uint64_t tot;
   block_excl_scan_u64(cs, s_red64, &tot);
-  if (tid == 0) {
-    A.bsum[blockIdx.x] = tot;
-    __threadfence();
-    unsigned t = atomicAdd(&A.fs->ticket_b, 1u);
-    s_last = (t == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (!s_last) return;
-  __threadfence();
-  // exclusive scan over all block sums (chunk per thread), in place
-  const int nb = gridDim.x;
-  const int E2 = (nb + TB - 1) / TB;
-  const int q0 = min(nb, tid * E2), q1 = min(nb, q0 + E2);
-  uint64_t c2 = 0;
-  for (int q = q0; q < q1; ++q) c2 += ((volatile unsigned long long*)A.bsum)[q];
-  uint64_t Qt;
-  uint64_t pre = block_excl_scan_u64(c2, s_red64, &Qt);
-  __syncthreads();
-  for (int q = q0; q < q1; ++q) {
-    uint64_t v = ((volatile unsigned long long*)A.bsum)[q];
-    A.bsum[q] = pre;
-    pre += v;
-  }
-  if (tid == 0) {
-    A.fs->Qt = Qt;
-    A.fs->ticket_b = 0u;
-    if (Qt == 0ull && !fb) { A.fs->fb = 1; A.fs->status |= MKF_ST_FALLBACK; }
-  }
+  if (tid == 0) A.bsum[blockIdx.x] = tot;
 }
 
-__global__ void __launch_bounds__(256) bpf_stream_c(StreamArgs A, int tile_c) {
+// Number of targets i in [0, N) with T_i <= X, by one warp: a float estimate
+// of N X / Qt (within a few of the count) settled by exact 64-bit thresholds
+// at 32 candidates around it (T_i is nondecreasing, so the candidates at or
+// below X are the lanes under the count); the 128-bit count when the estimate
+// misses by 16 or more.
+__device__ __forceinline__ int count_targets_le_warp(const RsThresh& th, uint64_t X, int N, uint32_t U, uint64_t Qt,
+                                                     int lane) {
+  const float xf = fmaf((float)(uint32_t)(X >> 32), 4294967296.0f, (float)(uint32_t)X);
+  const float qf = fmaf((float)(uint32_t)(Qt >> 32), 4294967296.0f, (float)(uint32_t)Qt);
+  const int est = (int)fminf(fmaxf(xf / qf * (float)N, 0.0f), (float)N);
+  const int i = est - 16 + lane;
+  const bool le = (i < 0) || (i < N && rs_threshold64(th, (uint32_t)i) <= X);
+  const int c = __popc(__ballot_sync(0xffffffffu, le));
+  if (c > 0 && c < 32) return est - 16 + c;
+  return count_targets_le(X, N, U, Qt);
+}
+
+__global__ void __launch_bounds__(256, 5) bpf_stream_c(StreamArgs A, int tile_c) {
   extern __shared__ __align__(16) unsigned char smem_c[];
   uint64_t* sQ = reinterpret_cast<uint64_t*>(smem_c);
   __shared__ uint64_t s_red64[34];
   __shared__ int s_lo, s_hi;
+  __shared__ RsThresh s_th;
+  __shared__ RsStep s_st[2];
   const int tid = threadIdx.x, TB = blockDim.x;
   const float M = A.fs->M;
-  const int fb = A.fs->fb;
-  const uint64_t Qt = A.fs->Qt;
+  // the total Qt and this tile's exclusive prefix, from the tile sums of
+  // bpf_stream_b (every block forms them: a few thousand L2-resident words)
+  uint64_t all = 0, before = 0;
+  for (int q = tid; q < (int)gridDim.x; q += TB) {
+    const uint64_t v = A.bsum[q];
+    all += v;
+    before += (q < (int)blockIdx.x) ? v : 0ull;
+  }
+  uint64_t Qt, Xprev;
+  block_excl_scan_u64(all, s_red64, &Qt);
+  block_excl_scan_u64(before, s_red64, &Xprev);
+  const int fb = A.fs->fb || Qt == 0ull;
+  if (blockIdx.x == 0 && tid == 0 && Qt == 0ull && !A.fs->fb) atomicOr(&A.fs->status, MKF_ST_FALLBACK);
   const int base = blockIdx.x * tile_c, end = min(A.N, base + tile_c), n = end - base;
   const uint32_t U = step_uniform(A);
   if (fb) {
     for (int i = base + tid; i < end; i += TB) A.anc_out[i] = resample_fallback_index(U, i, A.N);
     return;
+  }
+  // the resampling rule's constants (64-bit divisions), once per block
+  if (tid < 32) {
+    const RsThresh th = rs_thresh_setup(Qt, A.N, U);
+    const RsStep st1 = rs_step_setup(th, (uint32_t)TB), st4 = rs_step_setup(th, 4u * (uint32_t)TB);
+    if (tid == 0) { s_th = th; s_st[0] = st1; s_st[1] = st4; }
   }
   // the tile's integer weights, read coalesced, then prefix sums over
   // contiguous chunks of an odd length (distinct banks across a warp)
@@ -1034,23 +1043,30 @@ __global__ void __launch_bounds__(256) bpf_stream_c(StreamArgs A, int tile_c) {
   uint64_t cs = 0;
   for (int j = j0; j < j1; ++j) cs += sQ[j];
   uint64_t tot;
-  uint64_t pre = block_excl_scan_u64(cs, s_red64, &tot) + A.bsum[blockIdx.x];
+  uint64_t pre = block_excl_scan_u64(cs, s_red64, &tot) + Xprev;
   for (int j = j0; j < j1; ++j) {
     pre += sQ[j];
     sQ[j] = pre;
   }
-  if (tid == 0) {
-    uint64_t Xprev = A.bsum[blockIdx.x];
-    s_lo = (blockIdx.x == 0) ? 0 : count_targets_le(Xprev, A.N, U, Qt);
-    s_hi = (blockIdx.x == gridDim.x - 1) ? A.N : count_targets_le(Xprev + tot, A.N, U, Qt);
+  // the tile's target range [lo, hi): warp 0 and warp 1 count the targets at
+  // or below each end of the tile's prefix range
+  {
+    const int w = tid >> 5;
+    if (w < 2) {
+      const RsThresh th = s_th;
+      const bool first = (w == 0) ? (blockIdx.x == 0) : (blockIdx.x == gridDim.x - 1);
+      const int c = first ? (w == 0 ? 0 : A.N)
+                          : count_targets_le_warp(th, w == 0 ? Xprev : Xprev + tot, A.N, U, Qt, tid & 31);
+      if ((tid & 31) == 0) (w == 0 ? s_lo : s_hi) = c;
+    }
   }
   __syncthreads();
   // targets of this tile by 64-bit thresholds walked along each thread's
   // stride (one division estimate per thread, not per target), four
   // interleaved searches per thread; targets past hi are formed and dropped
-  const RsThresh th = rs_thresh_setup(Qt, A.N, U);
+  const RsThresh th = s_th;
   const int lo = s_lo, hi = s_hi;
-  const RsStep st1 = rs_step_setup(th, (uint32_t)TB), st4 = rs_step_setup(th, 4u * (uint32_t)TB);
+  const RsStep st1 = s_st[0], st4 = s_st[1];
   RsWalk wk[4];
   wk[0] = rs_walk_init64(th, (uint32_t)(lo + tid));
 #pragma unroll
@@ -1085,7 +1101,6 @@ struct BpfHandle {
 };
 
 constexpr int kStreamTB = 256;
-constexpr int kTileA = 2048;
 constexpr int kTileB = 4096;
 
 }  // namespace mkf
@@ -1162,14 +1177,19 @@ static size_t stream_a_smem(const DevModels& m) {
   return m.diag ? stream_a_smem_bytes<24, true>(m) : stream_a_smem_bytes<24, false>(m);
 }
 // opt the instance this model launches into its dynamic shared memory size
-// (above the default 48 KB only for d = 24 with a full noise factor)
-static cudaError_t stream_a_attr(const DevModels& m) {
+// (above the default 48 KB only for d = 24 with a full noise factor) and
+// report its resident blocks per SM
+template <typename Kern>
+static cudaError_t kernel_smem_occ(Kern kern, int bytes, int* occ) {
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, kStreamTB, bytes);
+  return e;
+}
+static cudaError_t stream_a_attr(const DevModels& m, int* occ) {
   const int bytes = (int)stream_a_smem(m);
   if (m.d == 12)
-    return m.diag ? cudaFuncSetAttribute(bpf_stream_a<12, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
-                  : cudaFuncSetAttribute(bpf_stream_a<12, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  return m.diag ? cudaFuncSetAttribute(bpf_stream_a<24, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes)
-                : cudaFuncSetAttribute(bpf_stream_a<24, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    return m.diag ? kernel_smem_occ(bpf_stream_a<12, true>, bytes, occ) : kernel_smem_occ(bpf_stream_a<12, false>, bytes, occ);
+  return m.diag ? kernel_smem_occ(bpf_stream_a<24, true>, bytes, occ) : kernel_smem_occ(bpf_stream_a<24, false>, bytes, occ);
 }
 
 static void stream_a(const DevModels& m, const StreamArgs& a, int nb, cudaStream_t s) {
@@ -1198,20 +1218,29 @@ extern "C" int mkf_bpf_create(const mkf_bpf_models* models, const mkf_bpf_track*
   h.tr = *track;
   h.N = track->n_particles;
   h.d = models->d;
-  // tiles: at most kTileA / kTileB particles per block, fewer when N is small so
-  // that a frame spreads over about 4 (propagate) / 2 (sums, search) blocks per SM
+  // tiles.  Propagate/score: one wave of resident blocks, each over one
+  // contiguous tile (its fixed cost -- model staging, pick table, the block's
+  // estimate merge -- is paid once per block, and no partial last wave).  Sums
+  // and search: tiles of at most kTileB particles in a whole number of waves of
+  // the search kernel's resident blocks.
   const int sms = num_sms();
-  auto tile_for = [&](int cap, int per_sm) {
-    int t = (h.N + per_sm * sms - 1) / (per_sm * sms);
-    t = (t + kStreamTB - 1) / kStreamTB * kStreamTB;
-    return std::min(cap, std::max(kStreamTB, t));
-  };
-  h.tile_a = tile_for(kTileA, 4);
-  h.tile_b = tile_for(kTileB, 2);
+  int occ_a = 0, occ_c = 0;
+  cudaError_t e = stream_a_attr(h.m, &occ_a);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_c, bpf_stream_c, kStreamTB, kTileB * sizeof(uint64_t));
+  if (e != cudaSuccess) {
+    free_models(h.m);
+    delete H;
+    return cuda_fail(e, "mkf_bpf_create: kernel attributes", __FILE__, __LINE__);
+  }
+  auto round_tb = [](long long t) { return (int)std::max<long long>(kStreamTB, (t + kStreamTB - 1) / kStreamTB * kStreamTB); };
+  const long long wave_a = (long long)sms * std::max(1, occ_a), wave_c = (long long)sms * std::max(1, occ_c);
+  h.tile_a = round_tb((h.N + wave_a - 1) / wave_a);
+  const long long waves_c = std::max(1LL, (h.N + wave_c * kTileB - 1) / (wave_c * kTileB));
+  h.tile_b = std::min(kTileB, round_tb((h.N + waves_c * wave_c - 1) / (waves_c * wave_c)));
   h.nb_a = (h.N + h.tile_a - 1) / h.tile_a;
   h.nb_b = (h.N + h.tile_b - 1) / h.tile_b;
   const size_t N = h.N, d = h.d;
-  cudaError_t e = cudaSuccess;
   if (e == cudaSuccess) e = cudaMalloc(&h.xa, N * d * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&h.xb, N * d * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&h.logw, N * sizeof(float));
@@ -1221,7 +1250,6 @@ extern "C" int mkf_bpf_create(const mkf_bpf_models* models, const mkf_bpf_track*
   if (e == cudaSuccess) e = cudaMalloc(&h.bsum, (size_t)h.nb_b * sizeof(unsigned long long));
   if (e == cudaSuccess) e = cudaMalloc(&h.fs, sizeof(FrameScalars));
   if (e == cudaSuccess) e = cudaMemset(h.fs, 0, sizeof(FrameScalars));
-  if (e == cudaSuccess) e = stream_a_attr(h.m);
   if (e != cudaSuccess) {
     mkf_bpf_destroy(H);
     return cuda_fail(e, "mkf_bpf_create: allocation", __FILE__, __LINE__);
