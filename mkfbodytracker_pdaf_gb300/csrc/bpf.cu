@@ -185,6 +185,23 @@ __device__ __forceinline__ float ex2_neg(float s) {   // 2^(-s), MUFU.EX2
   return r;
 }
 
+// global -> shared copies that complete asynchronously (cp.async: no registers
+// held while in flight); the issuing thread waits for its own groups
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 // Shared-memory detection layout of one joint (2 MKF_MAX_DET floats): pairs of
 // detections as (x_i, x_i+1, y_i, y_i+1), scaled by L.k, so that one 16-byte
 // load gives two detections' x and y as packed pairs.
@@ -345,7 +362,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
   // scatter: sW (log-weights then weights) | sA (ancestors)
   uint64_t* sQ = reinterpret_cast<uint64_t*>(smem);
   float* sW = reinterpret_cast<float*>(smem);
-  int* sA = LOW ? A.anc + (size_t)blockIdx.x * Nmax : reinterpret_cast<int*>(smem + (SEARCH ? 8 : 4) * (size_t)Nmax);
+  int* const sA_slot = LOW ? A.anc + (size_t)blockIdx.x * Nmax : reinterpret_cast<int*>(smem + (SEARCH ? 8 : 4) * (size_t)Nmax);
   float* sP = reinterpret_cast<float*>(smem + (LOW ? 8 : SEARCH ? 12 : 8) * (size_t)Nmax);   // Nmax % 32 == 0
   const int K = A.K, J = A.J;
   const int Lsz = pad4(DIAG ? K * D : K * D * (D + 1) / 2);
@@ -363,6 +380,13 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
   uint8_t* s_ktab = reinterpret_cast<uint8_t*>(s_red64 + 34);
   __shared__ int s_item;
   __shared__ int s_flag;
+  __shared__ PhiloxPre s_pre[D / 4];   // this frame's item-independent Philox words per stream
+  __shared__ PhiloxKeys s_keys;        // this track's round keys
+  // the next frame's list offsets and raw detections, copied with cp.async
+  // while this frame runs (thread q < J MKF_MAX_DET owns slot q)
+  __shared__ int s_offn[MKF_MAX_J + 1];
+  __shared__ int s_nn[MKF_MAX_J];   // the next frame's list lengths
+  __shared__ __align__(8) float2 s_raw[MKF_MAX_J * MKF_MAX_DET];
 
   float* xa0 = A.scratch + (size_t)blockIdx.x * 2 * D * Nmax;
   float* xb0 = xa0 + (size_t)D * Nmax;
@@ -392,7 +416,8 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       for (int i = tid; i < K; i += TB) s_cum[i] = gc[i];
       for (int i = tid; i < J * 3 * D; i += TB) s_Bm[i] = gB[i];
       for (int i = tid; i < J * 3; i += TB) s_mm[i] = gm[i];
-      if (tid == 0) s_flag = 0;
+      if (tid == 0) { s_flag = 0; s_keys = philox_keys(seed, trk); }
+      if (tid < D / 4) s_pre[tid] = philox_pre(seed, trk, kFramePrior, (uint32_t)tid);
       __syncthreads();
       build_pick_table(s_cum, K, s_ktab, tid, TB);
     }
@@ -405,13 +430,16 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
     pv.K = K; pv.J = J; pv.fx = A.m.fx; pv.fy = A.m.fy; pv.cx = A.m.cx; pv.cy = A.m.cy;
     const bool dbg = (A.dbg_w != nullptr) && (b == A.dbg_track);
     const LikConst LK = lik_const(pv, ob.x, ob.y, ob.z);
+    // LOW: the ancestors of a track with 3 N <= 2 Nmax fit in shared memory
+    // behind its N prefix entries, else they use the CTA's global slot
+    int* const sA = (LOW && 3 * N <= 2 * Nmax) ? reinterpret_cast<int*>(sQ + N) : sA_slot;
 
     float* xa = xa0;
     float* xb = xb0;
     // prior draw (frame index 0xFFFFFFFF), identity ancestry
     for (int i = tid; i < N; i += TB) {
       float eps[D], x[D];
-      float uc = particle_draws<D>(seed, trk, kFramePrior, (uint32_t)i, eps);
+      float uc = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i, eps);
       prior_sample<D>(pv, eps, uc, x);
       store_state<D>(xa, Nmax, i, x);
       sA[i] = i;
@@ -423,20 +451,39 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
     int E = (N + TB - 1) / TB;
     if (E > 1 && !(E & 1)) ++E;
     const int j0 = min(N, tid * E), j1 = min(N, j0 + E);
+    // staging slot q = tid of a thread with tid < J MKF_MAX_DET (<= 64 <= TB,
+    // so one slot at most): list q / MKF_MAX_DET, entry q % MKF_MAX_DET
     for (int t = 0; t < T; ++t) {
       const long long g = g0 + t;
-      // this frame's detection lists (each staging thread reads its list's
-      // bounds itself, so one barrier suffices)
-      for (int q = tid; q < J * MKF_MAX_DET; q += TB) {
-        const int j = q / MKF_MAX_DET, i = q - j * MKF_MAX_DET;
-        const int lo = A.det_off[g * J + j], n = A.det_off[g * J + j + 1] - lo;
-        const int nc = min(max(n, 0), MKF_MAX_DET);
-        if (i == 0) {
-          if (n > MKF_MAX_DET) atomicOr(&s_flag, MKF_ST_TRUNC);
-          s_cnt[j] = nc;
+      // this frame's detection lists: read directly for the first frame (each
+      // staging thread reads its list's bounds itself, so one barrier
+      // suffices), else from the copies made during the previous frame
+      if (tid < J * MKF_MAX_DET) {
+        const int qj = tid / MKF_MAX_DET, qi = tid % MKF_MAX_DET;
+        int n, nc;
+        float2 z = make_float2(0.0f, 0.0f);
+        if (t == 0) {
+          const int lo = A.det_off[g * J + qj];
+          n = A.det_off[g * J + qj + 1] - lo;
+          nc = min(max(n, 0), MKF_MAX_DET);
+          if (qi < nc) z = A.det[lo + qi];
+        } else {
+          n = s_nn[qj];
+          nc = min(max(n, 0), MKF_MAX_DET);
+          if (qi < nc) z = s_raw[tid];
         }
-        stage_list_slot(s_det + j * 2 * MKF_MAX_DET, i, nc, A.det, lo, LK.k);
+        if (qi == 0) {
+          if (n > MKF_MAX_DET) atomicOr(&s_flag, MKF_ST_TRUNC);
+          s_cnt[qj] = nc;
+        }
+        float* dj = s_det + qj * 2 * MKF_MAX_DET;
+        if (qi < nc) stage_det(dj, qi, z, LK.k);
+        else if (qi < pad4(nc)) stage_det(dj, qi, make_float2(INFINITY, INFINITY), 1.0f);
       }
+      // the next frame's offsets, copied while this frame runs
+      if (t + 1 < T && tid <= J) cp_async4(&s_offn[tid], A.det_off + (g + 1) * J + tid);
+      cp_async_commit();
+      if (tid < D / 4) s_pre[tid] = philox_pre(seed, trk, (uint32_t)t, (uint32_t)tid);
       __syncthreads();
 
       // ---- propagate from the resampled set and score.  Besides the
@@ -462,8 +509,8 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
           float x[D], eps[D], y[D], eps2[D];
           load_state<D>(xa, Nmax, an, x);
           load_state<D>(xa, Nmax, an2, y);
-          const float uc = particle_draws<D>(seed, trk, (uint32_t)t, (uint32_t)i, eps);
-          const float uc2 = particle_draws<D>(seed, trk, (uint32_t)t, (uint32_t)i2, eps2);
+          const float uc = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i, eps);
+          const float uc2 = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i2, eps2);
           propagate<D, DIAG, VEC>(pv, eps, uc, x);
           propagate<D, DIAG, VEC>(pv, eps2, uc2, y);
           store_state<D>(xb, Nmax, i, x);
@@ -482,7 +529,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
           const int an = sA[i];
           float x[D], eps[D];
           load_state<D>(xa, Nmax, an, x);
-          float uc = particle_draws<D>(seed, trk, (uint32_t)t, (uint32_t)i, eps);
+          float uc = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i, eps);
           propagate<D, DIAG, VEC>(pv, eps, uc, x);
           store_state<D>(xb, Nmax, i, x);
           float ll = loglik<D, VEC>(pv, x, s_cnt, s_det, LK);
@@ -498,7 +545,16 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
           for (int r = 0; r < D / 2; ++r) fv[r] = pk_fma(ww, make_float2(x[2 * r], x[2 * r + 1]), fv[r]);
         }
       }
+      if (tid <= J) cp_async_wait_all();   // s_offn, visible after block_max's barriers
       const float M = block_max(lmax, s_red);
+      // the next frame's detections, copied while this frame resamples
+      if (tid < J * MKF_MAX_DET && t + 1 < T) {
+        const int qj = tid / MKF_MAX_DET, qi = tid % MKF_MAX_DET;
+        const int lo = s_offn[qj], n = s_offn[qj + 1] - lo;
+        if (qi == 0) s_nn[qj] = n;
+        if (qi < min(max(n, 0), MKF_MAX_DET)) cp_async8(&s_raw[tid], A.det + lo + qi);
+      }
+      cp_async_commit();
       const bool fb = !(M > -INFINITY) || !(M < INFINITY);
       const bool fused = !PAIR && (M - Lub >= -60.0f);
 
@@ -556,13 +612,18 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       uint64_t P = 0, Qt = 0;
       {
         const int lane = tid & 31, w = tid >> 5, nw = (TB + 31) >> 5;
+        // the warp's sums of acc (column 2, the max weight, is a max and only
+        // the scatter variant uses it): lane c << SH ends with column c's sum
+        constexpr int NP = NV <= 16 ? 16 : 32, SH = NV <= 16 ? 1 : 0;
+        float r[NP];
 #pragma unroll
-        for (int c = 0; c < NV; ++c) acc[c] = (c == 2) ? warp_max(acc[c]) : warp_sum(acc[c]);
+        for (int c = 0; c < NP; ++c) r[c] = (c < NV && c != 2) ? acc[c] : 0.0f;
+        const float wm = SEARCH ? 0.0f : warp_max(acc[2]);
+        warp_sum_split<NP>(r, lane);
         const uint64_t inc = SEARCH ? warp_incl_scan_u64(cs, lane) : 0ull;
         __syncthreads();
-        if (lane == 0)
-#pragma unroll
-          for (int c = 0; c < NV; ++c) s_red[w * NV + c] = acc[c];
+        if (!(lane & ((1 << SH) - 1)) && (lane >> SH) < NV)
+          s_red[w * NV + (lane >> SH)] = (lane >> SH) == 2 ? wm : r[0];
         if (SEARCH && lane == 31) s_red64[w] = inc;
         __syncthreads();
         if (tid < 32) {
@@ -650,6 +711,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
           }
         }
       }
+      cp_async_wait_all();   // this thread's s_raw slot for the next frame
       __syncthreads();
       if (dbg)
         for (int i = tid; i < N; i += TB) A.dbg_anc[(size_t)t * N + i] = sA[i];
@@ -767,14 +829,6 @@ __device__ void block_merge(float& m, float& s, float& s2, float* v, float* red)
   }
 }
 
-// 16-byte global -> shared copies that complete asynchronously (cp.async, no
-// registers held while in flight), one commit group per particle step
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
 
 // Dynamic shared memory of bpf_stream_a: the model's parameter block
 // (params_floats: a | mb | L | Bm | mm | cumpi) and a two-slot ring holding
@@ -801,8 +855,11 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
   __shared__ float s_red[32 * (D + 3)];
   __shared__ bool s_last;
   __shared__ uint8_t s_ktab[kPickBins];
+  __shared__ PhiloxPre s_pre[D / 4];
+  __shared__ PhiloxKeys s_keys;
   const int tid = threadIdx.x, TB = blockDim.x;
   const int K = A.pv.K, J = A.pv.J;
+  const uint32_t frame = A.prior ? kFramePrior : step_frame(A);
   const LikConst LK = lik_const(A.pv, A.kappa, A.pd, A.sigma);
   // this block's copy of the model (the propagate and likelihood read it per
   // particle) and its component pick table; the prior's mu and S0c stay global
@@ -820,6 +877,8 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
   for (int q = tid; q < J * 3 * D; q += TB) s_Bm[q] = pv.Bm[q];
   for (int q = tid; q < J * 3; q += TB) s_mm[q] = pv.mm[q];
   for (int q = tid; q < K; q += TB) s_cum[q] = pv.cumpi[q];
+  if (tid == 0) s_keys = philox_keys(A.seed, A.track);
+  if (tid < D / 4) s_pre[tid] = philox_pre(A.seed, A.track, frame, (uint32_t)tid);
   __syncthreads();
   build_pick_table(s_cum, K, s_ktab, tid, TB);
   pv.a = s_a; pv.mb = s_mb; pv.Lq = s_L; pv.Ld = s_L; pv.Bm = s_Bm; pv.mm = s_mm;
@@ -844,11 +903,10 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
   for (int r = 0; r < D; ++r) v[r] = 0.0f;
   const int base = blockIdx.x * A.tile_a;
   const int end = min(A.N, base + A.tile_a);
-  const uint32_t frame = step_frame(A);
   if (A.prior) {
     for (int i = base + tid; i < end; i += TB) {
       float x[D], eps[D];
-      float uc = particle_draws<D>(A.seed, A.track, kFramePrior, (uint32_t)i, eps);
+      float uc = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i, eps);
       prior_sample<D>(pv, eps, uc, x);
       store_state<D>(A.xb, A.N, i, x);
     }
@@ -876,7 +934,7 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
     if (i + TB < end) gather_state_async<D>(ring, slot, tid, TB, A.xa, A.N, an_next);
     cp_async_commit();
     if (i + 2 * TB < end) an_next = A.anc[i + 2 * TB];
-    float uc = particle_draws<D>(A.seed, A.track, frame, (uint32_t)i, eps);
+    float uc = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i, eps);
     propagate<D, DIAG>(pv, eps, uc, x);
     store_state<D>(A.xb, A.N, i, x);
     float ll = loglik<D>(pv, x, s_cnt, s_det, LK);

@@ -89,6 +89,132 @@ MKF_HD uint32_t resample_uniform(uint64_t seed, uint32_t track, uint32_t frame) 
   return draw_block(seed, track, frame, kItemFrame, kStreamResample).x;
 }
 
+// ---------------------------------------------------------------- Philox, split by item
+// The particle draws are draw_block(seed, track, frame, item, stream) for the
+// items of one frame: the counter {frame, item, stream, 0} varies only in its
+// second word, which enters round 0 through one XOR.  Everything that does not
+// depend on the item is therefore computed once per frame and stream:
+//  round 0: both products (frame, stream) and three of the four output words;
+//  round 1: the product of word 2 and word 0's output (x1 below);
+//  round 2: the product of x1 and word 3's output (w2);
+// and the round keys once per track.  Per item that leaves one XOR, one product
+// and one XOR, then one product and two XORs, then seven full rounds: 34
+// operations instead of 60.  philox_item equals philox4x32_10 bit for bit
+// (checked on the host against the direct form).
+struct alignas(16) PhiloxPre {
+  uint32_t x0;   // round 0: word 0 = x0 ^ item
+  uint32_t z1;   // round 1: word 2 = hi(M0 (x0 ^ item)) ^ z1
+  uint32_t x2;   // round 2: word 0 = hi(M1 word2) ^ x2
+  uint32_t z2;   // round 2: word 2 = lo(M0 (x0 ^ item)) ^ z2
+  uint32_t w2;   // round 2: word 3
+  uint32_t pad[3];
+};
+struct alignas(16) PhiloxKeys { uint32_t k[14]; uint32_t pad[2]; };   // (k0, k1) of rounds 3..9
+
+MKF_HD void philox_mulhilo(uint32_t m, uint32_t a, uint32_t& lo, uint32_t& hi) {
+#ifdef __CUDA_ARCH__
+  lo = m * a;
+  hi = __umulhi(m, a);
+#else
+  const uint64_t p = (uint64_t)m * a;
+  lo = (uint32_t)p;
+  hi = (uint32_t)(p >> 32);
+#endif
+}
+
+MKF_HD PhiloxKeys philox_keys(uint64_t seed, uint32_t track) {
+  PhiloxKeys ks;
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32) ^ track;
+  for (int r = 1; r < 10; ++r) {
+    k0 += 0x9E3779B9u; k1 += 0xBB67AE85u;
+    if (r >= 3) { ks.k[2 * (r - 3)] = k0; ks.k[2 * (r - 3) + 1] = k1; }
+  }
+  ks.pad[0] = ks.pad[1] = 0u;
+  return ks;
+}
+
+MKF_HD PhiloxPre philox_pre(uint64_t seed, uint32_t track, uint32_t frame, uint32_t stream) {
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32) ^ track;
+  uint32_t l0, h0, l1, h1;
+  // round 0 on {frame, item, stream, 0}
+  philox_mulhilo(0xD2511F53u, frame, l0, h0);
+  philox_mulhilo(0xCD9E8D57u, stream, l1, h1);
+  const uint32_t y0 = l1, z0 = h0 ^ k1, w0 = l0;
+  PhiloxPre p;
+  p.x0 = h1 ^ k0;
+  // round 1: words 0 and 1 of the output depend only on z0 and y0
+  philox_mulhilo(0xCD9E8D57u, z0, l1, h1);
+  const uint32_t x1 = h1 ^ y0 ^ (k0 + 0x9E3779B9u), y1 = l1;
+  p.z1 = w0 ^ (k1 + 0xBB67AE85u);
+  // round 2: the product of x1
+  philox_mulhilo(0xD2511F53u, x1, l0, h0);
+  p.x2 = y1 ^ (k0 + 2u * 0x9E3779B9u);
+  p.z2 = h0 ^ (k1 + 2u * 0xBB67AE85u);
+  p.w2 = l0;
+  p.pad[0] = p.pad[1] = p.pad[2] = 0u;
+  return p;
+}
+
+// one round of philox4x32_10 with round key (k0, k1)
+MKF_HD u32x4 philox_round(u32x4 c, uint32_t k0, uint32_t k1) {
+  uint32_t lo0, hi0, lo1, hi1;
+  philox_mulhilo(0xD2511F53u, c.x, lo0, hi0);
+  philox_mulhilo(0xCD9E8D57u, c.z, lo1, hi1);
+  return u32x4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+}
+
+// rounds 0..2 of the split form: the counter words entering round 3
+MKF_HD u32x4 philox_item_head(const PhiloxPre& p, uint32_t item) {
+  uint32_t la, ha, lb, hb;
+  philox_mulhilo(0xD2511F53u, p.x0 ^ item, la, ha);   // round 1, word 0's product
+  const uint32_t z1 = ha ^ p.z1;                       // round 1 output: {x1, y1, z1, la}
+  philox_mulhilo(0xCD9E8D57u, z1, lb, hb);             // round 2, word 2's product
+  return u32x4{hb ^ p.x2, lb, la ^ p.z2, p.w2};
+}
+
+MKF_HD u32x4 philox_item(const PhiloxPre& p, const PhiloxKeys& ks, uint32_t item) {
+  u32x4 c = philox_item_head(p, item);
+  MKF_UNROLL
+  for (int r = 0; r < 7; ++r) c = philox_round(c, ks.k[2 * r], ks.k[2 * r + 1]);
+  return c;
+}
+
+#ifdef __CUDACC__
+// 16 bytes from shared memory on every call (volatile: never hoisted into
+// registers across a loop, which would cost the particle loops their registers)
+__device__ __forceinline__ uint4 lds_u4(const void* p) {
+  uint4 v;
+  asm volatile("ld.shared.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "r"((uint32_t)__cvta_generic_to_shared(p)));
+  return v;
+}
+
+// philox_item for NB streams of one item, the blocks advanced round by round
+// (each round key read once for all of them); pre and ks in shared memory
+template <int NB>
+__device__ __forceinline__ void philox_items_smem(const PhiloxPre* pre, const PhiloxKeys* ks, uint32_t item,
+                                                  u32x4* out) {
+#pragma unroll
+  for (int b = 0; b < NB; ++b) {
+    const uint4 a = lds_u4(&pre[b].x0);
+    const uint4 w = lds_u4(&pre[b].w2);
+    PhiloxPre p;
+    p.x0 = a.x; p.z1 = a.y; p.x2 = a.z; p.z2 = a.w; p.w2 = w.x;
+    out[b] = philox_item_head(p, item);
+  }
+#pragma unroll
+  for (int r = 0; r < 7; r += 2) {
+    const uint4 k = lds_u4(&ks->k[2 * r]);
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      out[b] = philox_round(out[b], k.x, k.y);
+      if (r + 1 < 7) out[b] = philox_round(out[b], k.z, k.w);
+    }
+  }
+}
+#endif
+
 // ---------------------------------------------------------------- component pick
 // First k with u < cumpi[k] (the last component if none): with cumpi
 // nondecreasing that is the number of c < K-1 with cumpi[c] <= u, counted with
@@ -221,6 +347,24 @@ __device__ __forceinline__ float particle_draws(uint64_t seed, uint32_t track, u
   return unit_bits(lowb << 8) - 1.0f;
 }
 
+// particle_draws with the item-independent Philox work done beforehand:
+// pre[b] = philox_pre(seed, track, frame, b) for b < D / 4, ks =
+// philox_keys(seed, track), both in shared memory.  Same values.
+template <int D>
+__device__ __forceinline__ float particle_draws_pre(const PhiloxPre* pre, const PhiloxKeys& ks, uint32_t item,
+                                                    float* eps) {
+  static_assert(D % 4 == 0, "particle_draws_pre: D must be a multiple of 4");
+  uint32_t lowb = 0;
+#pragma unroll
+  for (int b = 0; b < D / 4; ++b) {
+    u32x4 w;
+    philox_items_smem<1>(pre + b, &ks, item, &w);
+    if (b == 0) lowb = (w.x & 0xFFu) | ((w.y & 0xFFu) << 8) | ((w.z & 0xFFu) << 16);
+    box_muller2(w, eps + 4 * b);
+  }
+  return unit_bits(lowb << 8) - 1.0f;
+}
+
 // ---------------------------------------------------------------- block helpers
 __device__ __forceinline__ float warp_max(float v) {
 #pragma unroll
@@ -244,6 +388,30 @@ __device__ __forceinline__ uint64_t warp_incl_scan_u64(uint64_t v, int lane) {
     if (lane >= o) v += t;
   }
   return v;
+}
+
+// Sums of N values (N = 16 or 32) over the warp with 2 N - 1 exchanges instead
+// of 5 N: at each level a lane keeps half of its values and receives the other
+// lane's copy of that half.  Afterwards lane i << (5 - log2 N) holds total i in
+// v[0] (other entries are scratch).  The order of the additions is fixed.
+template <int N>
+__device__ __forceinline__ void warp_sum_split(float (&v)[N], int lane) {
+  static_assert(N == 16 || N == 32, "warp_sum_split: N must be 16 or 32");
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int o = 16 >> k, h = (N >> k) / 2;   // h values kept at this level (0: the last sums)
+    if (h >= 1) {
+      const bool upper = (lane & o) != 0;
+#pragma unroll
+      for (int i = 0; i < h; ++i) {
+        const float send = upper ? v[i] : v[i + h];
+        const float keep = upper ? v[i + h] : v[i];
+        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+      }
+    } else {
+      v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
+    }
+  }
 }
 
 // block-wide max; red must hold >= 32 floats; all threads get the result

@@ -22,7 +22,8 @@
 //    a sample.  (The weights cover the picks that the random-mixture workloads
 //    and the shipped models make.)
 //  - philox: philox4x32_10 (every draw of the kernels) against the Random123
-//    known-answer vectors;
+//    known-answer vectors; philox_split: the particle kernels' per-item form
+//    (philox_pre + philox_keys + philox_item) against the direct form;
 //  - walk: the scatter walk over per-thread chunks (scatter_walk with
 //    count_targets_le, the RBPF, PDAF, pf2D and scatter-variant resampler) and
 //    the 128-bit binary search (resample_search) against a direct two-pointer
@@ -241,6 +242,28 @@ static void philox() {
   std::printf("philox %lld %lld\n", bad, n);
 }
 
+// the per-item split (philox_pre / philox_keys / philox_item, used by the
+// particle kernels) against the direct philox4x32_10 of draw_block
+static void philox_split(std::mt19937_64& rng) {
+  long long bad = 0, n = 0;
+  for (int it = 0; it < 20000; ++it) {
+    const uint64_t seed = it < 4 ? (it & 1 ? ~0ull : 0ull) : rng();
+    const uint32_t track = it < 4 ? (it & 2 ? ~0u : 0u) : (uint32_t)rng();
+    const uint32_t frame = it % 7 == 0 ? mkf::kFramePrior : (uint32_t)(rng() % 4096);
+    const uint32_t stream = (uint32_t)(rng() % 8);
+    const mkf::PhiloxPre pre = mkf::philox_pre(seed, track, frame, stream);
+    const mkf::PhiloxKeys ks = mkf::philox_keys(seed, track);
+    for (int q = 0; q < 50; ++q) {
+      const uint32_t item = q < 2 ? (q ? ~0u : 0u) : (uint32_t)rng();
+      const mkf::u32x4 a = mkf::philox_item(pre, ks, item);
+      const mkf::u32x4 b = mkf::draw_block(seed, track, frame, item, stream);
+      bad += a.x != b.x || a.y != b.y || a.z != b.z || a.w != b.w;
+      ++n;
+    }
+  }
+  std::printf("philox_split %lld %lld\n", bad, n);
+}
+
 static void walk(std::mt19937_64& rng) {
   long long bad = 0, n = 0;
   for (int it = 0; it < 600; ++it) {
@@ -284,6 +307,7 @@ static void walk(std::mt19937_64& rng) {
 int main() {
   std::mt19937_64 rng(20140601);
   philox();
+  philox_split(rng);
   walk(rng);
   thresholds(rng);
   stride_walk(rng);
