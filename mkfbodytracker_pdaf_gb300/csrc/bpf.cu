@@ -185,23 +185,6 @@ __device__ __forceinline__ float ex2_neg(float s) {   // 2^(-s), MUFU.EX2
   return r;
 }
 
-// global -> shared copies that complete asynchronously (cp.async: no registers
-// held while in flight); the issuing thread waits for its own groups
-__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
-  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
-
 // Shared-memory detection layout of one joint (2 MKF_MAX_DET floats): pairs of
 // detections as (x_i, x_i+1, y_i, y_i+1), scaled by L.k, so that one 16-byte
 // load gives two detections' x and y as packed pairs.

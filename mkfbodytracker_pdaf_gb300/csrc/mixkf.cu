@@ -421,7 +421,12 @@ struct Smem {
   int* dcnt;            // [kDetBlock][MKF_MAX_J]
   float *w, *l, *wb, *red;
   double* dred;
+  float *stg0, *stg1;   // backward: staged frame records [xin | Pin | w (32) | xo], two buffers
 };
+
+// floats of one staged frame record (xin, Pin, the 32 weight slots, xo; the
+// same order and offsets as in the global frame record from FL.xin on)
+__host__ __device__ inline int stage_floats(int d) { return d + d * d + 32 + d; }
 
 // Prefetch the lists of frames g .. g+n-1 (n <= kDetBlock) into shared memory:
 // one coalesced pass instead of two dependent DRAM round trips per frame.
@@ -556,14 +561,17 @@ __device__ float* carve(Smem& s, float* base, int d) {
   p = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(p) + 7) & ~uintptr_t(7));
   s.dred = reinterpret_cast<double*>(p);
   p += 2 * 40;
+  p = reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
+  s.stg0 = p; p += stage_floats(d);
+  s.stg1 = p; p += stage_floats(d);
   return reinterpret_cast<float*>((reinterpret_cast<uintptr_t>(p) + 15) & ~uintptr_t(15));
 }
 
 // bytes of the shared state carved by carve() (an upper bound, 16-byte multiple)
 size_t mix_smem_bytes(int d) {
   size_t b = sizeof(float) * (size_t)(4 * d + 4 * d * d + d + 2 * kDetBlock * MKF_MAX_J * kMixMaxC +
-                                      kDetBlock * MKF_MAX_J + 32 * 3 + 64 + 8) +
-             sizeof(double) * 40 + 64;
+                                      kDetBlock * MKF_MAX_J + 32 * 3 + 64 + 8 + 2 * stage_floats(d)) +
+             sizeof(double) * 40 + 96;
   return (b + 15) & ~size_t(15);
 }
 
@@ -608,9 +616,10 @@ __global__ void __launch_bounds__(1024) mix_forward_kernel(MixArgs A) {
 // ---------------------------------------------------------------- backward kernel
 // Per segment of C frames: recompute the frames from the segment's checkpoint
 // keeping every frame's records (one forward), then reverse them.
-// STAGE: the per-component adjoint work blocks live in shared memory (used
-// when they fit), so the fixed-order cross-component sums read shared memory;
-// otherwise they stay in the global slot.  Records always stay in the slot.
+// STAGE: the per-component adjoint work blocks and the FP64 parameter
+// adjoints live in shared memory (used when they fit), so the fixed-order
+// cross-component sums and the per-segment flushes stay on chip; otherwise
+// both stay in the global slot.  Records always stay in the slot.
 template <int D, bool STAGE>
 __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
   extern __shared__ __align__(16) float msm[];
@@ -625,7 +634,13 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
   const int SR = fwd_scratch_floats(d);
   float* slot = A.slots + (size_t)blockIdx.x * A.slot_floats;
   float* frames = slot + (size_t)K * WL.size;               // C frame records
-  double* gacc = A.gacc + (size_t)blockIdx.x * A.ng;       // mu, a, Lq, sigma
+  // FP64 parameter adjoints (mu, a, Lq, sigma): STAGE: in shared memory
+  // behind the work blocks (copied to the CTA's global slot at the end), else
+  // the global slot itself
+  double* const gslot = A.gacc + (size_t)blockIdx.x * A.ng;
+  double* const gacc = STAGE ? reinterpret_cast<double*>(scr + (size_t)K * (SR + WL.size)) : gslot;
+  if (STAGE)
+    for (int i = tid; i < A.ng; i += TB) gacc[i] = 0.0;
   float* wb = STAGE ? scr + (size_t)K * SR + (size_t)k * WL.size     // this component's work block
                     : slot + (size_t)k * WL.size;
   float* const wbase = STAGE ? scr + (size_t)K * SR : slot;
@@ -635,12 +650,12 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
   float sbl = 0.0f;                                         // sigma adjoint of this segment (lane 0)
   double sbd = 0.0;                                         // and its FP64 running sum
   for (int i = lane; i < 2 * d + d * d; i += 32) wb[WL.gmu + i] = 0.0f;   // gmu, ga, Sq
-  // stage frame record fr's input state, mixture weights and collapsed mean
-  auto stage_frame = [&](const float* fr) {
-    for (int i = tid; i < d; i += TB) { s.xh[i] = fr[FL.xin + i]; s.xo[i] = fr[FL.xo + i]; }
-    for (int i = tid; i < d * d; i += TB) s.Ph[i] = fr[FL.Pin + i];
-    for (int i = tid; i < K; i += TB) s.w[i] = fr[FL.w + i];
-  };
+  // frame record fr's input state, mixture weights and collapsed mean
+  // (stage_floats(d) contiguous floats from FL.xin) are copied into a staging
+  // buffer with cp.async, and checkpoints (d + d^2 floats) into s.xh, s.Ph; the
+  // issuing threads wait for their copies before a barrier
+  constexpr int SG4 = (2 * D + D * D + 32) / 4, CK4 = (D + D * D) / 4;
+  const int fxin = FL.xin;
   for (int b = blockIdx.x; b < A.n_tracks; b += gridDim.x) {
     const int T = A.n_frames[b];
     const long long g0 = A.frame_base[b];
@@ -650,15 +665,17 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
     const float* ck = A.ck + A.ck_off[b];
     for (int i = tid; i < d; i += TB) s.Xb[i] = 0.0f;
     for (int i = tid; i < d * d; i += TB) s.Pb[i] = 0.0f;
-    __syncthreads();
     const int nck = (T + A.C - 1) / A.C;
+    // the last segment's checkpoint; each later one is copied while the
+    // segment after it is reversed (s.xh, s.Ph are free then)
+    if (nck > 0)
+      for (int i = tid; i < CK4; i += TB) cp_async16(s.xh + 4 * i, ck + (size_t)(nck - 1) * (d + d * d) + 4 * i);
+    cp_async_commit();
+    cp_async_wait_all();
+    __syncthreads();
     for (int sg = nck - 1; sg >= 0; --sg) {
       const int t0 = sg * A.C, t1 = min(T, t0 + A.C);
-      // ---- recompute the segment from its checkpoint, keeping every frame's records
-      const float* c0 = ck + (size_t)sg * (d + d * d);
-      for (int i = tid; i < d; i += TB) s.xh[i] = c0[i];
-      for (int i = tid; i < d * d; i += TB) s.Ph[i] = c0[d + i];
-      __syncthreads();
+      // ---- recompute the segment from its checkpoint (in s.xh, s.Ph), keeping every frame's records
       for (int t = t0; t < t1; ++t) {
         float* fr = frames + (size_t)(t - t0) * FL.size;
         for (int i = tid; i < d; i += TB) fr[FL.xin + i] = s.xh[i];
@@ -672,23 +689,39 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
         __syncthreads();
       }
       // ---- reverse the segment.  Four barriers a frame: the pass that sums
-      // frame t's per-component adjoints into Xb, Pb also stages frame t-1 and
-      // forms its symmetrised covariance adjoint Pcb from the same sums.
-      stage_frame(frames + (size_t)(t1 - 1 - t0) * FL.size);
+      // frame t's per-component adjoints into Xb, Pb also forms frame t-1's
+      // symmetrised covariance adjoint Pcb from the same sums.  Frame t-1's
+      // input state, weights and collapsed mean are copied into the other
+      // staging buffer while frame t is reversed.
+      for (int i = tid; i < SG4; i += TB)
+        cp_async16(s.stg0 + 4 * i, frames + (size_t)(t1 - 1 - t0) * FL.size + fxin + 4 * i);
+      cp_async_commit();
       for (int i = tid; i < d * d; i += TB) {
         const int r = i / d, c = i - r * d;
         s.Pcb[i] = 0.5f * (s.Pb[i] + s.Pb[c * d + r]);
       }
+      cp_async_wait_all();
       __syncthreads();
+      if (sg > 0)
+        for (int i = tid; i < CK4; i += TB) cp_async16(s.xh + 4 * i, ck + (size_t)(sg - 1) * (d + d * d) + 4 * i);
+      cp_async_commit();
       for (int t = t1 - 1; t >= t0; --t) {
         const float* fr = frames + (size_t)(t - t0) * FL.size;
         const float* cb = fr + (size_t)k * FL.comp_size;
-        const float* xin = s.xh;
-        const float* Pin = s.Ph;
-        const float* xo = s.xo;
+        const bool odd = ((t1 - 1 - t) & 1) != 0;   // frame t in stg1, else stg0; frame t-1 in the other
+        const float* st = odd ? s.stg1 : s.stg0;
+        if (t > t0) {
+          float* nx = odd ? s.stg0 : s.stg1;
+          for (int i = tid; i < SG4; i += TB) cp_async16(nx + 4 * i, fr - FL.size + fxin + 4 * i);
+        }
+        cp_async_commit();
+        const float* xin = st;
+        const float* Pin = st + d;
+        const float* wv = st + d + d * d;
+        const float* xo = wv + 32;
         const float* xk = cb + FL.comp_xk;
         const float* Pk = cb + FL.comp_Pk;
-        const float wk = fr[FL.w + k];
+        const float wk = wv[k];
         // collapse reverse: P' = sym(sum w (P_k + D D^T)), x' = sum w x_k, softmax (dc = 1)
         float* Dkb = wb + WL.Dkb;
         if (lane < d) {
@@ -714,7 +747,7 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
         if (lane == 0) s.wb[k] = wbk;
         __syncthreads();
         // sum_q w_q wb_q, formed by every warp in the same order
-        const float swb = wsum(lane < K ? s.w[lane] * s.wb[lane] : 0.0f);
+        const float swb = wsum(lane < K ? wv[lane] * s.wb[lane] : 0.0f);
         const float lb = wk * (wbk - swb) + wk;
         float* xb = wb + WL.xb;
         float* Pb = wb + WL.Pb;
@@ -779,7 +812,7 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
             s.Pcb[i] = 0.5f * (v + vt);
           }
         }
-        if (t > t0) stage_frame(fr - FL.size);
+        cp_async_wait_all();   // frame t-1's staging buffer (and the next checkpoint)
         __syncthreads();
       }
       // flush this segment's FP32 parameter adjoints into the CTA's FP64
@@ -835,6 +868,10 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
     double v = 0.0;
     for (int q = 0; q < K; ++q) v += s.dred[q];
     gacc[A.ng - 1] += v;
+  }
+  if (STAGE) {
+    __syncthreads();
+    for (int i = tid; i < A.ng; i += TB) gslot[i] = gacc[i];
   }
 }
 
@@ -970,7 +1007,8 @@ static int mix_grid(mkf_mixkf* h) {
   const size_t base = mix_smem_bytes(d);
   const int SRf = fwd_scratch_floats(d);
   h->smem_f = base + sizeof(float) * (size_t)K * SRf;
-  const size_t smem_stage = base + sizeof(float) * (size_t)K * (SRf + WL.size);
+  // STAGE: the work blocks and the FP64 parameter adjoints in shared memory
+  const size_t smem_stage = base + sizeof(float) * (size_t)K * (SRf + WL.size) + sizeof(double) * (size_t)h->ng;
   int dev = 0, optin = 0;
   MKF_CUDA(cudaGetDevice(&dev));
   MKF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));

@@ -180,6 +180,23 @@ MKF_HD u32x4 philox_item(const PhiloxPre& p, const PhiloxKeys& ks, uint32_t item
 }
 
 #ifdef __CUDACC__
+// global -> shared copies that complete asynchronously (cp.async: no registers
+// held while in flight); the issuing thread waits for its own groups
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
 // 16 bytes from shared memory on every call (volatile: never hoisted into
 // registers across a loop, which would cost the particle loops their registers)
 __device__ __forceinline__ uint4 lds_u4(const void* p) {
