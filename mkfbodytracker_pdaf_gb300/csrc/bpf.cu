@@ -207,7 +207,11 @@ template <int D, bool VEC = true>
 __device__ __forceinline__ float loglik(const PView& p, const float* x, const int* cnt, const float* det,
                                         const LikConst& L) {
   float ll = 0.0f;
-  for (int j = 0; j < p.J; ++j) {
+  // unrolled to the largest joint count, so that the joints' independent
+  // chains (projection, detection sum, logarithm) can overlap
+#pragma unroll
+  for (int j = 0; j < MKF_MAX_J; ++j) {
+    if (j >= p.J) break;
     const float* B = p.Bm + j * 3 * D;
     float q0, q1, q2;
     if (VEC) {
@@ -248,12 +252,16 @@ __device__ __forceinline__ float loglik(const PView& p, const float* x, const in
     // four partial sums (detection i into sum i mod 4) so the exponentials of
     // a list overlap; sums (0, 1) and (2, 3) are packed pairs.  The list is
     // padded with +inf detections to a multiple of four (stage_list): their
-    // terms are 2^-inf = +0 exactly, so every group runs the same code.
+    // terms are 2^-inf = +0 exactly, so every group runs the same code.  The
+    // loop is unrolled to the longest list, so that the groups' loads and
+    // exponentials can be issued ahead of the sums.
     float2 accA = make_float2(0.0f, 0.0f), accB = make_float2(0.0f, 0.0f);
     const float* dj = det + j * 2 * MKF_MAX_DET;
     const float2 uu = make_float2(u, u), vv = make_float2(v, v);
     const int n = (cnt[j] + 3) & ~3;
-    for (int i = 0; i < n; i += 4) {
+#pragma unroll
+    for (int i = 0; i < MKF_MAX_DET; i += 4) {
+      if (i >= n) break;
       const float4 g0 = ld4(dj + 2 * i), g1 = ld4(dj + 2 * i + 4);
       const float2 dxA = pk_sub(make_float2(g0.x, g0.y), uu), dyA = pk_sub(make_float2(g0.z, g0.w), vv);
       const float2 dxB = pk_sub(make_float2(g1.x, g1.y), uu), dyB = pk_sub(make_float2(g1.z, g1.w), vv);
@@ -551,6 +559,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       for (int c = 0; c < NV; ++c) acc[c] = 0.0f;   // s, s2, wmax, v[D]
       uint64_t cs = 0;
       if (SEARCH) {
+#pragma unroll 4
         for (int j = j0; j < j1; ++j) {
           const float ll = LOW ? __uint_as_float((uint32_t)sQ[j]) : __int_as_float(sA[j]);
           float w = fb ? 0.0f : (ll == M ? 1.0f : __expf(ll - M));
@@ -643,6 +652,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       const uint32_t U = resample_uniform(seed, trk, (uint32_t)t);
       if (SEARCH) {
         uint64_t pre = P;
+#pragma unroll 4
         for (int j = j0; j < j1; ++j) {
           pre += sQ[j];
           sQ[j] = pre;
