@@ -377,6 +377,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
   // while this frame runs (thread q < J MKF_MAX_DET owns slot q)
   __shared__ int s_offn[MKF_MAX_J + 1];
   __shared__ int s_nn[MKF_MAX_J];   // the next frame's list lengths
+  __shared__ int s_lmax;            // this frame's max log-weight, order-preserving int form
   __shared__ __align__(8) float2 s_raw[MKF_MAX_J * MKF_MAX_DET];
 
   float* xa0 = A.scratch + (size_t)blockIdx.x * 2 * D * Nmax;
@@ -475,6 +476,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       if (t + 1 < T && tid <= J) cp_async4(&s_offn[tid], A.det_off + (g + 1) * J + tid);
       cp_async_commit();
       if (tid < D / 4) s_pre[tid] = philox_pre(seed, trk, (uint32_t)t, (uint32_t)tid);
+      if (tid == 0) s_lmax = float_ordered(-INFINITY);
       __syncthreads();
 
       // ---- propagate from the resampled set and score.  Besides the
@@ -536,8 +538,15 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
           for (int r = 0; r < D / 2; ++r) fv[r] = pk_fma(ww, make_float2(x[2 * r], x[2 * r + 1]), fv[r]);
         }
       }
-      if (tid <= J) cp_async_wait_all();   // s_offn, visible after block_max's barriers
-      const float M = block_max(lmax, s_red);
+      if (tid <= J) cp_async_wait_all();   // s_offn, visible after the barrier below
+      // block max: one shared atomic per warp and one barrier (the max is
+      // order independent, so M is the same as any reduction tree's)
+      {
+        const float wmx = warp_max(lmax);
+        if ((tid & 31) == 0) atomicMax(&s_lmax, float_ordered(wmx));
+      }
+      __syncthreads();
+      const float M = float_unordered(s_lmax);
       // the next frame's detections, copied while this frame resamples
       if (tid < J * MKF_MAX_DET && t + 1 < T) {
         const int qj = tid / MKF_MAX_DET, qi = tid % MKF_MAX_DET;
@@ -613,7 +622,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
         const float wm = SEARCH ? 0.0f : warp_max(acc[2]);
         warp_sum_split<NP>(r, lane);
         const uint64_t inc = SEARCH ? warp_incl_scan_u64(cs, lane) : 0ull;
-        __syncthreads();
+        // (s_red and s_red64 were last read before the previous frame's final barrier)
         if (!(lane & ((1 << SH) - 1)) && (lane >> SH) < NV)
           s_red[w * NV + (lane >> SH)] = (lane >> SH) == 2 ? wm : r[0];
         if (SEARCH && lane == 31) s_red64[w] = inc;

@@ -329,14 +329,18 @@ __device__ __forceinline__ float unit_bits(uint32_t w) { return __uint_as_float(
 // Both Box-Muller pairs of one Philox block, (w.x, w.y) -> z[0], z[1] and
 // (w.z, w.w) -> z[2], z[3], with the two pairs' arithmetic in packed f32x2
 // instructions.  Uniforms of 23 bits: u1 = 2 - [1, 2) in (0, 1], u2 = [1, 2) - 1
-// in [0, 1), both exact.  r = sqrt(-2 ln u1) with -2 ln u1 = lg2(u1) (-2 ln 2),
-// angle pi (2 u2 - 1) as fma(2 pi, u2, -pi) (the same single rounding), z = r (cos, sin).
+// in [0, 1), both exact.  r = sqrt(-2 ln u1) with -2 ln u1 = lg2(u1) (-2 ln 2)
+// and sqrt.approx, angle pi (2 u2 - 1) as fma(2 pi, u2, -pi) (the same single
+// rounding), z = r (cos, sin).
 __device__ __forceinline__ void box_muller2(u32x4 w, float* z) {
   const float2 u1 = pk_sub(make_float2(2.0f, 2.0f), make_float2(unit_bits(w.x), unit_bits(w.z)));
   const float2 u2 = pk_sub(make_float2(unit_bits(w.y), unit_bits(w.w)), make_float2(1.0f, 1.0f));
   const float2 y = pk_mul(make_float2(lg2_approx(u1.x), lg2_approx(u1.y)),
                           make_float2(-1.3862943611198906f, -1.3862943611198906f));
-  const float2 r = pk_mul(y, make_float2(rsqrtf(fmaxf(y.x, 1e-30f)), rsqrtf(fmaxf(y.y, 1e-30f))));
+  float r0, r1;   // MUFU square roots (y >= 0; y = 0 gives 0)
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(y.x));
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r1) : "f"(y.y));
+  const float2 r = make_float2(r0, r1);
   const float2 ang = pk_fma(make_float2(6.283185307179586f, 6.283185307179586f), u2,
                             make_float2(-3.14159265358979f, -3.14159265358979f));
   float s0, c0, s1, c1;
@@ -430,6 +434,14 @@ __device__ __forceinline__ void warp_sum_split(float (&v)[N], int lane) {
     }
   }
 }
+
+// An int whose signed order is the float order (any non-NaN float), so that
+// atomicMax on it is a float max; float_unordered inverts it.
+__device__ __forceinline__ int float_ordered(float f) {
+  const int i = __float_as_int(f);
+  return i ^ ((i >> 31) & 0x7FFFFFFF);
+}
+__device__ __forceinline__ float float_unordered(int i) { return __int_as_float(i ^ ((i >> 31) & 0x7FFFFFFF)); }
 
 // block-wide max; red must hold >= 32 floats; all threads get the result
 __device__ __forceinline__ float block_max(float v, float* red) {
