@@ -378,6 +378,9 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
   __shared__ int s_offn[MKF_MAX_J + 1];
   __shared__ int s_nn[MKF_MAX_J];   // the next frame's list lengths
   __shared__ int s_lmax;            // this frame's max log-weight, order-preserving int form
+  __shared__ uint32_t s_U;          // this frame's resampling uniform
+  __shared__ RsThresh s_th;         // and the resampling rule's constants (SEARCH)
+  __shared__ RsStep s_st1, s_st4;
   __shared__ __align__(8) float2 s_raw[MKF_MAX_J * MKF_MAX_DET];
 
   float* xa0 = A.scratch + (size_t)blockIdx.x * 2 * D * Nmax;
@@ -477,6 +480,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       cp_async_commit();
       if (tid < D / 4) s_pre[tid] = philox_pre(seed, trk, (uint32_t)t, (uint32_t)tid);
       if (tid == 0) s_lmax = float_ordered(-INFINITY);
+      if (tid == 32) s_U = resample_uniform(seed, trk, (uint32_t)t);
       __syncthreads();
 
       // ---- propagate from the resampled set and score.  Besides the
@@ -645,6 +649,14 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
         if (SEARCH) {
           P = s_red64[w] + inc - cs;
           Qt = s_red64[32];
+          // the rule's constants (64-bit divisions) once, published by the
+          // prefix pass's barrier
+          if (tid == 0 && Qt != 0) {
+            const RsThresh th = rs_thresh_setup(Qt, N, s_U);
+            s_th = th;
+            s_st1 = rs_step_setup(th, (uint32_t)TB);
+            s_st4 = rs_step_setup(th, 4u * (uint32_t)TB);
+          }
         }
       }
       const float S = s_red[0], S2 = s_red[1], Wmax = s_red[2];
@@ -658,7 +670,7 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
       // ---- exact systematic resampling: SEARCH: chunk prefix sums in place,
       // then a binary search per target; otherwise chunk sums, block scan and
       // a scatter walk per chunk
-      const uint32_t U = resample_uniform(seed, trk, (uint32_t)t);
+      const uint32_t U = s_U;
       if (SEARCH) {
         uint64_t pre = P;
 #pragma unroll 4
@@ -671,14 +683,15 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
           for (int i = tid; i < N; i += TB) sA[i] = resample_fallback_index(U, i, N);
         } else {
           // four targets per thread at a time (i, i + TB, i + 2 TB, i + 3 TB),
-          // their thresholds walked along the stride (one division per frame);
-          // a target past N - 1 is searched (in bounds) but not stored
-          const RsThresh th = rs_thresh_setup(Qt, N, U);
-          const RsStep st4 = rs_step_setup(th, 4u * (uint32_t)TB);
+          // their thresholds walked along the stride (one 32-bit division per
+          // thread and frame); a target past N - 1 is searched (in bounds) but
+          // not stored
+          const RsThresh th = s_th;
+          const RsStep st4 = s_st4;
           RsWalk wk[4];
           wk[0] = rs_walk_init(th, (uint32_t)tid);
           {
-            const RsStep st1 = rs_step_setup(th, (uint32_t)TB);
+            const RsStep st1 = s_st1;
 #pragma unroll
             for (int g = 1; g < 4; ++g) { wk[g] = wk[g - 1]; rs_walk_next(th, st1, wk[g]); }
           }
