@@ -1068,35 +1068,12 @@ __global__ void __launch_bounds__(256, 5) bpf_stream_c(StreamArgs A, int tile_c)
   __shared__ int s_lo, s_hi;
   __shared__ RsThresh s_th;
   __shared__ RsStep s_st[2];
-  const int tid = threadIdx.x, TB = blockDim.x;
+  const int tid = threadIdx.x, TB = blockDim.x, lane = tid & 31, w = tid >> 5;
   const float M = A.fs->M;
-  // the total Qt and this tile's exclusive prefix, from the tile sums of
-  // bpf_stream_b (every block forms them: a few thousand L2-resident words)
-  uint64_t all = 0, before = 0;
-  for (int q = tid; q < (int)gridDim.x; q += TB) {
-    const uint64_t v = A.bsum[q];
-    all += v;
-    before += (q < (int)blockIdx.x) ? v : 0ull;
-  }
-  uint64_t Qt, Xprev;
-  block_excl_scan_u64(all, s_red64, &Qt);
-  block_excl_scan_u64(before, s_red64, &Xprev);
-  const int fb = A.fs->fb || Qt == 0ull;
-  if (blockIdx.x == 0 && tid == 0 && Qt == 0ull && !A.fs->fb) atomicOr(&A.fs->status, MKF_ST_FALLBACK);
+  const int fbM = A.fs->fb;
   const int base = blockIdx.x * tile_c, end = min(A.N, base + tile_c), n = end - base;
-  const uint32_t U = step_uniform(A);
-  if (fb) {
-    for (int i = base + tid; i < end; i += TB) A.anc_out[i] = resample_fallback_index(U, i, A.N);
-    return;
-  }
-  // the resampling rule's constants (64-bit divisions), once per block
-  if (tid < 32) {
-    const RsThresh th = rs_thresh_setup(Qt, A.N, U);
-    const RsStep st1 = rs_step_setup(th, (uint32_t)TB), st4 = rs_step_setup(th, 4u * (uint32_t)TB);
-    if (tid == 0) { s_th = th; s_st[0] = st1; s_st[1] = st4; }
-  }
-  // the tile's integer weights, read coalesced, then prefix sums over
-  // contiguous chunks of an odd length (distinct banks across a warp)
+  // the tile's integer weights (they need M only), read coalesced; issued
+  // first, so that their loads overlap the tile-sum loads below
   {
     const int n4 = n >> 2;
     const float4* l4 = reinterpret_cast<const float4*>(A.logw + base);
@@ -1104,12 +1081,45 @@ __global__ void __launch_bounds__(256, 5) bpf_stream_c(StreamArgs A, int tile_c)
     for (int q = tid; q < n4; q += TB) {
       const float4 lw = l4[q];
       ulonglong2* d2 = reinterpret_cast<ulonglong2*>(sQ) + 2 * q;
-      d2[0] = make_ulonglong2(quantize39(stream_weight(lw.x, M, fb)), quantize39(stream_weight(lw.y, M, fb)));
-      d2[1] = make_ulonglong2(quantize39(stream_weight(lw.z, M, fb)), quantize39(stream_weight(lw.w, M, fb)));
+      d2[0] = make_ulonglong2(quantize39(stream_weight(lw.x, M, fbM)), quantize39(stream_weight(lw.y, M, fbM)));
+      d2[1] = make_ulonglong2(quantize39(stream_weight(lw.z, M, fbM)), quantize39(stream_weight(lw.w, M, fbM)));
     }
-    for (int j = 4 * n4 + tid; j < n; j += TB) sQ[j] = quantize39(stream_weight(A.logw[base + j], M, fb));
+    for (int j = 4 * n4 + tid; j < n; j += TB) sQ[j] = quantize39(stream_weight(A.logw[base + j], M, fbM));
   }
+  // the total Qt and this tile's exclusive prefix, from the tile sums of
+  // bpf_stream_b (every block forms them: a few thousand L2-resident words);
+  // block totals of two integer sums, one barrier (which also publishes sQ)
+  uint64_t all = 0, before = 0;
+  for (int q = tid; q < (int)gridDim.x; q += TB) {
+    const uint64_t v = A.bsum[q];
+    all += v;
+    before += (q < (int)blockIdx.x) ? v : 0ull;
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    all += __shfl_xor_sync(0xffffffffu, all, o);
+    before += __shfl_xor_sync(0xffffffffu, before, o);
+  }
+  if (lane == 0) { s_red64[w] = all; s_red64[16 + w] = before; }
   __syncthreads();
+  uint64_t Qt = 0, Xprev = 0;
+  for (int q = 0; q < (TB >> 5); ++q) { Qt += s_red64[q]; Xprev += s_red64[16 + q]; }
+  const int fb = fbM || Qt == 0ull;
+  if (blockIdx.x == 0 && tid == 0 && Qt == 0ull && !fbM) atomicOr(&A.fs->status, MKF_ST_FALLBACK);
+  const uint32_t U = step_uniform(A);
+  if (fb) {
+    for (int i = base + tid; i < end; i += TB) A.anc_out[i] = resample_fallback_index(U, i, A.N);
+    return;
+  }
+  // the resampling rule's constants (64-bit divisions), once per block (read
+  // after the chunk scan's barriers)
+  if (tid == 0) {
+    const RsThresh th = rs_thresh_setup(Qt, A.N, U);
+    s_th = th;
+    s_st[0] = rs_step_setup(th, (uint32_t)TB);
+    s_st[1] = rs_step_setup(th, 4u * (uint32_t)TB);
+  }
+  // prefix sums over contiguous chunks of an odd length (distinct banks across a warp)
   int E = (n + TB - 1) / TB;
   if (E > 1 && !(E & 1)) ++E;
   const int j0 = min(n, tid * E), j1 = min(n, j0 + E);
@@ -1124,7 +1134,6 @@ __global__ void __launch_bounds__(256, 5) bpf_stream_c(StreamArgs A, int tile_c)
   // the tile's target range [lo, hi): warp 0 and warp 1 count the targets at
   // or below each end of the tile's prefix range
   {
-    const int w = tid >> 5;
     if (w < 2) {
       const RsThresh th = s_th;
       const bool first = (w == 0) ? (blockIdx.x == 0) : (blockIdx.x == gridDim.x - 1);
