@@ -375,14 +375,14 @@ template <int D>
 __device__ __forceinline__ float particle_draws_pre(const PhiloxPre* pre, const PhiloxKeys& ks, uint32_t item,
                                                     float* eps) {
   static_assert(D % 4 == 0, "particle_draws_pre: D must be a multiple of 4");
-  uint32_t lowb = 0;
+  // every block's Philox first (independent chains the scheduler can
+  // interleave), then the Box-Muller pairs
+  u32x4 w[D / 4];
 #pragma unroll
-  for (int b = 0; b < D / 4; ++b) {
-    u32x4 w;
-    philox_items_smem<1>(pre + b, &ks, item, &w);
-    if (b == 0) lowb = (w.x & 0xFFu) | ((w.y & 0xFFu) << 8) | ((w.z & 0xFFu) << 16);
-    box_muller2(w, eps + 4 * b);
-  }
+  for (int b = 0; b < D / 4; ++b) philox_items_smem<1>(pre + b, &ks, item, &w[b]);
+  const uint32_t lowb = (w[0].x & 0xFFu) | ((w[0].y & 0xFFu) << 8) | ((w[0].z & 0xFFu) << 16);
+#pragma unroll
+  for (int b = 0; b < D / 4; ++b) box_muller2(w[b], eps + 4 * b);
   return unit_bits(lowb << 8) - 1.0f;
 }
 
