@@ -333,13 +333,16 @@ __host__ __device__ constexpr int params_floats(int K, int J, bool diag) {
 // shared memory (the layout of each variant below), then the track's model.
 // Per frame: propagate + score (accumulating the estimate sums), block max,
 // weights and ESS, exact systematic resampling, the gather folded into the
-// next frame's propagate.
+// next frame's propagate.  The next frame's detection lists are copied with
+// cp.async while a frame resamples, and the Philox words and resampling
+// constants that do not depend on the particle are formed once per frame.
 // Code variants chosen by the autotuner: VEC (float4 vs scalar parameter loads)
 // and SEARCH (ancestors by binary search over the shared prefix sums, 12 Nmax
 // bytes of shared memory, vs the scatter walk over each thread's chunk, 8 Nmax).
 // LOW (with SEARCH): 8 Nmax bytes of shared memory, so that three CTAs of the
 // largest tracks fit on an SM; the log-weights are kept in the prefix array's
-// entries and the ancestors in the CTA's global slot (L2).
+// entries, and the ancestors in shared memory behind the N prefix entries
+// when 3 N <= 2 Nmax, else in the CTA's global slot (L2).
 template <int D, bool DIAG, int TBMAX, int MINB, bool VEC, bool SEARCH, bool PAIR = false, bool LOW = false>
 __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
   static_assert(!LOW || (SEARCH && !PAIR), "the LOW layout is a SEARCH variant");

@@ -443,18 +443,6 @@ __device__ __forceinline__ int float_ordered(float f) {
 }
 __device__ __forceinline__ float float_unordered(int i) { return __int_as_float(i ^ ((i >> 31) & 0x7FFFFFFF)); }
 
-// block-wide max; red must hold >= 32 floats; all threads get the result
-__device__ __forceinline__ float block_max(float v, float* red) {
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
-  v = warp_max(v);
-  __syncthreads();
-  if (lane == 0) red[w] = v;
-  __syncthreads();
-  float r = lane < nw ? red[lane] : -INFINITY;
-  r = warp_max(r);
-  return r;
-}
-
 // exclusive block scan of one uint64 per thread; red holds >= 33 uint64
 __device__ __forceinline__ uint64_t block_excl_scan_u64(uint64_t v, uint64_t* red, uint64_t* total) {
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
