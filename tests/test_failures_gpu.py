@@ -29,11 +29,14 @@ def _poisoned_batch():
     return batch, g
 
 
-def test_batched_reports_and_recovers(cuda, olib):
+@pytest.mark.parametrize("variant", [3, 11], ids=["search", "search_lowsmem"])
+def test_batched_reports_and_recovers(cuda, olib, variant):
+    """Both search layouts; the over-long list is in frame 2, so it reaches the
+    kernel through the next-frame list copy, not the first frame's direct read."""
     from mkfbodytracker_pdaf_gb300.filters import BatchedBootstrapPF
     torch = cuda
     batch, g_nan = _poisoned_batch()
-    runner = BatchedBootstrapPF(batch, block_threads=256, variant=3)
+    runner = BatchedBootstrapPF(batch, block_threads=256, ctas_per_sm=3 if variant == 11 else 0, variant=variant)
     N0, T0 = int(batch.tracks[0]["n_particles"]), int(batch.tracks[0]["n_frames"])
     wd = torch.zeros((T0, N0), dtype=torch.float32, device="cuda")
     ad = torch.zeros((T0, N0), dtype=torch.int32, device="cuda")
@@ -55,6 +58,30 @@ def test_batched_reports_and_recovers(cuda, olib):
     g0 = int(batch.tracks[0]["frame_base"])
     assert np.isfinite(e[g_nan + 1:g0 + T0]).all()
     assert np.isfinite(e[int(batch.tracks[1]["frame_base"]):]).all()
+
+
+def test_batched_first_frame_truncation(cuda):
+    """An over-long list in a track's first frame (read directly, not copied
+    ahead) is truncated and reported the same way."""
+    from mkfbodytracker_pdaf_gb300 import synth
+    from mkfbodytracker_pdaf_gb300.filters import BatchedBootstrapPF
+    batch = synth.make_bpf_batch(17, [400, 900], [3, 3], [2.0, 2.0], [0.9, 0.9])
+    J = batch.model["J"]
+    det = batch.det.copy()
+    off = batch.det_off.astype(np.int64).copy()
+    g = int(batch.tracks[1]["frame_base"])          # track 1, frame 0, joint 0
+    lo, hi = off[g * J], off[g * J + 1]
+    extra = np.tile(np.array([[320.0, 240.0]], np.float32), (20 - (hi - lo), 1))
+    det = np.concatenate([det[:hi], extra, det[hi:]]).astype(np.float32)
+    off[g * J + 1:] += len(extra)
+    batch.det, batch.det_off = det, off.astype(batch.det_off.dtype)
+    for variant, cps in ((3, 0), (11, 3)):
+        runner = BatchedBootstrapPF(batch, block_threads=256, ctas_per_sm=cps, variant=variant)
+        est, ll, ess, st = runner.run(*runner.device_inputs())
+        cuda.cuda.synchronize()
+        st = st.cpu().numpy()
+        assert st[0] == 0 and st[1] == ST_TRUNC, (variant, st)
+        assert np.isfinite(est.cpu().numpy()).all()
 
 
 def test_plain_path_reports_nan_frame(cuda):
