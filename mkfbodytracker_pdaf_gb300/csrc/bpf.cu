@@ -99,14 +99,14 @@ struct PView {
 
 // mixture component of a particle-frame (mkf_common.cuh: by count, or through
 // the track's kPickBins table when the view has one)
-__device__ __forceinline__ int pick_component(const PView& p, float u) {
-  return p.ktab ? pick_component_table(p.ktab, p.cumpi, p.K, u) : pick_component(p.cumpi, p.K, u);
+__device__ __forceinline__ int pick_component(const PView& p, float u, int ubin) {
+  return p.ktab ? pick_component_table_bin(p.ktab, p.cumpi, p.K, u, ubin) : pick_component(p.cumpi, p.K, u);
 }
 
 template <int D>
-__device__ __forceinline__ void prior_sample(const PView& p, const float* eps, float uc, float* x) {
+__device__ __forceinline__ void prior_sample(const PView& p, const float* eps, float uc, int ubin, float* x) {
   constexpr int DD = D * (D + 1) / 2;
-  int k = pick_component(p, uc);
+  int k = pick_component(p, uc, ubin);
   const float* L = p.S0c + k * DD;
 #pragma unroll
   for (int r = 0; r < D; ++r) {
@@ -122,9 +122,9 @@ __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast
 // x' = A_k x + (I - A_k) mu_k + L_k eps.  VEC: float4 parameter loads (rows of
 // a, mb, Ld, Bm are 16-byte aligned since D % 4 == 0); otherwise scalar loads.
 template <int D, bool DIAG, bool VEC = true>
-__device__ __forceinline__ void propagate(const PView& p, const float* eps, float uc, float* x) {
+__device__ __forceinline__ void propagate(const PView& p, const float* eps, float uc, int ubin, float* x) {
   constexpr int DD = D * (D + 1) / 2;
-  int k = pick_component(p, uc);
+  int k = pick_component(p, uc, ubin);
   const float* a = p.a + k * D;
   const float* mb = p.mb + k * D;
   if (DIAG) {
@@ -437,8 +437,9 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
     // prior draw (frame index 0xFFFFFFFF), identity ancestry
     for (int i = tid; i < N; i += TB) {
       float eps[D], x[D];
-      float uc = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i, eps);
-      prior_sample<D>(pv, eps, uc, x);
+      int ub;
+      float uc = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i, eps, ub);
+      prior_sample<D>(pv, eps, uc, ub, x);
       store_state<D>(xa, Nmax, i, x);
       sA[i] = i;
     }
@@ -509,10 +510,11 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
           float x[D], eps[D], y[D], eps2[D];
           load_state<D>(xa, Nmax, an, x);
           load_state<D>(xa, Nmax, an2, y);
-          const float uc = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i, eps);
-          const float uc2 = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i2, eps2);
-          propagate<D, DIAG, VEC>(pv, eps, uc, x);
-          propagate<D, DIAG, VEC>(pv, eps2, uc2, y);
+          int ub, ub2;
+          const float uc = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i, eps, ub);
+          const float uc2 = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i2, eps2, ub2);
+          propagate<D, DIAG, VEC>(pv, eps, uc, ub, x);
+          propagate<D, DIAG, VEC>(pv, eps2, uc2, ub2, y);
           store_state<D>(xb, Nmax, i, x);
           const float ll = loglik<D, VEC>(pv, x, s_cnt, s_det, LK);
           if (SEARCH) sA[i] = __float_as_int(ll); else sW[i] = ll;
@@ -529,8 +531,9 @@ __global__ void __launch_bounds__(TBMAX, MINB) bpf_batched_kernel(BatchArgs A) {
           const int an = sA[i];
           float x[D], eps[D];
           load_state<D>(xa, Nmax, an, x);
-          float uc = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i, eps);
-          propagate<D, DIAG, VEC>(pv, eps, uc, x);
+          int ub;
+          float uc = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i, eps, ub);
+          propagate<D, DIAG, VEC>(pv, eps, uc, ub, x);
           store_state<D>(xb, Nmax, i, x);
           float ll = loglik<D, VEC>(pv, x, s_cnt, s_det, LK);
           if (LOW) sQ[i] = (uint64_t)__float_as_uint(ll);
@@ -924,8 +927,9 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
   if (A.prior) {
     for (int i = base + tid; i < end; i += TB) {
       float x[D], eps[D];
-      float uc = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i, eps);
-      prior_sample<D>(pv, eps, uc, x);
+      int ub;
+      float uc = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i, eps, ub);
+      prior_sample<D>(pv, eps, uc, ub, x);
       store_state<D>(A.xb, A.N, i, x);
     }
     return;
@@ -952,8 +956,9 @@ __global__ void __launch_bounds__(256) bpf_stream_a(StreamArgs A) {
     if (i + TB < end) gather_state_async<D>(ring, slot, tid, TB, A.xa, A.N, an_next);
     cp_async_commit();
     if (i + 2 * TB < end) an_next = A.anc[i + 2 * TB];
-    float uc = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i, eps);
-    propagate<D, DIAG>(pv, eps, uc, x);
+    int ub;
+    float uc = particle_draws_pre<D>(s_pre, s_keys, (uint32_t)i, eps, ub);
+    propagate<D, DIAG>(pv, eps, uc, ub, x);
     store_state<D>(A.xb, A.N, i, x);
     float ll = loglik<D>(pv, x, s_cnt, s_det, LK);
     A.logw[i] = ll;

@@ -271,6 +271,18 @@ MKF_HD int pick_component_table(const uint8_t* tab, const float* cumpi, int K, f
     while (k < K - 1 && u >= cumpi[k]) ++k;
   return k;
 }
+// the same with u's bin floor(u kPickBins) given (the particle draws form it
+// from the uniform's bits without a float-to-int conversion)
+MKF_HD int pick_component_table_bin(const uint8_t* tab, const float* cumpi, int K, float u, int bin) {
+  const int e = tab[bin];
+  int k = e & 0x7F;
+  if (e & 0x80)
+    while (k < K - 1 && u >= cumpi[k]) ++k;
+  return k;
+}
+// u = ((lowb << 8) >> 9) 2^-23 for the 24-bit value lowb of the particle
+// draws, so floor(u kPickBins) = lowb >> 14 exactly (kPickBins = 2^10)
+MKF_HD int pick_bin_of(uint32_t lowb) { return (int)(lowb >> 14); }
 
 #ifdef __CUDACC__
 // ---------------------------------------------------------------- packed FP32 pairs
@@ -370,10 +382,11 @@ __device__ __forceinline__ float particle_draws(uint64_t seed, uint32_t track, u
 
 // particle_draws with the item-independent Philox work done beforehand:
 // pre[b] = philox_pre(seed, track, frame, b) for b < D / 4, ks =
-// philox_keys(seed, track), both in shared memory.  Same values.
+// philox_keys(seed, track), both in shared memory.  Same values; ubin is the
+// component uniform's bin of the pick table.
 template <int D>
 __device__ __forceinline__ float particle_draws_pre(const PhiloxPre* pre, const PhiloxKeys& ks, uint32_t item,
-                                                    float* eps) {
+                                                    float* eps, int& ubin) {
   static_assert(D % 4 == 0, "particle_draws_pre: D must be a multiple of 4");
   // every block's Philox first (independent chains the scheduler can
   // interleave), then the Box-Muller pairs
@@ -383,6 +396,7 @@ __device__ __forceinline__ float particle_draws_pre(const PhiloxPre* pre, const 
   const uint32_t lowb = (w[0].x & 0xFFu) | ((w[0].y & 0xFFu) << 8) | ((w[0].z & 0xFFu) << 16);
 #pragma unroll
   for (int b = 0; b < D / 4; ++b) box_muller2(w[b], eps + 4 * b);
+  ubin = pick_bin_of(lowb);
   return unit_bits(lowb << 8) - 1.0f;
 }
 

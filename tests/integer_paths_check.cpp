@@ -35,6 +35,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <limits>
 #include <random>
 #include <vector>
@@ -225,6 +226,43 @@ static void pick(std::mt19937_64& rng) {
   std::printf("pick %lld %lld\n", bad, n);
 }
 
+// the pick table's bin from the particle draws' 24-bit value lowb, without a
+// float conversion (pick_bin_of), against floor(u kPickBins) of the uniform
+// u = ((lowb << 8) >> 9) 2^-23 that the kernels pass beside it, for every lowb;
+// and the table pick with that bin against the count
+static void pickbin(std::mt19937_64& rng) {
+  long long bad = 0, n = 0;
+  for (uint32_t lowb = 0; lowb < (1u << 24); ++lowb) {
+    uint32_t bits = 0x3F800000u | ((lowb << 8) >> 9);
+    float f;
+    std::memcpy(&f, &bits, 4);
+    const float u = f - 1.0f;
+    bad += mkf::pick_bin_of(lowb) != (int)(u * (float)mkf::kPickBins);
+    ++n;
+  }
+  std::uniform_real_distribution<float> u01(0.0f, 1.0f);
+  std::vector<uint8_t> tab(mkf::kPickBins);
+  for (int it = 0; it < 200; ++it) {
+    const int K = 1 + (int)(rng() % 32);
+    std::vector<float> cum(K);
+    float tot = 0.0f;
+    for (int k = 0; k < K; ++k) { tot += (rng() % 5 == 0) ? 0.0f : u01(rng); cum[k] = tot; }
+    for (int k = 0; k < K; ++k) cum[k] /= tot > 0.0f ? tot : 1.0f;
+    mkf::build_pick_table(cum.data(), K, tab.data(), 0, 1);
+    for (int q = 0; q < 20000; ++q) {
+      const uint32_t lowb = (uint32_t)(rng() & 0xFFFFFFu);
+      uint32_t bits = 0x3F800000u | ((lowb << 8) >> 9);
+      float f;
+      std::memcpy(&f, &bits, 4);
+      const float u = f - 1.0f;
+      bad += mkf::pick_component_table_bin(tab.data(), cum.data(), K, u, mkf::pick_bin_of(lowb)) !=
+             mkf::pick_component(cum.data(), K, u);
+      ++n;
+    }
+  }
+  std::printf("pickbin %lld %lld\n", bad, n);
+}
+
 static void philox() {
   struct Kat { mkf::u32x4 ctr; uint32_t k0, k1; mkf::u32x4 out; };
   const Kat kats[] = {
@@ -314,5 +352,6 @@ int main() {
   quantize(rng);
   search(rng);
   pick(rng);
+  pickbin(rng);
   return 0;
 }

@@ -32,7 +32,7 @@ def results(tmp_path_factory):
 
 
 @pytest.mark.parametrize("piece,min_cases", [("thresholds", 400000), ("stride", 100000), ("quantize", 1000000), ("search", 400000),
-                                             ("pick", 6000000), ("philox", 3), ("philox_split", 1000000),
+                                             ("pick", 6000000), ("pickbin", 16777216), ("philox", 3), ("philox_split", 1000000),
                                              ("walk", 1000000)])
 def test_against_independent_restatement(results, piece, min_cases):
     bad, n = results[piece]
