@@ -37,14 +37,14 @@ BYTES_PER_PF = 112          # algorithmic bytes per particle-frame (state in/out
 # DRAM bytes per particle-frame of bpf_batched_kernel (autotuned shape: 256
 # threads x 3 CTAs/SM, float4 loads + search with ancestors in global memory):
 # dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture on 2048
-# tracks of the same workload (252.4 GB over 4.148e9 particle-frames), scaled
+# tracks of the same workload (261.5 GB over 4.148e9 particle-frames), scaled
 # to a full launch by particle-frames
-TRAFFIC_BYTES_PER_PF = 60.8
+TRAFFIC_BYTES_PER_PF = 63.0
 # warp instructions issued per particle-frame by the same kernel (smsp__inst_executed.sum
-# of the same capture: 1.0218e11 over 4.148e9 particle-frames); with the SM count, the
+# of the same capture: 1.0040e11 over 4.148e9 particle-frames); with the SM count, the
 # four schedulers of an SM and the sampled SM clock it gives the issue roofline, the
 # bound this kernel actually meets
-WARP_INST_PER_PF = 24.63
+WARP_INST_PER_PF = 24.20
 
 
 def load_peaks():
