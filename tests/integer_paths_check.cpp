@@ -20,7 +20,10 @@
 //    K in [1, 32], cumulative weights with zero-weight components, sums short of
 //    or past 1, cumulative values on bin edges, and every uniform u = m 2^-24 of
 //    a sample.  (The weights cover the picks that the random-mixture workloads
-//    and the shipped models make.)
+//    and the shipped models make.)  pickbin: the table bin that the particle
+//    draws take from their 24-bit value (pick_bin_of) against floor(u 1024) of
+//    the uniform passed beside it, for every 24-bit value, and the table pick
+//    with that bin against the count;
 //  - philox: philox4x32_10 (every draw of the kernels) against the Random123
 //    known-answer vectors; philox_split: the particle kernels' per-item form
 //    (philox_pre + philox_keys + philox_item) against the direct form;
