@@ -236,3 +236,50 @@ def test_batched_variant_flags_checked(cuda):
     runner.run(*runner.device_inputs())
     cuda.cuda.synchronize()
     assert runner.last_grid() == 1          # capped at the number of tracks
+
+
+@pytest.mark.parametrize("shape", [(256, 3, 11), (256, 0, 3)], ids=["lowsmem", "search"])
+def test_batched_tiny_tracks_parity(cuda, olib, shape):
+    """Tracks of 1, 2, 3, 31, 33 and 257 particles (a single particle, fewer
+    particles than a warp, one past a warp, one past a CTA) against the oracle,
+    teacher-forced, in one batch with a 4096-particle track (so that the small
+    tracks keep their ancestors in shared memory under the LOW layout)."""
+    from mkfbodytracker_pdaf_gb300 import synth
+    from mkfbodytracker_pdaf_gb300.filters import BatchedBootstrapPF
+    torch = cuda
+    Ns = [1, 2, 3, 31, 33, 257, 4096]
+    Ts = [6, 5, 4, 6, 3, 4, 2]
+    batch = synth.make_bpf_batch(53, Ns, Ts, [2.0, 0.0, 5.0, 8.0, 1.0, 3.0, 4.0],
+                                 [0.9, 0.95, 0.8, 0.7, 0.9, 0.85, 0.9])
+    tb, cps, var = shape
+    runner = BatchedBootstrapPF(batch, block_threads=tb, ctas_per_sm=cps, variant=var)
+    det_off, det = runner.device_inputs()
+    for dbg_track in range(len(Ns) - 1):
+        N = int(batch.tracks[dbg_track]["n_particles"])
+        T = int(batch.tracks[dbg_track]["n_frames"])
+        wd = torch.zeros((T, N), dtype=torch.float32, device="cuda")
+        ad = torch.zeros((T, N), dtype=torch.int32, device="cuda")
+        runner.set_debug(dbg_track, wd, ad)
+        est, ll, ess, st = runner.run(det_off, det)
+        torch.cuda.synchronize()
+        assert (st.cpu().numpy() & ~8 == 0).all()
+        g0 = int(batch.tracks[dbg_track]["frame_base"])
+        frames = [dict(est=est[g0 + f].double().cpu().numpy(), loglik=float(ll[g0 + f].item()),
+                       w=wd[f].cpu().numpy(), anc=ad[f].cpu().numpy()) for f in range(T)]
+        check_track(torch, olib, batch, dbg_track, frames)
+        if N == 1:
+            assert (ad.cpu().numpy() == 0).all()
+            assert np.allclose(ess[g0:g0 + T].cpu().numpy(), 1.0)
+
+
+@pytest.mark.parametrize("n", [1, 3, 33, 257])
+def test_plain_path_tiny_tracks_parity(cuda, olib, n):
+    """The per-track streaming kernels with a single particle, fewer than a
+    warp, one past a warp and one past a block, against the oracle."""
+    from mkfbodytracker_pdaf_gb300 import synth
+    torch = cuda
+    batch = synth.make_bpf_batch(60 + n, [n], [4], [3.0], [0.9])
+    frames, pf = _run_stream(torch, batch, 0, 4)
+    rep = check_track(torch, olib, batch, 0, frames)
+    assert rep.anc_frames == 4
+    assert pf.status() == 0
