@@ -188,7 +188,8 @@ int mkf_bpf_batch_set_tuning(mkf_bpf_batch_t h, int block_threads, int ctas_per_
  * search over shared prefix sums (12 bytes/particle of shared memory) instead
  * of the scatter walk (8 bytes/particle), MKF_BPF_PAIR = two particles per
  * loop iteration (implies the other two), MKF_BPF_LOWSMEM = the search with
- * 8 bytes/particle of shared memory (ancestors kept in global memory; needs
+ * 8 bytes/particle of shared memory (ancestors behind a track's prefix sums
+ * when 3 n_particles <= 2 x the batch's largest, else in global memory; needs
  * VEC_LOADS | SEARCH, not PAIR).  Results are identical. */
 enum { MKF_BPF_VEC_LOADS = 1, MKF_BPF_SEARCH = 2, MKF_BPF_PAIR = 4, MKF_BPF_LOWSMEM = 8 };
 int mkf_bpf_batch_set_variant(mkf_bpf_batch_t h, int flags);
