@@ -9,9 +9,10 @@
 // weights of pfPose.cpp:247-298.
 //
 // Launch shape: one CTA per track (static round-robin over a persistent grid,
-// so every reduction has a fixed order), one warp per mixture component.  A
-// warp's predict/update/reverse runs lane-parallel over matrix entries; the
-// collapse and its reverse are CTA-wide.  Each warp's forward scratch (its
+// so every reduction has a fixed order), one lane group per mixture component:
+// half a warp at d = 12, a whole warp at d = 24.  A group's
+// predict/update/reverse runs lane-parallel over matrix entries; the
+// collapse and its reverse are CTA-wide.  Each group's forward scratch (its
 // component state and the joint update being formed) is in shared memory; the
 // per-frame joint records of a backward segment are in the CTA's global slot
 // (sized to stay L2-resident); the per-component adjoint work blocks are in
@@ -108,37 +109,60 @@ struct MixArgs {
 
 __device__ __forceinline__ float wsum(float v) { return warp_sum(v); }
 
-// N warp sums at once (N = 2, 4 or 8), every lane getting all N totals.
-// Recursive halving: at each xor step a lane keeps half of its current values
-// and adds its partner's copy of that half, so the N sums need N - 1 + 5 - log2 N
-// exchanges instead of 5 N; lane (i << (5 - log2 N)) ends with total i, which is
-// then broadcast.  The order of the additions is fixed (deterministic).
-template <int N>
-__device__ __forceinline__ void wsum_multi(float (&v)[N], int lane) {
+// Lanes per mixture component: half a warp (two components per warp) when a
+// component's d-wide work fits in 16 lanes, else the whole warp.  The d-wide
+// phases, scalar steps and reductions of the per-component Kalman algebra then
+// cost half the warp instructions at d = 12.
+template <int D>
+__host__ __device__ constexpr int lpc_of() { return D <= 16 ? 16 : 32; }
+
+// The lanes of one component: LPC consecutive lanes of a warp
+template <int LPC>
+struct Grp {
+  int sub;         // lane within the group
+  unsigned mask;   // the group's lanes
+  __device__ __forceinline__ explicit Grp(int tid)
+      : sub(tid & (LPC - 1)), mask(LPC == 32 ? 0xffffffffu : (0xffffu << (tid & 16))) {}
+  __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+  __device__ __forceinline__ float bcast(float v, int src) const { return __shfl_sync(mask, v, src, LPC); }
+  __device__ __forceinline__ float sum(float v) const {
+#pragma unroll
+    for (int o = LPC / 2; o; o >>= 1) v += __shfl_xor_sync(mask, v, o, LPC);
+    return v;
+  }
+};
+
+// N group sums at once (N = 2, 4 or 8), every lane of the group getting all N
+// totals.  Recursive halving: at each xor step a lane keeps half of its current
+// values and adds its partner's copy of that half, so the N sums need N - 1 +
+// log2 LPC - log2 N exchanges instead of N log2 LPC; lane (i << (log2 LPC -
+// log2 N)) ends with total i, which is then broadcast.  The order of the
+// additions is fixed (deterministic).
+template <int N, int LPC>
+__device__ __forceinline__ void wsum_multi(float (&v)[N], const Grp<LPC>& g) {
   constexpr int LG = N == 2 ? 1 : N == 4 ? 2 : 3;
+  constexpr int LG5 = LPC == 32 ? 5 : 4;
   static_assert(N == 2 || N == 4 || N == 8, "wsum_multi: N must be 2, 4 or 8");
   float c[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) c[i] = v[i];
-  int n = N;
 #pragma unroll
-  for (int o = 16; o >= 1; o >>= 1) {
-    if (n > 1) {
-      const int h = n / 2;
-      const bool upper = (lane & o) != 0;
+  for (int k = 0; k < LG5; ++k) {
+    const int o = (LPC / 2) >> k, h = (N >> k) / 2;   // h values kept at this level (0: the last sums)
+    if (h >= 1) {
+      const bool upper = (g.sub & o) != 0;
 #pragma unroll
       for (int i = 0; i < h; ++i) {
         const float send = upper ? c[i] : c[i + h];
         const float keep = upper ? c[i + h] : c[i];
-        c[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        c[i] = keep + __shfl_xor_sync(g.mask, send, o, LPC);
       }
-      n = h;
     } else {
-      c[0] += __shfl_xor_sync(0xffffffffu, c[0], o);
+      c[0] += __shfl_xor_sync(g.mask, c[0], o, LPC);
     }
   }
 #pragma unroll
-  for (int i = 0; i < N; ++i) v[i] = __shfl_sync(0xffffffffu, c[0], i << (5 - LG));
+  for (int i = 0; i < N; ++i) v[i] = __shfl_sync(g.mask, c[0], i << (LG5 - LG), LPC);
 }
 
 // ---------------------------------------------------------------- forward pieces
@@ -149,8 +173,9 @@ __device__ __forceinline__ void wsum_multi(float (&v)[N], int lane) {
 // keeps this update for the reverse sweep
 template <int D>
 __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const float* Bj, const float* mj,
-                           int n, const float2* z, float pd, float kappa, float* Rg, int lane) {
-  constexpr int d = D;
+                           int n, const float2* z, float pd, float kappa, float* Rg, const Grp<lpc_of<D>()>& g) {
+  constexpr int d = D, LPC = lpc_of<D>();
+  const int lane = g.sub;
   float* H = R + R_H;
   float* U = R + rec_U(d);
   float* Kg = R + rec_Kg(d);
@@ -159,43 +184,43 @@ __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const 
   if (rec) {   // x and P are contiguous, and so are their record copies (d % 4 == 0)
     const float4* xP = reinterpret_cast<const float4*>(x);
     float4* RxP = reinterpret_cast<float4*>(Rg + rec_X(d));
-    for (int i = lane; i < (d + d * d) / 4; i += 32) RxP[i] = xP[i];
+    for (int i = lane; i < (d + d * d) / 4; i += LPC) RxP[i] = xP[i];
   }
   float pt = 0.0f;
   if (lane < 3) {
     pt = mj[lane];
     for (int c = 0; c < d; ++c) pt = fmaf(Bj[lane * d + c], x[c], pt);
   }
-  const float p0 = __shfl_sync(0xffffffffu, pt, 0), p1 = __shfl_sync(0xffffffffu, pt, 1),
-              p2 = __shfl_sync(0xffffffffu, pt, 2);
+  const float p0 = g.bcast(pt, 0), p1 = g.bcast(pt, 1),
+              p2 = g.bcast(pt, 2);
   if (!(p2 > kMixZMin)) {
     if (rec && lane == 0) Rg[R_VIS] = 0.0f;
-    __syncwarp();
+    g.sync();
     return logf(kappa);
   }
   const float iz = 1.0f / p2;
   const float zh0 = M.fx * p0 * iz + M.cx, zh1 = M.fy * p1 * iz + M.cy;
   const float J00 = M.fx * iz, J02 = -M.fx * p0 * iz * iz, J11 = M.fy * iz, J12 = -M.fy * p1 * iz * iz;
-  for (int i = lane; i < 2 * d; i += 32) {
+  for (int i = lane; i < 2 * d; i += LPC) {
     const int a = i / d, c = i - a * d;
     H[i] = (a == 0) ? fmaf(J00, Bj[c], J02 * Bj[2 * d + c]) : fmaf(J11, Bj[d + c], J12 * Bj[2 * d + c]);
   }
-  __syncwarp();
-  for (int i = lane; i < 2 * d; i += 32) {
+  g.sync();
+  for (int i = lane; i < 2 * d; i += LPC) {
     const int r = i >> 1, a = i & 1;
     float s = 0.0f;
     for (int c = 0; c < d; ++c) s = fmaf(P[r * d + c], H[a * d + c], s);
     U[i] = s;
   }
-  __syncwarp();
+  g.sync();
   float sv = 0.0f;
   if (lane < 4) {
     const int a = lane >> 1, b = lane & 1;
     for (int r = 0; r < d; ++r) sv = fmaf(H[a * d + r], U[r * 2 + b], sv);
     if (a == b) sv += M.sigma * M.sigma;
   }
-  const float S00 = __shfl_sync(0xffffffffu, sv, 0), S01 = __shfl_sync(0xffffffffu, sv, 1),
-              S10 = __shfl_sync(0xffffffffu, sv, 2), S11 = __shfl_sync(0xffffffffu, sv, 3);
+  const float S00 = g.bcast(sv, 0), S01 = g.bcast(sv, 1),
+              S10 = g.bcast(sv, 2), S11 = g.bcast(sv, 3);
   const float det = S00 * S11 - S01 * S10;
   const float Si00 = S11 / det, Si01 = -S01 / det, Si10 = -S10 / det, Si11 = S00 / det;
   const float ld = logf(det);
@@ -207,26 +232,26 @@ __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const 
     const float q = n0 * (Si00 * n0 + Si01 * n1) + n1 * (Si10 * n0 + Si11 * n1);
     e = c0 * expf(-0.5f * q - 0.5f * ld);
   }
-  const float ell = b + wsum(e);
+  const float ell = b + g.sum(e);
   const float beta = e / ell, beta0 = b / ell;
-  const float nb0 = wsum(beta * n0), nb1 = wsum(beta * n1);
-  const float C00 = wsum(beta * n0 * n0) - nb0 * nb0;
-  const float C01 = wsum(beta * n0 * n1) - nb0 * nb1;
-  const float C11 = wsum(beta * n1 * n1) - nb1 * nb1;
+  const float nb0 = g.sum(beta * n0), nb1 = g.sum(beta * n1);
+  const float C00 = g.sum(beta * n0 * n0) - nb0 * nb0;
+  const float C01 = g.sum(beta * n0 * n1) - nb0 * nb1;
+  const float C11 = g.sum(beta * n1 * n1) - nb1 * nb1;
   const float M00 = (1.0f - beta0) * S00 - C00, M01 = (1.0f - beta0) * S01 - C01;
   const float M10 = (1.0f - beta0) * S10 - C01, M11 = (1.0f - beta0) * S11 - C11;
-  for (int i = lane; i < 2 * d; i += 32) {
+  for (int i = lane; i < 2 * d; i += LPC) {
     const int r = i >> 1, a = i & 1;
     Kg[i] = U[r * 2] * (a ? Si01 : Si00) + U[r * 2 + 1] * (a ? Si11 : Si10);
   }
-  __syncwarp();
-  for (int i = lane; i < 2 * d; i += 32) {
+  g.sync();
+  for (int i = lane; i < 2 * d; i += LPC) {
     const int r = i >> 1, a = i & 1;
     W[i] = Kg[r * 2] * (a ? M01 : M00) + Kg[r * 2 + 1] * (a ? M11 : M10);
   }
-  __syncwarp();
+  g.sync();
   if (lane < d) x[lane] += Kg[lane * 2] * nb0 + Kg[lane * 2 + 1] * nb1;
-  for (int i = lane; i < d * d; i += 32) {
+  for (int i = lane; i < d * d; i += LPC) {
     const int r = i / d, c = i - r * d;
     P[i] -= W[r * 2] * Kg[c * 2] + W[r * 2 + 1] * Kg[c * 2 + 1];
   }
@@ -244,22 +269,23 @@ __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const 
     R[R_NU + 2 * lane] = n0; R[R_NU + 2 * lane + 1] = n1;
     R[R_E + lane] = e; R[R_BETA + lane] = beta;
   }
-  __syncwarp();
+  g.sync();
   if (rec) {
     const float4* R4 = reinterpret_cast<const float4*>(R);
     float4* G4 = reinterpret_cast<float4*>(Rg);
-    for (int i = lane; i < rec_X(d) / 4; i += 32) G4[i] = R4[i];
+    for (int i = lane; i < rec_X(d) / 4; i += LPC) G4[i] = R4[i];
   }
-  __syncwarp();
+  g.sync();
   return logf(ell);
 }
 
 // ---------------------------------------------------------------- reverse pieces
 template <int D>
 __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, float pd, float kappa, float* xb,
-                          float* Pb, float gl, float* tmp, float& sb, int lane) {
+                          float* Pb, float gl, float* tmp, float& sb, const Grp<lpc_of<D>()>& g) {
   if (R[R_VIS] == 0.0f) return;
-  constexpr int d = D;
+  constexpr int d = D, LPC = lpc_of<D>();
+  const int lane = g.sub;
   const int n = (int)R[R_N];
   const float* H = R + R_H;
   const float* U = R + rec_U(d);
@@ -279,10 +305,10 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
   // x' = x + Kg nb
   float t2[2] = {0.0f, 0.0f};
   if (lane < d) { t2[0] = Kg[lane * 2] * xb[lane]; t2[1] = Kg[lane * 2 + 1] * xb[lane]; }
-  wsum_multi<2>(t2, lane);
+  wsum_multi<2>(t2, g);
   float nbb0 = t2[0], nbb1 = t2[1];
   // P' = P - W Kg^T
-  for (int i = lane; i < 2 * d; i += 32) {
+  for (int i = lane; i < 2 * d; i += LPC) {
     const int r = i >> 1, a = i & 1;
     float s = 0.0f, t = 0.0f;
     for (int c = 0; c < d; ++c) {
@@ -292,7 +318,7 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
     Wb[i] = -s;
     Kgb[i] = xb[r] * (a ? nb1 : nb0) - t;
   }
-  __syncwarp();
+  g.sync();
   // W = Kg M: the M adjoint (partials), and the Kg adjoint's W term; the
   // S^-1 adjoint of Kg = U Si (partials, from the finished Kg adjoint) is
   // reduced together with the M adjoint
@@ -301,16 +327,16 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
     r8[0] = Kg[lane * 2] * Wb[lane * 2]; r8[1] = Kg[lane * 2] * Wb[lane * 2 + 1];
     r8[2] = Kg[lane * 2 + 1] * Wb[lane * 2]; r8[3] = Kg[lane * 2 + 1] * Wb[lane * 2 + 1];
   }
-  for (int i = lane; i < 2 * d; i += 32) {
+  for (int i = lane; i < 2 * d; i += LPC) {
     const int r = i >> 1, a = i & 1;
     Kgb[i] += Wb[r * 2] * Mm[a * 2] + Wb[r * 2 + 1] * Mm[a * 2 + 1];
   }
-  __syncwarp();
+  g.sync();
   if (lane < d) {
     r8[4] = U[lane * 2] * Kgb[lane * 2]; r8[5] = U[lane * 2] * Kgb[lane * 2 + 1];
     r8[6] = U[lane * 2 + 1] * Kgb[lane * 2]; r8[7] = U[lane * 2 + 1] * Kgb[lane * 2 + 1];
   }
-  wsum_multi<8>(r8, lane);
+  wsum_multi<8>(r8, g);
   const float Mb[4] = {r8[0], r8[1], r8[2], r8[3]};
   // M = (1 - beta0) S - Cn
   float Sb[4], Cnb[4];
@@ -326,9 +352,9 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
   }
   nbb0 -= Cs0 * nb0 + Cs1 * nb1;
   nbb1 -= Cs1 * nb0 + Cs3 * nb1;
-  __syncwarp();
+  g.sync();
   // Kg = U Si
-  for (int i = lane; i < 2 * d; i += 32) {
+  for (int i = lane; i < 2 * d; i += LPC) {
     const int r = i >> 1, a = i & 1;
     Ub[i] = Kgb[r * 2] * Si[a * 2] + Kgb[r * 2 + 1] * Si[a * 2 + 1];
   }
@@ -340,7 +366,7 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
     nub1 += be * nbb1;
   }
   // beta = e / ell, beta0 = b / ell, log ell
-  const float num = b0b * b + wsum(betab * ee);
+  const float num = b0b * b + g.sum(betab * ee);
   const float ellb = -num / (ell * ell) + gl / ell;
   float ldp = 0.0f, q00 = 0.0f, q01 = 0.0f, q11 = 0.0f;
   if (lane < n) {
@@ -352,7 +378,7 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
     q00 = qb * n0 * n0; q01 = qb * n0 * n1; q11 = qb * n1 * n1;
   }
   float r6[8] = {ldp, q00, q01, q11, nub0, nub1, 0.0f, 0.0f};
-  wsum_multi<8>(r6, lane);
+  wsum_multi<8>(r6, g);
   const float ldb = r6[0];
   Sib[0] += r6[1];
   Sib[1] += r6[2]; Sib[2] += r6[2];
@@ -368,29 +394,29 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
       for (int c = 0; c < 2; ++c) Sb[a * 2 + c] -= T1[a * 2] * Si[c * 2] + T1[a * 2 + 1] * Si[c * 2 + 1];
   }
   if (lane == 0) sb += 2.0f * M.sigma * (Sb[0] + Sb[3]);
-  __syncwarp();
+  g.sync();
   // S = H U + sigma^2 I
-  for (int i = lane; i < 2 * d; i += 32) {
+  for (int i = lane; i < 2 * d; i += LPC) {
     const int a = i / d, r = i - a * d;
     Hb[i] = Sb[a * 2] * U[r * 2] + Sb[a * 2 + 1] * U[r * 2 + 1];
   }
-  for (int i = lane; i < 2 * d; i += 32) {
+  for (int i = lane; i < 2 * d; i += LPC) {
     const int r = i >> 1, c = i & 1;
     Ub[i] += H[r] * Sb[c] + H[d + r] * Sb[2 + c];
   }
-  __syncwarp();
+  g.sync();
   // U = P H^T
-  for (int i = lane; i < d * d; i += 32) {
+  for (int i = lane; i < d * d; i += LPC) {
     const int r = i / d, c = i - r * d;
     Pb[i] += Ub[r * 2] * H[c] + Ub[r * 2 + 1] * H[d + c];
   }
-  for (int i = lane; i < 2 * d; i += 32) {
+  for (int i = lane; i < 2 * d; i += LPC) {
     const int a = i / d, c = i - a * d;
     float s = 0.0f;
     for (int r = 0; r < d; ++r) s = fmaf(Ub[r * 2 + a], Pin[r * d + c], s);
     Hb[i] += s;
   }
-  __syncwarp();
+  g.sync();
   // H = Jp Bj
   float jb = 0.0f;
   if (lane < 6) {
@@ -398,7 +424,7 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
     for (int c = 0; c < d; ++c) jb = fmaf(Hb[a * d + c], Bj[t * d + c], jb);
   }
   float Jb[6];
-  for (int q = 0; q < 6; ++q) Jb[q] = __shfl_sync(0xffffffffu, jb, q);
+  for (int q = 0; q < 6; ++q) Jb[q] = g.bcast(jb, q);
   const float iz = R[R_IZ], iz2 = iz * iz, iz3 = iz2 * iz;
   const float J00 = R[R_JP], J02 = R[R_JP + 2], J11 = R[R_JP + 4], J12 = R[R_JP + 5];
   const float p0 = R[R_P3], p1 = R[R_P3 + 1];
@@ -407,7 +433,7 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
   const float pb2 = J02 * zhb0 + J12 * zhb1 + Jb[0] * (-M.fx * iz2) + Jb[2] * (2.0f * M.fx * p0 * iz3) +
                     Jb[4] * (-M.fy * iz2) + Jb[5] * (2.0f * M.fy * p1 * iz3);
   if (lane < d) xb[lane] += Bj[lane] * pb0 + Bj[d + lane] * pb1 + Bj[2 * d + lane] * pb2;
-  __syncwarp();
+  g.sync();
 }
 
 // ---------------------------------------------------------------- CTA-wide frame pieces
@@ -464,40 +490,44 @@ template <int D>
 __device__ float frame_forward(const MixArgs& A, float* scr, int SR, float* frg, const FrameLayout& FL,
                                const float* Bm, const float* mm, float pd, float kappa, Smem& s) {
   const MixDev& M = A.M;
-  constexpr int d = D;
+  constexpr int d = D, LPC = lpc_of<D>();
   const int K = M.K, J = M.J;
-  const int tid = threadIdx.x, TB = blockDim.x, lane = tid & 31, k = tid >> 5;
-  float* xk = scr + (size_t)k * SR;
-  float* Pk = xk + d;
-  float* R = Pk + d * d;
-  float* cg = frg ? frg + (size_t)k * FL.comp_size : nullptr;
-  const float* a = M.a + k * d;
-  const float* mu = M.mu + k * d;
-  if (lane < d) xk[lane] = fmaf(a[lane], s.xh[lane], (1.0f - a[lane]) * mu[lane]);
-  const float* Qk = M.Q + (size_t)k * d * d;
-  for (int i = lane; i < d * d; i += 32) {
-    const int r = i / d, c = i - r * d;
-    Pk[i] = fmaf(a[r] * a[c], s.Ph[i], Qk[i]);
+  const int tid = threadIdx.x, TB = blockDim.x, k = tid / LPC;
+  const Grp<LPC> g(tid);
+  const int lane = g.sub;
+  if (k < K) {
+    float* xk = scr + (size_t)k * SR;
+    float* Pk = xk + d;
+    float* R = Pk + d * d;
+    float* cg = frg ? frg + (size_t)k * FL.comp_size : nullptr;
+    const float* a = M.a + k * d;
+    const float* mu = M.mu + k * d;
+    if (lane < d) xk[lane] = fmaf(a[lane], s.xh[lane], (1.0f - a[lane]) * mu[lane]);
+    const float* Qk = M.Q + (size_t)k * d * d;
+    for (int i = lane; i < d * d; i += LPC) {
+      const int r = i / d, c = i - r * d;
+      Pk[i] = fmaf(a[r] * a[c], s.Ph[i], Qk[i]);
+    }
+    g.sync();
+    float ll = 0.0f;
+    for (int j = 0; j < J; ++j)
+      ll += joint_fwd<D>(M, R, xk, Pk, Bm + j * 3 * d, mm + j * 3, s.cnt[j], s.det + j * kMixMaxC, pd, kappa,
+                         cg ? cg + j * rec_size(d) : nullptr, g);
+    if (cg) {   // xk, Pk contiguous in the scratch and in the record (comp_Pk = comp_xk + d)
+      const float4* s4 = reinterpret_cast<const float4*>(xk);
+      float4* g4 = reinterpret_cast<float4*>(cg + FL.comp_xk);
+      for (int i = lane; i < (d + d * d) / 4; i += LPC) g4[i] = s4[i];
+    }
+    if (lane == 0) s.l[k] = M.logpi[k] + ll;
   }
-  __syncwarp();
-  float ll = 0.0f;
-  for (int j = 0; j < J; ++j)
-    ll += joint_fwd<D>(M, R, xk, Pk, Bm + j * 3 * d, mm + j * 3, s.cnt[j], s.det + j * kMixMaxC, pd, kappa,
-                       cg ? cg + j * rec_size(d) : nullptr, lane);
-  if (cg) {   // xk, Pk contiguous in the scratch and in the record (comp_Pk = comp_xk + d)
-    const float4* s4 = reinterpret_cast<const float4*>(xk);
-    float4* g4 = reinterpret_cast<float4*>(cg + FL.comp_xk);
-    for (int i = lane; i < (d + d * d) / 4; i += 32) g4[i] = s4[i];
-  }
-  if (lane == 0) s.l[k] = M.logpi[k] + ll;
   __syncthreads();
-  if (k == 0) {
-    const float v = lane < K ? s.l[lane] : -INFINITY;
+  if (tid < 32) {   // K <= 32: the softmax over components in the first warp
+    const float v = tid < K ? s.l[tid] : -INFINITY;
     const float mx = warp_max(v);
-    const float sum = warp_sum(lane < K ? expf(v - mx) : 0.0f);
+    const float sum = warp_sum(tid < K ? expf(v - mx) : 0.0f);
     const float c = mx + logf(sum);
-    if (lane < K) s.w[lane] = expf(v - c);
-    if (lane == 0) s.red[0] = c;
+    if (tid < K) s.w[tid] = expf(v - c);
+    if (tid == 0) s.red[0] = c;
   }
   __syncthreads();
   for (int r = tid; r < d; r += TB) {
@@ -576,8 +606,12 @@ size_t mix_smem_bytes(int d) {
 }
 
 // ---------------------------------------------------------------- forward kernel
+// Register caps: at d = 12 (half-warp groups, 256 threads for 15 components,
+// at most 512) 128 registers and two CTAs per SM, which measured faster than
+// 80 (three CTAs) or 64 (four, with spills in the backward); at d = 24 (whole
+// warps, up to 1024 threads) 64.
 template <int D>
-__global__ void __launch_bounds__(1024) mix_forward_kernel(MixArgs A) {
+__global__ void __maxnreg__(D <= 16 ? 128 : 64) mix_forward_kernel(MixArgs A) {
   extern __shared__ __align__(16) float msm[];
   Smem s;
   float* scr = carve(s, msm, D);                 // per-warp component scratch follows
@@ -621,14 +655,17 @@ __global__ void __launch_bounds__(1024) mix_forward_kernel(MixArgs A) {
 // cross-component sums and the per-segment flushes stay on chip; otherwise
 // both stay in the global slot.  Records always stay in the slot.
 template <int D, bool STAGE>
-__global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
+__global__ void __maxnreg__(D <= 16 ? 128 : 64) mix_backward_kernel(MixArgs A) {
   extern __shared__ __align__(16) float msm[];
   Smem s;
   float* scr = carve(s, msm, D);
   const MixDev& M = A.M;
-  constexpr int d = D, DD = D * (D + 1) / 2;
+  constexpr int d = D, DD = D * (D + 1) / 2, LPC = lpc_of<D>();
   const int J = M.J, K = M.K;
-  const int tid = threadIdx.x, TB = blockDim.x, lane = tid & 31, k = tid >> 5;
+  const int tid = threadIdx.x, TB = blockDim.x, k = tid / LPC;
+  const Grp<LPC> g(tid);
+  const int lane = g.sub;
+  const bool act = LPC == 32 || k < K;   // a group past the last component (K odd) only joins the barriers
   const FrameLayout FL = frame_layout(d, K, J);
   const WorkLayout WL = work_layout(d);
   const int SR = fwd_scratch_floats(d);
@@ -649,7 +686,8 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
   const float* Lk = M.Lq + k * DD;
   float sbl = 0.0f;                                         // sigma adjoint of this segment (lane 0)
   double sbd = 0.0;                                         // and its FP64 running sum
-  for (int i = lane; i < 2 * d + d * d; i += 32) wb[WL.gmu + i] = 0.0f;   // gmu, ga, Sq
+  if (act)
+    for (int i = lane; i < 2 * d + d * d; i += LPC) wb[WL.gmu + i] = 0.0f;   // gmu, ga, Sq
   // frame record fr's input state, mixture weights and collapsed mean
   // (stage_floats(d) contiguous floats from FL.xin) are copied into a staging
   // buffer with cp.async, and checkpoints (d + d^2 floats) into s.xh, s.Ph; the
@@ -721,54 +759,59 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
         const float* xo = wv + 32;
         const float* xk = cb + FL.comp_xk;
         const float* Pk = cb + FL.comp_Pk;
-        const float wk = wv[k];
+        const float wk = act ? wv[k] : 0.0f;
         // collapse reverse: P' = sym(sum w (P_k + D D^T)), x' = sum w x_k, softmax (dc = 1)
         float* Dkb = wb + WL.Dkb;
-        if (lane < d) {
+        if (act && lane < d) {
           float v = 0.0f;
           for (int c = 0; c < d; ++c) v = fmaf(s.Pcb[lane * d + c], xk[c] - xo[c], v);
           Dkb[lane] = 2.0f * wk * v;
         }
         __syncthreads();
-        // xt = Xb - sum_q Dkb_q: every warp forms its own copy (lane r), in the same order
-        float xt = 0.0f;
-        if (lane < d) {
-          float v = s.Xb[lane];
+        // xt = Xb - sum_q Dkb_q: every group forms its own copy (lane r), in the same order
+        float xt = 0.0f, wbk = 0.0f;
+        if (act) {
+          if (lane < d) {
+            float v = s.Xb[lane];
 #pragma unroll 4
-          for (int q = 0; q < K; ++q) v -= wbase[(size_t)q * WL.size + WL.Dkb + lane];
-          xt = v;
+            for (int q = 0; q < K; ++q) v -= wbase[(size_t)q * WL.size + WL.Dkb + lane];
+            xt = v;
+          }
+          float wbp = (lane < d) ? xk[lane] * xt : 0.0f;
+          for (int i = lane; i < d * d; i += LPC) {
+            const int r = i / d, c = i - r * d;
+            wbp = fmaf(s.Pcb[i], Pk[i] + (xk[r] - xo[r]) * (xk[c] - xo[c]), wbp);
+          }
+          wbk = g.sum(wbp);
+          if (lane == 0) s.wb[k] = wbk;
         }
-        float wbp = (lane < d) ? xk[lane] * xt : 0.0f;
-        for (int i = lane; i < d * d; i += 32) {
-          const int r = i / d, c = i - r * d;
-          wbp = fmaf(s.Pcb[i], Pk[i] + (xk[r] - xo[r]) * (xk[c] - xo[c]), wbp);
-        }
-        const float wbk = wsum(wbp);
-        if (lane == 0) s.wb[k] = wbk;
         __syncthreads();
-        // sum_q w_q wb_q, formed by every warp in the same order
-        const float swb = wsum(lane < K ? wv[lane] * s.wb[lane] : 0.0f);
+        // sum_q w_q wb_q, formed by every group in the same order
+        float swp = 0.0f;
+        for (int q = lane; q < K; q += LPC) swp = fmaf(wv[q], s.wb[q], swp);
+        const float swb = g.sum(swp);
         const float lb = wk * (wbk - swb) + wk;
         float* xb = wb + WL.xb;
         float* Pb = wb + WL.Pb;
         float* Xin = wb + WL.Xin;
         float* Pinb = wb + WL.Pin;
-        if (wk > 0.0f) {
+        if (!act) {
+        } else if (wk > 0.0f) {
           if (lane < d) xb[lane] = Dkb[lane] + wk * xt;
-          for (int i = lane; i < d * d; i += 32) Pb[i] = wk * s.Pcb[i];
-          __syncwarp();
+          for (int i = lane; i < d * d; i += LPC) Pb[i] = wk * s.Pcb[i];
+          g.sync();
           // each joint's record is copied (coalesced, 16 bytes per lane and step)
-          // into this warp's forward scratch, idle during the reverse sweep, so
+          // into this group's forward scratch, idle during the reverse sweep, so
           // that the reverse reads it from shared memory instead of L2
           float* Rs = scr + (size_t)k * SR;
           const int RS4 = rec_size(d) / 4;
           for (int j = J - 1; j >= 0; --j) {
             const float4* src = reinterpret_cast<const float4*>(cb + j * rec_size(d));
             float4* dst = reinterpret_cast<float4*>(Rs);
-            for (int q = lane; q < RS4; q += 32) dst[q] = src[q];
-            __syncwarp();
-            joint_bwd<D>(M, Rs, Bm + j * 3 * d, pd, kappa, xb, Pb, lb, wb + WL.tmp, sbl, lane);
-            __syncwarp();
+            for (int q = lane; q < RS4; q += LPC) dst[q] = src[q];
+            g.sync();
+            joint_bwd<D>(M, Rs, Bm + j * 3 * d, pd, kappa, xb, Pb, lb, wb + WL.tmp, sbl, g);
+            g.sync();
           }
           // predict reverse: x = a*xin + (1-a)*mu ; P = A Pin A + Q (Q = L L^T: its
           // adjoint Pb is summed here and turned into the L adjoint once a segment)
@@ -783,14 +826,14 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
               g += (Pb[lane * d + c] * Pin[lane * d + c] + Pb[c * d + lane] * Pin[c * d + lane]) * a[c];
             ga[lane] += g;
           }
-          for (int i = lane; i < d * d; i += 32) {
+          for (int i = lane; i < d * d; i += LPC) {
             const int r = i / d, c = i - r * d;
             Pinb[i] = a[r] * a[c] * Pb[i];
             Sq[i] += Pb[i];
           }
         } else {
           if (lane < d) Xin[lane] = 0.0f;
-          for (int i = lane; i < d * d; i += 32) Pinb[i] = 0.0f;
+          for (int i = lane; i < d * d; i += LPC) Pinb[i] = 0.0f;
         }
         __syncthreads();
         for (int r = tid; r < d; r += TB) {
@@ -817,13 +860,13 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
       }
       // flush this segment's FP32 parameter adjoints into the CTA's FP64
       // accumulators; the L_Q adjoint is tril((Sq + Sq^T) L_Q)
-      for (int i = lane; i < d; i += 32) {
-        gacc[k * d + i] += (double)wb[WL.gmu + i];
-        gacc[K * d + k * d + i] += (double)wb[WL.ga + i];
-      }
-      {
+      if (act) {
+        for (int i = lane; i < d; i += LPC) {
+          gacc[k * d + i] += (double)wb[WL.gmu + i];
+          gacc[K * d + k * d + i] += (double)wb[WL.ga + i];
+        }
         const float* Sq = wb + WL.Sq;
-        for (int i = lane; i < DD; i += 32) {
+        for (int i = lane; i < DD; i += LPC) {
           int r = (int)((sqrtf(8.0f * i + 1.0f) - 1.0f) * 0.5f);
           while (r * (r + 1) / 2 > i) --r;
           while ((r + 1) * (r + 2) / 2 <= i) ++r;
@@ -832,11 +875,11 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
           for (int t2 = c; t2 < d; ++t2) g = fmaf(Sq[r * d + t2] + Sq[t2 * d + r], Lk[t2 * (t2 + 1) / 2 + c], g);
           gacc[2 * K * d + k * DD + i] += (double)g;
         }
+        sbd += (double)sbl;
+        sbl = 0.0f;
+        g.sync();
+        for (int i = lane; i < 2 * d + d * d; i += LPC) wb[WL.gmu + i] = 0.0f;
       }
-      sbd += (double)sbl;
-      sbl = 0.0f;
-      __syncwarp();
-      for (int i = lane; i < 2 * d + d * d; i += 32) wb[WL.gmu + i] = 0.0f;
       __syncthreads();
     }
     // prior: x = sum pi mu, P = sum pi (S0 + D D^T)
@@ -846,7 +889,7 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
       s.xh[r] = v;
     }
     __syncthreads();
-    if (lane < d) {
+    if (act && lane < d) {
       float v = 0.0f;
       for (int c = 0; c < d; ++c) v = fmaf(s.Pb[lane * d + c] + s.Pb[c * d + lane], mu[c] - s.xh[c], v);
       wb[WL.Dkb + lane] = M.pi[k] * v;
@@ -858,11 +901,11 @@ __global__ void __launch_bounds__(1024) mix_backward_kernel(MixArgs A) {
       s.xt[r] = v;
     }
     __syncthreads();
-    if (lane < d) gacc[k * d + lane] += (double)(wb[WL.Dkb + lane] + M.pi[k] * s.xt[lane]);
+    if (act && lane < d) gacc[k * d + lane] += (double)(wb[WL.Dkb + lane] + M.pi[k] * s.xt[lane]);
     __syncthreads();
   }
-  // sigma: per-warp lane 0 partials, fixed-order sum
-  if (lane == 0) s.dred[k] = sbd;
+  // sigma: per-group lane 0 partials, fixed-order sum
+  if (act && lane == 0) s.dred[k] = sbd;
   __syncthreads();
   if (tid == 0) {
     double v = 0.0;
@@ -1054,7 +1097,7 @@ extern "C" int mkf_mixkf_create(const mkf_mix_model* model, int n_tracks, const 
   h->d = d; h->K = K; h->J = J; h->DD = DD; h->n_tracks = n_tracks; h->G = n_frames_total;
   h->maxT = maxT;
   h->ng = 2 * K * d + K * DD + 1;
-  h->tpb = 32 * K;
+  h->tpb = (K * (d <= 16 ? 16 : 32) + 31) / 32 * 32;   // lpc_of<D>() lanes per component, whole warps
   h->fx = model->fx; h->fy = model->fy; h->cx = model->cx; h->cy = model->cy;
   h->h_nf = static_cast<int*>(malloc(sizeof(int) * n_tracks));
   if (!h->h_nf) { delete h; return MKF_ERR_NOMEM; }
