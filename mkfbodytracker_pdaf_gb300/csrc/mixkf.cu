@@ -437,7 +437,7 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
 }
 
 // ---------------------------------------------------------------- CTA-wide frame pieces
-constexpr int kDetBlock = 32;     // frames of detection lists prefetched at once
+constexpr int kDetBlock = 16;     // frames of detection lists prefetched at once
 
 struct Smem {
   float *xh, *Ph, *xo, *Po, *Xb, *Pb, *Pcb, *xt;
@@ -606,12 +606,12 @@ size_t mix_smem_bytes(int d) {
 }
 
 // ---------------------------------------------------------------- forward kernel
-// Register caps: at d = 12 (half-warp groups, 256 threads for 15 components,
-// at most 512) 128 registers and two CTAs per SM, which measured faster than
-// 80 (three CTAs) or 64 (four, with spills in the backward); at d = 24 (whole
-// warps, up to 1024 threads) 64.
-template <int D>
-__global__ void __maxnreg__(D <= 16 ? 128 : 64) mix_forward_kernel(MixArgs A) {
+// REGS, the register cap of both kernels: at d = 24 (whole warps, up to 1024
+// threads) 64; at d = 12 (half-warp groups, 256 threads for 15 components)
+// 128 when every track has its own CTA at two CTAs per SM (faster per CTA),
+// else 80, so that three CTAs share an SM (mix_grid chooses).
+template <int D, int REGS>
+__global__ void __maxnreg__(REGS) mix_forward_kernel(MixArgs A) {
   extern __shared__ __align__(16) float msm[];
   Smem s;
   float* scr = carve(s, msm, D);                 // per-warp component scratch follows
@@ -650,12 +650,13 @@ __global__ void __maxnreg__(D <= 16 ? 128 : 64) mix_forward_kernel(MixArgs A) {
 // ---------------------------------------------------------------- backward kernel
 // Per segment of C frames: recompute the frames from the segment's checkpoint
 // keeping every frame's records (one forward), then reverse them.
-// STAGE: the per-component adjoint work blocks and the FP64 parameter
-// adjoints live in shared memory (used when they fit), so the fixed-order
-// cross-component sums and the per-segment flushes stay on chip; otherwise
-// both stay in the global slot.  Records always stay in the slot.
-template <int D, bool STAGE>
-__global__ void __maxnreg__(D <= 16 ? 128 : 64) mix_backward_kernel(MixArgs A) {
+// STAGE: the per-component adjoint work blocks live in shared memory (used
+// when they fit), so the fixed-order cross-component sums stay on chip;
+// otherwise they stay in the global slot.  Records always stay in the slot,
+// and the FP64 parameter adjoints (flushed once a segment) in the CTA's
+// accumulator row.
+template <int D, bool STAGE, int REGS>
+__global__ void __maxnreg__(REGS) mix_backward_kernel(MixArgs A) {
   extern __shared__ __align__(16) float msm[];
   Smem s;
   float* scr = carve(s, msm, D);
@@ -671,13 +672,8 @@ __global__ void __maxnreg__(D <= 16 ? 128 : 64) mix_backward_kernel(MixArgs A) {
   const int SR = fwd_scratch_floats(d);
   float* slot = A.slots + (size_t)blockIdx.x * A.slot_floats;
   float* frames = slot + (size_t)K * WL.size;               // C frame records
-  // FP64 parameter adjoints (mu, a, Lq, sigma): STAGE: in shared memory
-  // behind the work blocks (copied to the CTA's global slot at the end), else
-  // the global slot itself
-  double* const gslot = A.gacc + (size_t)blockIdx.x * A.ng;
-  double* const gacc = STAGE ? reinterpret_cast<double*>(scr + (size_t)K * (SR + WL.size)) : gslot;
-  if (STAGE)
-    for (int i = tid; i < A.ng; i += TB) gacc[i] = 0.0;
+  // FP64 parameter adjoints (mu, a, Lq, sigma): the CTA's row, zeroed by the host
+  double* const gacc = A.gacc + (size_t)blockIdx.x * A.ng;
   float* wb = STAGE ? scr + (size_t)K * SR + (size_t)k * WL.size     // this component's work block
                     : slot + (size_t)k * WL.size;
   float* const wbase = STAGE ? scr + (size_t)K * SR : slot;
@@ -912,10 +908,6 @@ __global__ void __maxnreg__(D <= 16 ? 128 : 64) mix_backward_kernel(MixArgs A) {
     for (int q = 0; q < K; ++q) v += s.dred[q];
     gacc[A.ng - 1] += v;
   }
-  if (STAGE) {
-    __syncthreads();
-    for (int i = tid; i < A.ng; i += TB) gslot[i] = gacc[i];
-  }
 }
 
 // fixed-order reduction of the per-CTA FP64 accumulators
@@ -972,12 +964,15 @@ __global__ void adam_kernel(double* th, const double* g, double* m, double* v, c
   }
 }
 
+using MixKernel = void (*)(MixArgs);
+
 }  // namespace mkf
 
 using namespace mkf;
 
 struct mkf_mixkf {
-  int d, K, J, DD, n_tracks, C, ng, grid, tpb;
+  int d, K, J, DD, n_tracks, C, ng, grid, grid_f, tpb;
+  MixKernel fwd_kernel, bwd_kernel;   // chosen instantiations (register caps, STAGE)
   long long G;
   float *mu, *a, *Lq, *Q, *logpi, *pi, *S0, *sigma_d;
   float sigma_h;
@@ -1034,8 +1029,7 @@ static int mix_auto_stride(mkf_mixkf* h) {
   return std::min(c_sqrt, c_fit);
 }
 
-template <typename KF>
-static int mix_occ(KF kern, int tpb, size_t smem, int* occ) {
+static int mix_occ(MixKernel kern, int tpb, size_t smem, int* occ) {
   MKF_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   MKF_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern, tpb, smem));
   return MKF_OK;
@@ -1050,27 +1044,39 @@ static int mix_grid(mkf_mixkf* h) {
   const size_t base = mix_smem_bytes(d);
   const int SRf = fwd_scratch_floats(d);
   h->smem_f = base + sizeof(float) * (size_t)K * SRf;
-  // STAGE: the work blocks and the FP64 parameter adjoints in shared memory
-  const size_t smem_stage = base + sizeof(float) * (size_t)K * (SRf + WL.size) + sizeof(double) * (size_t)h->ng;
+  // STAGE: the work blocks in shared memory
+  const size_t smem_stage = base + sizeof(float) * (size_t)K * (SRf + WL.size);
   int dev = 0, optin = 0;
   MKF_CUDA(cudaGetDevice(&dev));
   MKF_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   h->stage = smem_stage <= (size_t)optin;
   h->smem_b = h->stage ? smem_stage : h->smem_f;
   if (h->smem_f > (size_t)optin) { set_error("mkf_mixkf: model too large for shared memory"); return MKF_ERR_ARG; }
-  int of = 0, ob = 0, st;
+  // per kernel two register caps at d = 12: the higher one when its resident
+  // CTAs already give every track its own CTA, else the lower one for one
+  // more CTA per SM; one cap (64) at d = 24
+  MixKernel f_hi, f_lo, b_hi, b_lo;
   if (d == 12) {
-    if ((st = mix_occ(mix_forward_kernel<12>, h->tpb, h->smem_f, &of))) return st;
-    st = h->stage ? mix_occ(mix_backward_kernel<12, true>, h->tpb, h->smem_b, &ob)
-                  : mix_occ(mix_backward_kernel<12, false>, h->tpb, h->smem_b, &ob);
+    f_hi = mix_forward_kernel<12, 128>;
+    f_lo = mix_forward_kernel<12, 80>;
+    b_hi = h->stage ? mix_backward_kernel<12, true, 128> : mix_backward_kernel<12, false, 128>;
+    b_lo = h->stage ? mix_backward_kernel<12, true, 80> : mix_backward_kernel<12, false, 80>;
   } else {
-    if ((st = mix_occ(mix_forward_kernel<24>, h->tpb, h->smem_f, &of))) return st;
-    st = h->stage ? mix_occ(mix_backward_kernel<24, true>, h->tpb, h->smem_b, &ob)
-                  : mix_occ(mix_backward_kernel<24, false>, h->tpb, h->smem_b, &ob);
+    f_hi = f_lo = mix_forward_kernel<24, 64>;
+    b_hi = b_lo = h->stage ? mix_backward_kernel<24, true, 64> : mix_backward_kernel<24, false, 64>;
   }
-  if (st) return st;
-  const int occ = std::max(1, std::min(of, ob));
-  h->grid = std::min(h->n_tracks, num_sms() * occ);
+  int of_hi = 0, of_lo = 0, ob_hi = 0, ob_lo = 0, st;
+  if ((st = mix_occ(f_hi, h->tpb, h->smem_f, &of_hi)) || (st = mix_occ(f_lo, h->tpb, h->smem_f, &of_lo)) ||
+      (st = mix_occ(b_hi, h->tpb, h->smem_b, &ob_hi)) || (st = mix_occ(b_lo, h->tpb, h->smem_b, &ob_lo)))
+    return st;
+  const int sms = num_sms();
+  const bool fh = h->n_tracks <= sms * of_hi || of_hi >= of_lo;
+  const bool bh = h->n_tracks <= sms * ob_hi || ob_hi >= ob_lo;
+  h->fwd_kernel = fh ? f_hi : f_lo;
+  h->bwd_kernel = bh ? b_hi : b_lo;
+  // each kernel its own persistent grid (the forward keeps no per-CTA slot)
+  h->grid_f = std::min(h->n_tracks, sms * std::max(1, fh ? of_hi : of_lo));
+  h->grid = std::min(h->n_tracks, sms * std::max(1, bh ? ob_hi : ob_lo));
   return MKF_OK;
 }
 
@@ -1202,8 +1208,7 @@ extern "C" int mkf_mixkf_forward(mkf_mixkf_t h, const int* d_det_off, const floa
   if (!h->have_theta) { set_error("mkf_mixkf_forward: set theta first"); return MKF_ERR_STATE; }
   cudaStream_t s = (cudaStream_t)stream;
   MixArgs A = mix_args(h, d_det_off, d_det);
-  if (h->d == 12) mix_forward_kernel<12><<<h->grid, h->tpb, h->smem_f, s>>>(A);
-  else mix_forward_kernel<24><<<h->grid, h->tpb, h->smem_f, s>>>(A);
+  h->fwd_kernel<<<h->grid_f, h->tpb, h->smem_f, s>>>(A);
   MKF_CHECK_LAUNCH("mkf_mixkf_forward");
   h->fwd_C = h->C;
   if (d_loglik) MKF_CUDA(cudaMemcpyAsync(d_loglik, h->ll, sizeof(double) * h->n_tracks, cudaMemcpyDeviceToDevice, s));
@@ -1224,13 +1229,7 @@ extern "C" int mkf_mixkf_backward(mkf_mixkf_t h, const int* d_det_off, const flo
   cudaStream_t s = (cudaStream_t)stream;
   MixArgs A = mix_args(h, d_det_off, d_det);
   MKF_CUDA(cudaMemsetAsync(h->gacc, 0, sizeof(double) * (size_t)h->ng * h->grid, s));
-  if (h->d == 12) {
-    if (h->stage) mix_backward_kernel<12, true><<<h->grid, h->tpb, h->smem_b, s>>>(A);
-    else mix_backward_kernel<12, false><<<h->grid, h->tpb, h->smem_b, s>>>(A);
-  } else {
-    if (h->stage) mix_backward_kernel<24, true><<<h->grid, h->tpb, h->smem_b, s>>>(A);
-    else mix_backward_kernel<24, false><<<h->grid, h->tpb, h->smem_b, s>>>(A);
-  }
+  h->bwd_kernel<<<h->grid, h->tpb, h->smem_b, s>>>(A);
   MKF_CHECK_LAUNCH("mkf_mixkf_backward");
   mix_reduce_kernel<<<(h->ng + 255) / 256, 256, 0, s>>>(h->gacc, h->grid, h->ng, d_grad);
   MKF_CHECK_LAUNCH("mkf_mixkf_backward: reduce");
