@@ -329,7 +329,7 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
   }
   for (int i = lane; i < 2 * d; i += LPC) {
     const int r = i >> 1, a = i & 1;
-    Kgb[i] += Wb[r * 2] * Mm[a * 2] + Wb[r * 2 + 1] * Mm[a * 2 + 1];
+    Kgb[i] += Wb[r * 2] * (a ? Mm[2] : Mm[0]) + Wb[r * 2 + 1] * (a ? Mm[3] : Mm[1]);
   }
   g.sync();
   if (lane < d) {
@@ -356,7 +356,7 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
   // Kg = U Si
   for (int i = lane; i < 2 * d; i += LPC) {
     const int r = i >> 1, a = i & 1;
-    Ub[i] = Kgb[r * 2] * Si[a * 2] + Kgb[r * 2 + 1] * Si[a * 2 + 1];
+    Ub[i] = Kgb[r * 2] * (a ? Si[2] : Si[0]) + Kgb[r * 2 + 1] * (a ? Si[3] : Si[1]);
   }
   float Sib[4] = {r8[4], r8[5], r8[6], r8[7]};
   // nb = sum beta nu
@@ -398,11 +398,11 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
   // S = H U + sigma^2 I
   for (int i = lane; i < 2 * d; i += LPC) {
     const int a = i / d, r = i - a * d;
-    Hb[i] = Sb[a * 2] * U[r * 2] + Sb[a * 2 + 1] * U[r * 2 + 1];
+    Hb[i] = (a ? Sb[2] : Sb[0]) * U[r * 2] + (a ? Sb[3] : Sb[1]) * U[r * 2 + 1];
   }
   for (int i = lane; i < 2 * d; i += LPC) {
     const int r = i >> 1, c = i & 1;
-    Ub[i] += H[r] * Sb[c] + H[d + r] * Sb[2 + c];
+    Ub[i] += H[r] * (c ? Sb[1] : Sb[0]) + H[d + r] * (c ? Sb[3] : Sb[2]);
   }
   g.sync();
   // U = P H^T
@@ -802,9 +802,12 @@ __global__ void __maxnreg__(REGS) mix_backward_kernel(MixArgs A) {
           float* Rs = scr + (size_t)k * SR;
           const int RS4 = rec_size(d) / 4;
           for (int j = J - 1; j >= 0; --j) {
-            const float4* src = reinterpret_cast<const float4*>(cb + j * rec_size(d));
-            float4* dst = reinterpret_cast<float4*>(Rs);
-            for (int q = lane; q < RS4; q += LPC) dst[q] = src[q];
+            // cp.async: all of a lane's 16-byte pieces in flight at once
+            // (plain copies through registers wait out each load before its store)
+            const float* src = cb + j * rec_size(d);
+            for (int q = lane; q < RS4; q += LPC) cp_async16(Rs + 4 * q, src + 4 * q);
+            cp_async_commit();
+            cp_async_wait_all();
             g.sync();
             joint_bwd<D>(M, Rs, Bm + j * 3 * d, pd, kappa, xb, Pb, lb, wb + WL.tmp, sbl, g);
             g.sync();
@@ -856,20 +859,41 @@ __global__ void __maxnreg__(REGS) mix_backward_kernel(MixArgs A) {
       }
       // flush this segment's FP32 parameter adjoints into the CTA's FP64
       // accumulators; the L_Q adjoint is tril((Sq + Sq^T) L_Q)
+      // (d <= LPC; every group of read-modify-writes loads its accumulators
+      // before it stores any, so their L2 round trips overlap)
       if (act) {
-        for (int i = lane; i < d; i += LPC) {
-          gacc[k * d + i] += (double)wb[WL.gmu + i];
-          gacc[K * d + k * d + i] += (double)wb[WL.ga + i];
+        if (lane < d) {
+          const float vm = wb[WL.gmu + lane], va = wb[WL.ga + lane];
+          double* const pm = gacc + k * d + lane;
+          double* const pa = gacc + K * d + k * d + lane;
+          const double om = *pm, oa = *pa;
+          *pm = om + (double)vm;
+          *pa = oa + (double)va;
         }
         const float* Sq = wb + WL.Sq;
-        for (int i = lane; i < DD; i += LPC) {
-          int r = (int)((sqrtf(8.0f * i + 1.0f) - 1.0f) * 0.5f);
-          while (r * (r + 1) / 2 > i) --r;
-          while ((r + 1) * (r + 2) / 2 <= i) ++r;
-          const int c = i - r * (r + 1) / 2;
-          float g = 0.0f;
-          for (int t2 = c; t2 < d; ++t2) g = fmaf(Sq[r * d + t2] + Sq[t2 * d + r], Lk[t2 * (t2 + 1) / 2 + c], g);
-          gacc[2 * K * d + k * DD + i] += (double)g;
+        double* const gl = gacc + 2 * K * d + k * DD;
+        constexpr int NCH = 2;
+        for (int i0 = lane; i0 < DD; i0 += NCH * LPC) {
+          float gv[NCH];
+#pragma unroll
+          for (int u = 0; u < NCH; ++u) {
+            const int i = i0 + u * LPC;
+            float gs = 0.0f;
+            if (i < DD) {
+              int r = (int)((sqrtf(8.0f * i + 1.0f) - 1.0f) * 0.5f);
+              while (r * (r + 1) / 2 > i) --r;
+              while ((r + 1) * (r + 2) / 2 <= i) ++r;
+              const int c = i - r * (r + 1) / 2;
+              for (int t2 = c; t2 < d; ++t2) gs = fmaf(Sq[r * d + t2] + Sq[t2 * d + r], Lk[t2 * (t2 + 1) / 2 + c], gs);
+            }
+            gv[u] = gs;
+          }
+          double ov[NCH];
+#pragma unroll
+          for (int u = 0; u < NCH; ++u) ov[u] = (i0 + u * LPC < DD) ? gl[i0 + u * LPC] : 0.0;
+#pragma unroll
+          for (int u = 0; u < NCH; ++u)
+            if (i0 + u * LPC < DD) gl[i0 + u * LPC] = ov[u] + (double)gv[u];
         }
         sbd += (double)sbl;
         sbl = 0.0f;
