@@ -166,6 +166,24 @@ __device__ __forceinline__ void wsum_multi(float (&v)[N], const Grp<LPC>& g) {
 }
 
 // ---------------------------------------------------------------- forward pieces
+// copy N4 16-byte pieces from shared to global memory, a lane's pieces loaded
+// two at a time before they are stored (through generic pointers each load
+// would otherwise wait for the store before it)
+template <int N4, int LPC>
+__device__ __forceinline__ void copy_s2g(float4* dst, const float4* src, int lane) {
+  constexpr int NIT = (N4 + LPC - 1) / LPC;
+#pragma unroll
+  for (int u0 = 0; u0 < NIT; u0 += 2) {
+    float4 v[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+      if (u0 + u < NIT && lane + (u0 + u) * LPC < N4) v[u] = src[lane + (u0 + u) * LPC];
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+      if (u0 + u < NIT && lane + (u0 + u) * LPC < N4) dst[lane + (u0 + u) * LPC] = v[u];
+  }
+}
+
 // sequential PDAF/EKF update of one joint for one component (whole warp)
 // R: this warp's scratch record (shared memory, R_H + 8d floats, 16-byte
 // aligned); x, P: the component state (shared memory, updated in place, P = x + d,
@@ -182,9 +200,8 @@ __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const 
   float* W = R + rec_W(d);
   const bool rec = Rg != nullptr;
   if (rec) {   // x and P are contiguous, and so are their record copies (d % 4 == 0)
-    const float4* xP = reinterpret_cast<const float4*>(x);
-    float4* RxP = reinterpret_cast<float4*>(Rg + rec_X(d));
-    for (int i = lane; i < (d + d * d) / 4; i += LPC) RxP[i] = xP[i];
+    copy_s2g<(D + D * D) / 4, LPC>(reinterpret_cast<float4*>(Rg + rec_X(d)), reinterpret_cast<const float4*>(x),
+                                   lane);
   }
   float pt = 0.0f;
   if (lane < 3) {
@@ -203,7 +220,8 @@ __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const 
   const float J00 = M.fx * iz, J02 = -M.fx * p0 * iz * iz, J11 = M.fy * iz, J12 = -M.fy * p1 * iz * iz;
   for (int i = lane; i < 2 * d; i += LPC) {
     const int a = i / d, c = i - a * d;
-    H[i] = (a == 0) ? fmaf(J00, Bj[c], J02 * Bj[2 * d + c]) : fmaf(J11, Bj[d + c], J12 * Bj[2 * d + c]);
+    H[i] = (a == 0) ? fmaf(J00, __ldg(Bj + c), J02 * __ldg(Bj + 2 * d + c))
+                    : fmaf(J11, __ldg(Bj + d + c), J12 * __ldg(Bj + 2 * d + c));
   }
   g.sync();
   for (int i = lane; i < 2 * d; i += LPC) {
@@ -271,9 +289,7 @@ __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const 
   }
   g.sync();
   if (rec) {
-    const float4* R4 = reinterpret_cast<const float4*>(R);
-    float4* G4 = reinterpret_cast<float4*>(Rg);
-    for (int i = lane; i < rec_X(d) / 4; i += LPC) G4[i] = R4[i];
+    copy_s2g<(R_H + 8 * D) / 4, LPC>(reinterpret_cast<float4*>(Rg), reinterpret_cast<const float4*>(R), lane);
   }
   g.sync();
   return logf(ell);
@@ -502,11 +518,13 @@ __device__ float frame_forward(const MixArgs& A, float* scr, int SR, float* frg,
     float* cg = frg ? frg + (size_t)k * FL.comp_size : nullptr;
     const float* a = M.a + k * d;
     const float* mu = M.mu + k * d;
-    if (lane < d) xk[lane] = fmaf(a[lane], s.xh[lane], (1.0f - a[lane]) * mu[lane]);
+    // the model is read-only in the kernel: __ldg lets these loads move ahead
+    // of the shared stores (generic pointers that could otherwise alias)
+    if (lane < d) xk[lane] = fmaf(__ldg(a + lane), s.xh[lane], (1.0f - __ldg(a + lane)) * __ldg(mu + lane));
     const float* Qk = M.Q + (size_t)k * d * d;
     for (int i = lane; i < d * d; i += LPC) {
       const int r = i / d, c = i - r * d;
-      Pk[i] = fmaf(a[r] * a[c], s.Ph[i], Qk[i]);
+      Pk[i] = fmaf(__ldg(a + r) * __ldg(a + c), s.Ph[i], __ldg(Qk + i));
     }
     g.sync();
     float ll = 0.0f;
@@ -818,16 +836,17 @@ __global__ void __maxnreg__(REGS) mix_backward_kernel(MixArgs A) {
           float* ga = wb + WL.ga;
           float* Sq = wb + WL.Sq;
           if (lane < d) {
-            Xin[lane] = a[lane] * xb[lane];
-            gmu[lane] += (1.0f - a[lane]) * xb[lane];
-            float g = (xin[lane] - mu[lane]) * xb[lane];
+            const float al = __ldg(a + lane);
+            Xin[lane] = al * xb[lane];
+            gmu[lane] += (1.0f - al) * xb[lane];
+            float g = (xin[lane] - __ldg(mu + lane)) * xb[lane];
             for (int c = 0; c < d; ++c)
-              g += (Pb[lane * d + c] * Pin[lane * d + c] + Pb[c * d + lane] * Pin[c * d + lane]) * a[c];
+              g += (Pb[lane * d + c] * Pin[lane * d + c] + Pb[c * d + lane] * Pin[c * d + lane]) * __ldg(a + c);
             ga[lane] += g;
           }
           for (int i = lane; i < d * d; i += LPC) {
             const int r = i / d, c = i - r * d;
-            Pinb[i] = a[r] * a[c] * Pb[i];
+            Pinb[i] = __ldg(a + r) * __ldg(a + c) * Pb[i];
             Sq[i] += Pb[i];
           }
         } else {
