@@ -175,6 +175,15 @@ __device__ __forceinline__ void wsum_multi(float (&v)[N], const Grp<LPC>& g) {
 }
 
 // ---------------------------------------------------------------- forward pieces
+// 16-byte loads and stores of four consecutive floats (16-byte aligned: every
+// matrix row here starts at a multiple of d floats, d % 4 == 0).  The matrix
+// loops below give a lane one row (d <= LPC) and walk its columns four at a
+// time, each element with the same operations in the same order as an
+// element-per-lane loop, so the results are the same
+__device__ __forceinline__ float4 lds4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void sts4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+__device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+
 // copy N4 16-byte pieces from shared to global memory, a lane's pieces loaded
 // two at a time before they are stored (through generic pointers each load
 // would otherwise wait for the store before it)
@@ -215,7 +224,11 @@ __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const 
   float pt = 0.0f;
   if (lane < 3) {
     pt = mj[lane];
-    for (int c = 0; c < d; ++c) pt = fmaf(Bj[lane * d + c], x[c], pt);
+#pragma unroll
+    for (int c = 0; c < D; c += 4) {
+      const float4 bq = ldg4(Bj + lane * d + c), xq = lds4(x + c);
+      pt = fmaf(bq.x, xq.x, pt); pt = fmaf(bq.y, xq.y, pt); pt = fmaf(bq.z, xq.z, pt); pt = fmaf(bq.w, xq.w, pt);
+    }
   }
   const float p0 = g.bcast(pt, 0), p1 = g.bcast(pt, 1),
               p2 = g.bcast(pt, 2);
@@ -227,17 +240,21 @@ __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const 
   const float iz = 1.0f / p2;
   const float zh0 = M.fx * p0 * iz + M.cx, zh1 = M.fy * p1 * iz + M.cy;
   const float J00 = M.fx * iz, J02 = -M.fx * p0 * iz * iz, J11 = M.fy * iz, J12 = -M.fy * p1 * iz * iz;
-  for (int i = lane; i < 2 * d; i += LPC) {
-    const int a = i / d, c = i - a * d;
-    H[i] = (a == 0) ? fmaf(J00, __ldg(Bj + c), J02 * __ldg(Bj + 2 * d + c))
-                    : fmaf(J11, __ldg(Bj + d + c), J12 * __ldg(Bj + 2 * d + c));
+  if (lane < d) {   // H = Jp Bj: column lane of both rows
+    const float b2 = __ldg(Bj + 2 * d + lane);
+    H[lane] = fmaf(J00, __ldg(Bj + lane), J02 * b2);
+    H[d + lane] = fmaf(J11, __ldg(Bj + d + lane), J12 * b2);
   }
   g.sync();
-  for (int i = lane; i < 2 * d; i += LPC) {
-    const int r = i >> 1, a = i & 1;
-    float s = 0.0f;
-    for (int c = 0; c < d; ++c) s = fmaf(P[r * d + c], H[a * d + c], s);
-    U[i] = s;
+  if (lane < d) {   // U = P H^T, row lane
+    float s0 = 0.0f, s1 = 0.0f;
+#pragma unroll 1   // (fully unrolled it costs the 80-register backward spills)
+    for (int c = 0; c < D; c += 4) {
+      const float4 pq = lds4(P + lane * d + c), h0 = lds4(H + c), h1 = lds4(H + d + c);
+      s0 = fmaf(pq.x, h0.x, s0); s0 = fmaf(pq.y, h0.y, s0); s0 = fmaf(pq.z, h0.z, s0); s0 = fmaf(pq.w, h0.w, s0);
+      s1 = fmaf(pq.x, h1.x, s1); s1 = fmaf(pq.y, h1.y, s1); s1 = fmaf(pq.z, h1.z, s1); s1 = fmaf(pq.w, h1.w, s1);
+    }
+    *reinterpret_cast<float2*>(U + lane * 2) = make_float2(s0, s1);
   }
   g.sync();
   float sv = 0.0f;
@@ -277,10 +294,19 @@ __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const 
     W[i] = Kg[r * 2] * (a ? M01 : M00) + Kg[r * 2 + 1] * (a ? M11 : M10);
   }
   g.sync();
-  if (lane < d) x[lane] += Kg[lane * 2] * nb0 + Kg[lane * 2 + 1] * nb1;
-  for (int i = lane; i < d * d; i += LPC) {
-    const int r = i / d, c = i - r * d;
-    P[i] -= W[r * 2] * Kg[c * 2] + W[r * 2 + 1] * Kg[c * 2 + 1];
+  if (lane < d) {
+    x[lane] += Kg[lane * 2] * nb0 + Kg[lane * 2 + 1] * nb1;
+    const float w0 = W[lane * 2], w1 = W[lane * 2 + 1];   // P -= W Kg^T, row lane
+#pragma unroll
+    for (int c = 0; c < D; c += 4) {
+      float4 pq = lds4(P + lane * d + c);
+      const float4 k01 = lds4(Kg + 2 * c), k23 = lds4(Kg + 2 * c + 4);
+      pq.x -= w0 * k01.x + w1 * k01.y;
+      pq.y -= w0 * k01.z + w1 * k01.w;
+      pq.z -= w0 * k23.x + w1 * k23.y;
+      pq.w -= w0 * k23.z + w1 * k23.w;
+      sts4(P + lane * d + c, pq);
+    }
   }
   if (lane == 0) {
     R[R_VIS] = 1.0f; R[R_N] = (float)n;
@@ -333,15 +359,21 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
   wsum_multi<2>(t2, g);
   float nbb0 = t2[0], nbb1 = t2[1];
   // P' = P - W Kg^T
-  for (int i = lane; i < 2 * d; i += LPC) {
-    const int r = i >> 1, a = i & 1;
-    float s = 0.0f, t = 0.0f;
-    for (int c = 0; c < d; ++c) {
-      s = fmaf(Pb[r * d + c], Kg[c * 2 + a], s);
-      t = fmaf(Pb[c * d + r], W[c * 2 + a], t);
+  if (lane < d) {   // row lane of Pb against Kg, column lane against W
+    float s0 = 0.0f, s1 = 0.0f, t0 = 0.0f, t1 = 0.0f;
+#pragma unroll
+    for (int c = 0; c < D; c += 2) {
+      const float2 pr = *reinterpret_cast<const float2*>(Pb + lane * d + c);
+      const float4 kq = lds4(Kg + 2 * c), wq = lds4(W + 2 * c);
+      const float pc0 = Pb[c * d + lane], pc1 = Pb[(c + 1) * d + lane];
+      s0 = fmaf(pr.x, kq.x, s0); s1 = fmaf(pr.x, kq.y, s1);
+      t0 = fmaf(pc0, wq.x, t0); t1 = fmaf(pc0, wq.y, t1);
+      s0 = fmaf(pr.y, kq.z, s0); s1 = fmaf(pr.y, kq.w, s1);
+      t0 = fmaf(pc1, wq.z, t0); t1 = fmaf(pc1, wq.w, t1);
     }
-    Wb[i] = -s;
-    Kgb[i] = xb[r] * (a ? nb1 : nb0) - t;
+    *reinterpret_cast<float2*>(Wb + lane * 2) = make_float2(-s0, -s1);
+    const float xr = xb[lane];
+    *reinterpret_cast<float2*>(Kgb + lane * 2) = make_float2(xr * nb0 - t0, xr * nb1 - t1);
   }
   g.sync();
   // W = Kg M: the M adjoint (partials), and the Kg adjoint's W term; the
@@ -431,22 +463,39 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
   }
   g.sync();
   // U = P H^T
-  for (int i = lane; i < d * d; i += LPC) {
-    const int r = i / d, c = i - r * d;
-    Pb[i] += Ub[r * 2] * H[c] + Ub[r * 2 + 1] * H[d + c];
-  }
-  for (int i = lane; i < 2 * d; i += LPC) {
-    const int a = i / d, c = i - a * d;
-    float s = 0.0f;
-    for (int r = 0; r < d; ++r) s = fmaf(Ub[r * 2 + a], Pin[r * d + c], s);
-    Hb[i] += s;
+  if (lane < d) {
+    const float u0 = Ub[lane * 2], u1 = Ub[lane * 2 + 1];   // Pb += Ub H, row lane
+#pragma unroll
+    for (int c = 0; c < D; c += 4) {
+      float4 pq = lds4(Pb + lane * d + c);
+      const float4 h0 = lds4(H + c), h1 = lds4(H + d + c);
+      pq.x += u0 * h0.x + u1 * h1.x;
+      pq.y += u0 * h0.y + u1 * h1.y;
+      pq.z += u0 * h0.z + u1 * h1.z;
+      pq.w += u0 * h0.w + u1 * h1.w;
+      sts4(Pb + lane * d + c, pq);
+    }
+    float s0 = 0.0f, s1 = 0.0f;   // Hb += Ub^T Pin, column lane of both rows
+#pragma unroll
+    for (int r = 0; r < D; ++r) {
+      const float2 u = *reinterpret_cast<const float2*>(Ub + r * 2);
+      const float pin = Pin[r * d + lane];
+      s0 = fmaf(u.x, pin, s0);
+      s1 = fmaf(u.y, pin, s1);
+    }
+    Hb[lane] += s0;
+    Hb[d + lane] += s1;
   }
   g.sync();
   // H = Jp Bj
   float jb = 0.0f;
   if (lane < 6) {
     const int a = lane / 3, t = lane - a * 3;
-    for (int c = 0; c < d; ++c) jb = fmaf(Hb[a * d + c], Bj[t * d + c], jb);
+#pragma unroll 1   // (fully unrolled it costs the 80-register backward spills)
+    for (int c = 0; c < D; c += 4) {
+      const float4 hq = lds4(Hb + a * d + c), bq = ldg4(Bj + t * d + c);
+      jb = fmaf(hq.x, bq.x, jb); jb = fmaf(hq.y, bq.y, jb); jb = fmaf(hq.z, bq.z, jb); jb = fmaf(hq.w, bq.w, jb);
+    }
   }
   float Jb[6];
   for (int q = 0; q < 6; ++q) Jb[q] = g.bcast(jb, q);
@@ -531,9 +580,14 @@ __device__ float frame_forward(const MixArgs& A, float* scr, int SR, float* frg,
     // of the shared stores (generic pointers that could otherwise alias)
     if (lane < d) xk[lane] = fmaf(__ldg(a + lane), s.xh[lane], (1.0f - __ldg(a + lane)) * __ldg(mu + lane));
     const float* Qk = M.Q + (size_t)k * d * d;
-    for (int i = lane; i < d * d; i += LPC) {
-      const int r = i / d, c = i - r * d;
-      Pk[i] = fmaf(__ldg(a + r) * __ldg(a + c), s.Ph[i], __ldg(Qk + i));
+    if (lane < d) {   // Pk = A Ph A + Q, row lane
+      const float ar = __ldg(a + lane);
+#pragma unroll
+      for (int c = 0; c < D; c += 4) {
+        const float4 ac = ldg4(a + c), ph = lds4(s.Ph + lane * d + c), q = ldg4(Qk + lane * d + c);
+        sts4(Pk + lane * d + c, make_float4(fmaf(ar * ac.x, ph.x, q.x), fmaf(ar * ac.y, ph.y, q.y),
+                                            fmaf(ar * ac.z, ph.z, q.z), fmaf(ar * ac.w, ph.w, q.w)));
+      }
     }
     g.sync();
     float ll = 0.0f;
@@ -787,7 +841,13 @@ __global__ void __maxnreg__(REGS) mix_backward_kernel(MixArgs A) {
         float* Dkb = wb + WL.Dkb;
         if (act && lane < d) {
           float v = 0.0f;
-          for (int c = 0; c < d; ++c) v = fmaf(s.Pcb[lane * d + c], xk[c] - xo[c], v);
+#pragma unroll
+          for (int c = 0; c < D; c += 4) {   // xk: this frame's record in the slot (written by this kernel)
+            const float4 pq = lds4(s.Pcb + lane * d + c), xq = *reinterpret_cast<const float4*>(xk + c);
+            const float4 oq = lds4(xo + c);
+            v = fmaf(pq.x, xq.x - oq.x, v); v = fmaf(pq.y, xq.y - oq.y, v);
+            v = fmaf(pq.z, xq.z - oq.z, v); v = fmaf(pq.w, xq.w - oq.w, v);
+          }
           Dkb[lane] = 2.0f * wk * v;
         }
         __syncthreads();
@@ -843,9 +903,18 @@ __global__ void __maxnreg__(REGS) mix_backward_kernel(MixArgs A) {
               const float* Wr = Rs + rec_W(d);
               const float* Kr = Rs + rec_Kg(d);
               float* Pr = Rs + rec_Pin(d);
-              for (int i = lane; i < d * d; i += LPC) {
-                const int r = i / d, c = i - r * d;
-                Pr[i] += Wr[r * 2] * Kr[c * 2] + Wr[r * 2 + 1] * Kr[c * 2 + 1];
+              if (lane < d) {
+                const float w0 = Wr[lane * 2], w1 = Wr[lane * 2 + 1];
+#pragma unroll
+                for (int c = 0; c < D; c += 4) {
+                  float4 pq = lds4(Pr + lane * d + c);
+                  const float4 k01 = lds4(Kr + 2 * c), k23 = lds4(Kr + 2 * c + 4);
+                  pq.x += w0 * k01.x + w1 * k01.y;
+                  pq.y += w0 * k01.z + w1 * k01.w;
+                  pq.z += w0 * k23.x + w1 * k23.y;
+                  pq.w += w0 * k23.z + w1 * k23.w;
+                  sts4(Pr + lane * d + c, pq);
+                }
               }
               g.sync();
             }
@@ -862,18 +931,26 @@ __global__ void __maxnreg__(REGS) mix_backward_kernel(MixArgs A) {
             Xin[lane] = al * xb[lane];
             gmu[lane] += (1.0f - al) * xb[lane];
             float g = (xin[lane] - __ldg(mu + lane)) * xb[lane];
-            for (int c = 0; c < d; ++c)
-              g += (Pb[lane * d + c] * Pin[lane * d + c] + Pb[c * d + lane] * Pin[c * d + lane]) * __ldg(a + c);
+#pragma unroll
+            for (int c = 0; c < D; c += 4) {
+              const float4 pr = lds4(Pb + lane * d + c), qr = lds4(Pin + lane * d + c), ac = ldg4(a + c);
+              g += (pr.x * qr.x + Pb[c * d + lane] * Pin[c * d + lane]) * ac.x;
+              g += (pr.y * qr.y + Pb[(c + 1) * d + lane] * Pin[(c + 1) * d + lane]) * ac.y;
+              g += (pr.z * qr.z + Pb[(c + 2) * d + lane] * Pin[(c + 2) * d + lane]) * ac.z;
+              g += (pr.w * qr.w + Pb[(c + 3) * d + lane] * Pin[(c + 3) * d + lane]) * ac.w;
+              // Pin adjoint A Pb A and the segment's Q adjoint sum, row lane
+              sts4(Pinb + lane * d + c, make_float4(al * ac.x * pr.x, al * ac.y * pr.y, al * ac.z * pr.z,
+                                                    al * ac.w * pr.w));
+              float4 sq = lds4(Sq + lane * d + c);
+              sq.x += pr.x; sq.y += pr.y; sq.z += pr.z; sq.w += pr.w;
+              sts4(Sq + lane * d + c, sq);
+            }
             ga[lane] += g;
           }
-          for (int i = lane; i < d * d; i += LPC) {
-            const int r = i / d, c = i - r * d;
-            Pinb[i] = __ldg(a + r) * __ldg(a + c) * Pb[i];
-            Sq[i] += Pb[i];
-          }
-        } else {
-          if (lane < d) Xin[lane] = 0.0f;
-          for (int i = lane; i < d * d; i += LPC) Pinb[i] = 0.0f;
+        } else if (lane < d) {
+          Xin[lane] = 0.0f;
+#pragma unroll
+          for (int c = 0; c < D; c += 4) sts4(Pinb + lane * d + c, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
         }
         __syncthreads();
         for (int r = tid; r < d; r += TB) {
