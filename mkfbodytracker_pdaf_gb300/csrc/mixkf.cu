@@ -284,14 +284,11 @@ __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const 
   const float C11 = g.sum(beta * n1 * n1) - nb1 * nb1;
   const float M00 = (1.0f - beta0) * S00 - C00, M01 = (1.0f - beta0) * S01 - C01;
   const float M10 = (1.0f - beta0) * S10 - C01, M11 = (1.0f - beta0) * S11 - C11;
-  for (int i = lane; i < 2 * d; i += LPC) {
-    const int r = i >> 1, a = i & 1;
-    Kg[i] = U[r * 2] * (a ? Si01 : Si00) + U[r * 2 + 1] * (a ? Si11 : Si10);
-  }
-  g.sync();
-  for (int i = lane; i < 2 * d; i += LPC) {
-    const int r = i >> 1, a = i & 1;
-    W[i] = Kg[r * 2] * (a ? M01 : M00) + Kg[r * 2 + 1] * (a ? M11 : M10);
+  if (lane < d) {   // Kg = U S^-1 and W = Kg M, row lane (W's row needs only Kg's)
+    const float2 u = *reinterpret_cast<const float2*>(U + lane * 2);
+    const float k0 = u.x * Si00 + u.y * Si10, k1 = u.x * Si01 + u.y * Si11;
+    *reinterpret_cast<float2*>(Kg + lane * 2) = make_float2(k0, k1);
+    *reinterpret_cast<float2*>(W + lane * 2) = make_float2(k0 * M00 + k1 * M10, k0 * M01 + k1 * M11);
   }
   g.sync();
   if (lane < d) {
@@ -384,9 +381,12 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
     r8[0] = Kg[lane * 2] * Wb[lane * 2]; r8[1] = Kg[lane * 2] * Wb[lane * 2 + 1];
     r8[2] = Kg[lane * 2 + 1] * Wb[lane * 2]; r8[3] = Kg[lane * 2 + 1] * Wb[lane * 2 + 1];
   }
-  for (int i = lane; i < 2 * d; i += LPC) {
-    const int r = i >> 1, a = i & 1;
-    Kgb[i] += Wb[r * 2] * (a ? Mm[2] : Mm[0]) + Wb[r * 2 + 1] * (a ? Mm[3] : Mm[1]);
+  if (lane < d) {
+    const float2 w = *reinterpret_cast<const float2*>(Wb + lane * 2);
+    float2 kb = *reinterpret_cast<const float2*>(Kgb + lane * 2);
+    kb.x += w.x * Mm[0] + w.y * Mm[1];
+    kb.y += w.x * Mm[2] + w.y * Mm[3];
+    *reinterpret_cast<float2*>(Kgb + lane * 2) = kb;
   }
   g.sync();
   if (lane < d) {
@@ -411,9 +411,10 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
   nbb1 -= Cs1 * nb0 + Cs3 * nb1;
   g.sync();
   // Kg = U Si
-  for (int i = lane; i < 2 * d; i += LPC) {
-    const int r = i >> 1, a = i & 1;
-    Ub[i] = Kgb[r * 2] * (a ? Si[2] : Si[0]) + Kgb[r * 2 + 1] * (a ? Si[3] : Si[1]);
+  if (lane < d) {
+    const float2 kb = *reinterpret_cast<const float2*>(Kgb + lane * 2);
+    *reinterpret_cast<float2*>(Ub + lane * 2) =
+        make_float2(kb.x * Si[0] + kb.y * Si[1], kb.x * Si[2] + kb.y * Si[3]);
   }
   float Sib[4] = {r8[4], r8[5], r8[6], r8[7]};
   // nb = sum beta nu
@@ -453,13 +454,15 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
   if (lane == 0) sb += 2.0f * M.sigma * (Sb[0] + Sb[3]);
   g.sync();
   // S = H U + sigma^2 I
-  for (int i = lane; i < 2 * d; i += LPC) {
-    const int a = i / d, r = i - a * d;
-    Hb[i] = (a ? Sb[2] : Sb[0]) * U[r * 2] + (a ? Sb[3] : Sb[1]) * U[r * 2 + 1];
-  }
-  for (int i = lane; i < 2 * d; i += LPC) {
-    const int r = i >> 1, c = i & 1;
-    Ub[i] += H[r] * (c ? Sb[1] : Sb[0]) + H[d + r] * (c ? Sb[3] : Sb[2]);
+  if (lane < d) {
+    const float2 u = *reinterpret_cast<const float2*>(U + lane * 2);
+    Hb[lane] = Sb[0] * u.x + Sb[1] * u.y;
+    Hb[d + lane] = Sb[2] * u.x + Sb[3] * u.y;
+    const float h0 = H[lane], h1 = H[d + lane];
+    float2 ub = *reinterpret_cast<const float2*>(Ub + lane * 2);
+    ub.x += h0 * Sb[0] + h1 * Sb[2];
+    ub.y += h0 * Sb[1] + h1 * Sb[3];
+    *reinterpret_cast<float2*>(Ub + lane * 2) = ub;
   }
   g.sync();
   // U = P H^T
