@@ -863,10 +863,20 @@ __global__ void __maxnreg__(REGS) mix_backward_kernel(MixArgs A) {
             for (int q = 0; q < K; ++q) v -= wbase[(size_t)q * WL.size + WL.Dkb + lane];
             xt = v;
           }
-          float wbp = (lane < d) ? xk[lane] * xt : 0.0f;
-          for (int i = lane; i < d * d; i += LPC) {
-            const int r = i / d, c = i - r * d;
-            wbp = fmaf(s.Pcb[i], Pk[i] + (xk[r] - xo[r]) * (xk[c] - xo[c]), wbp);
+          float wbp = 0.0f;
+          if (lane < d) {   // row lane of sum Pcb o (Pk + D D^T), D = xk - xo
+            const float xr = xk[lane];
+            const float dr = xr - xo[lane];
+            wbp = xr * xt;
+#pragma unroll
+            for (int c = 0; c < D; c += 4) {
+              const float4 pq = lds4(s.Pcb + lane * d + c), kq = *reinterpret_cast<const float4*>(Pk + lane * d + c);
+              const float4 xq = *reinterpret_cast<const float4*>(xk + c), oq = lds4(xo + c);
+              wbp = fmaf(pq.x, kq.x + dr * (xq.x - oq.x), wbp);
+              wbp = fmaf(pq.y, kq.y + dr * (xq.y - oq.y), wbp);
+              wbp = fmaf(pq.z, kq.z + dr * (xq.z - oq.z), wbp);
+              wbp = fmaf(pq.w, kq.w + dr * (xq.w - oq.w), wbp);
+            }
           }
           wbk = g.sum(wbp);
           if (lane == 0) s.wb[k] = wbk;
