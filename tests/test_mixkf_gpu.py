@@ -62,6 +62,25 @@ def test_gradient_matches_fp64_adjoint_and_fd(cuda, olib):
         assert abs(v @ grad - fd) <= 1e-4 * max(1.0, abs(fd)), (name, v @ grad, fd)
 
 
+def test_three_ctas_per_sm_instantiation_matches_oracle(cuda, olib):
+    """More tracks than two CTAs per SM hold: the create call picks the
+    80-register instantiation of both kernels (three CTAs per SM) that the
+    1024-track workload runs.  Forward and gradient against the FP64 CPU."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    b, om, th, g = _setup(olib, n_tracks=2 * sms + 16, T=12, K=15, seed=9)
+    g.set_theta(th)
+    g.forward()
+    ll = g.ll.cpu().numpy()
+    grad = g.backward().cpu().numpy()
+    L, ll_ref, gref = olib.mix_batch(om, b, grad=True)
+    np.testing.assert_allclose(ll, ll_ref, rtol=1e-4)
+    nw = np.linalg.norm(grad - gref) / np.linalg.norm(gref)
+    print("d12 K15 %d tracks normwise rel err vs FP64 adjoint: %.3g" % (b.n_tracks, nw))
+    assert nw < 5e-5, nw
+    assert g.status() == 0
+
+
 def test_gradient_deterministic(cuda, olib):
     b, om, th, g = _setup(olib, n_tracks=5, T=20)
     g.set_theta(th)
