@@ -31,22 +31,19 @@ namespace mkf {
 constexpr int kMixMaxC = MKF_MAX_DET;
 constexpr float kMixZMin = 0.05f;
 
-// joint record layout (floats); float 95 is padding, so that H, U, Kg, W, the
-// saved state and the saved covariance all start on a 16-byte boundary
+// joint record layout (floats); float 95 is padding, so that H, U, Kg and W
+// start on a 16-byte boundary
 enum {
   R_VIS = 0, R_N = 1, R_P3 = 2, R_IZ = 5, R_ZH = 6, R_JP = 8, R_S = 14, R_SI = 18, R_LD = 22,
   R_ELL = 23, R_B0 = 24, R_NB = 25, R_M = 27, R_NU = 31, R_E = 63, R_BETA = 79, R_H = 96
 };
-// At d <= 16 a record also keeps the state and covariance entering the update
-// (rec_X, rec_Pin); at d = 24 it ends at rec_X, and the reverse sweep rebuilds
-// the entering covariance from the component's final one and the records'
-// gains (P_in = P_out + W Kg^T, joint by joint backwards): a record is then 288
-// floats instead of 888, so that one segment of every resident CTA's records
-// stays in L2
-__host__ __device__ inline bool rec_keeps_P(int d) { return d <= 16; }
-__host__ __device__ inline int rec_size(int d) {
-  return rec_keeps_P(d) ? (R_H + 9 * d + d * d + 3) & ~3 : (R_H + 8 * d + 3) & ~3;
-}
+// A record ends at rec_X: it does not keep the covariance entering the update.
+// The reverse sweep rebuilds it in the group's scratch (rec_X .. rec_Pin + d^2
+// there) from the component's final covariance and the records' gains,
+// P_in = P_out + W Kg^T joint by joint backwards: a record is 192 floats
+// instead of 348 at d = 12 (288 instead of 888 at d = 24), so that more frames
+// of every resident CTA's records fit in L2
+__host__ __device__ inline int rec_size(int d) { return (R_H + 8 * d + 3) & ~3; }
 __host__ __device__ inline int rec_U(int d) { return R_H + 2 * d; }
 __host__ __device__ inline int rec_Kg(int d) { return R_H + 4 * d; }
 __host__ __device__ inline int rec_W(int d) { return R_H + 6 * d; }
@@ -217,10 +214,6 @@ __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const 
   float* Kg = R + rec_Kg(d);
   float* W = R + rec_W(d);
   const bool rec = Rg != nullptr;
-  if (rec && rec_keeps_P(d)) {   // x and P are contiguous, and so are their record copies (d % 4 == 0)
-    copy_s2g<(D + D * D) / 4, LPC>(reinterpret_cast<float4*>(Rg + rec_X(d)), reinterpret_cast<const float4*>(x),
-                                   lane);
-  }
   float pt = 0.0f;
   if (lane < 3) {
     pt = mj[lane];
@@ -906,12 +899,12 @@ __global__ void __maxnreg__(REGS) mix_backward_kernel(MixArgs A) {
             // (plain copies through registers wait out each load before its store)
             const float* src = cb + j * rec_size(d);
             for (int q = lane; q < RS4; q += LPC) cp_async16(Rs + 4 * q, src + 4 * q);
-            if (!rec_keeps_P(d) && j == J - 1)   // the component's final covariance, rebuilt backwards below
+            if (j == J - 1)   // the component's final covariance, rebuilt backwards below
               for (int q = lane; q < D * D / 4; q += LPC) cp_async16(Rs + rec_Pin(d) + 4 * q, Pk + 4 * q);
             cp_async_commit();
             cp_async_wait_all();
             g.sync();
-            if (!rec_keeps_P(d) && Rs[R_VIS] != 0.0f) {
+            if (Rs[R_VIS] != 0.0f) {
               // the covariance entering joint j: the forward's P -= W Kg^T undone
               const float* Wr = Rs + rec_W(d);
               const float* Kr = Rs + rec_Kg(d);
