@@ -31,11 +31,13 @@ namespace mkf {
 constexpr int kMixMaxC = MKF_MAX_DET;
 constexpr float kMixZMin = 0.05f;
 
-// joint record layout (floats); float 95 is padding, so that H, U, Kg and W
-// start on a 16-byte boundary
+// joint record layout (floats): the 2x2 matrices S, S^-1 and M and the
+// scalar groups (VIS, N, B0, ELL) and (NB, IZ, LD) each on a 16-byte boundary,
+// so that the reverse reads each with one 16-byte load; float 23 is padding;
+// H, U, Kg and W start on a 16-byte boundary
 enum {
-  R_VIS = 0, R_N = 1, R_P3 = 2, R_IZ = 5, R_ZH = 6, R_JP = 8, R_S = 14, R_SI = 18, R_LD = 22,
-  R_ELL = 23, R_B0 = 24, R_NB = 25, R_M = 27, R_NU = 31, R_E = 63, R_BETA = 79, R_H = 96
+  R_S = 0, R_SI = 4, R_M = 8, R_VIS = 12, R_N = 13, R_B0 = 14, R_ELL = 15, R_NB = 16, R_IZ = 18, R_LD = 19,
+  R_P3 = 20, R_JP = 24, R_ZH = 30, R_NU = 32, R_E = 64, R_BETA = 80, R_H = 96
 };
 // A record ends at rec_X: it does not keep the covariance entering the update.
 // The reverse sweep rebuilds it in the group's scratch (rec_X .. rec_Pin + d^2
@@ -324,10 +326,11 @@ __device__ float joint_fwd(const MixDev& M, float* R, float* x, float* P, const 
 template <int D>
 __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, float pd, float kappa, float* xb,
                           float* Pb, float gl, float* tmp, float& sb, const Grp<lpc_of<D>()>& g) {
-  if (R[R_VIS] == 0.0f) return;
+  const float4 hd = lds4(R + R_VIS);   // VIS, N, B0, ELL
+  if (hd.x == 0.0f) return;
   constexpr int d = D, LPC = lpc_of<D>();
   const int lane = g.sub;
-  const int n = (int)R[R_N];
+  const int n = (int)hd.y;
   const float* H = R + R_H;
   const float* U = R + rec_U(d);
   const float* Kg = R + rec_Kg(d);
@@ -337,11 +340,13 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
   float* Wb = tmp + 2 * d;
   float* Ub = tmp + 4 * d;
   float* Hb = tmp + 6 * d;
-  const float nb0 = R[R_NB], nb1 = R[R_NB + 1];
-  const float S[4] = {R[R_S], R[R_S + 1], R[R_S + 2], R[R_S + 3]};
-  const float Si[4] = {R[R_SI], R[R_SI + 1], R[R_SI + 2], R[R_SI + 3]};
-  const float Mm[4] = {R[R_M], R[R_M + 1], R[R_M + 2], R[R_M + 3]};
-  const float beta0 = R[R_B0], ell = R[R_ELL];
+  const float2 nbq = *reinterpret_cast<const float2*>(R + R_NB);
+  const float nb0 = nbq.x, nb1 = nbq.y;
+  const float4 S4 = lds4(R + R_S), Si4 = lds4(R + R_SI), M4 = lds4(R + R_M);
+  const float S[4] = {S4.x, S4.y, S4.z, S4.w};
+  const float Si[4] = {Si4.x, Si4.y, Si4.z, Si4.w};
+  const float Mm[4] = {M4.x, M4.y, M4.z, M4.w};
+  const float beta0 = hd.z, ell = hd.w;
   const float b = (1.0f - pd) * kappa;
   // x' = x + Kg nb
   float t2[2] = {0.0f, 0.0f};
@@ -395,7 +400,8 @@ __device__ void joint_bwd(const MixDev& M, const float* R, const float* Bj, floa
   const float Cs0 = 2.0f * Cnb[0], Cs1 = Cnb[1] + Cnb[2], Cs3 = 2.0f * Cnb[3];
   float n0 = 0.0f, n1 = 0.0f, be = 0.0f, ee = 0.0f, betab = 0.0f, nub0 = 0.0f, nub1 = 0.0f;
   if (lane < n) {
-    n0 = R[R_NU + 2 * lane]; n1 = R[R_NU + 2 * lane + 1]; be = R[R_BETA + lane]; ee = R[R_E + lane];
+    const float2 nu = *reinterpret_cast<const float2*>(R + R_NU + 2 * lane);
+    n0 = nu.x; n1 = nu.y; be = R[R_BETA + lane]; ee = R[R_E + lane];
     betab = n0 * (Cnb[0] * n0 + Cnb[1] * n1) + n1 * (Cnb[2] * n0 + Cnb[3] * n1);
     nub0 = be * (Cs0 * n0 + Cs1 * n1);
     nub1 = be * (Cs1 * n0 + Cs3 * n1);
