@@ -115,8 +115,6 @@ struct MixArgs {
   int* status;
 };
 
-__device__ __forceinline__ float wsum(float v) { return warp_sum(v); }
-
 // Lanes per mixture component: half a warp (two components per warp) when a
 // component's d-wide work fits in 16 lanes, else the whole warp.  The d-wide
 // phases, scalar steps and reductions of the per-component Kalman algebra then
@@ -201,8 +199,8 @@ __device__ __forceinline__ void copy_s2g(float4* dst, const float4* src, int lan
   }
 }
 
-// sequential PDAF/EKF update of one joint for one component (whole warp)
-// R: this warp's scratch record (shared memory, R_H + 8d floats, 16-byte
+// sequential PDAF/EKF update of one joint for one component (its lane group)
+// R: this group's scratch record (shared memory, R_H + 8d floats, 16-byte
 // aligned); x, P: the component state (shared memory, updated in place, P = x + d,
 // 16-byte aligned); Rg: when non-null the global record (16-byte aligned) that
 // keeps this update for the reverse sweep
@@ -554,10 +552,12 @@ __device__ __forceinline__ void select_frame_dets(Smem& s, int f) {
   s.cnt = s.dcnt + f * MKF_MAX_J;
 }
 
-// per-warp shared scratch of the frame forward: xk (d), Pk (d*d), record (R_H + 8d)
+// per-group shared scratch of the frame forward: xk (d), Pk (d*d), record (R_H + 8d);
+// in the reverse sweep a joint record (R_H + 8d) and the entering covariance
+// rebuilt behind it (rec_Pin .. rec_Pin + d*d)
 __host__ __device__ inline int fwd_scratch_floats(int d) { return (d + d * d + R_H + 8 * d + 3) & ~3; }
 
-// one frame forward (all warps); each warp's component lives in its shared
+// one frame forward (all groups); each group's component lives in its shared
 // scratch (stride SR floats from scr); when frg is non-null the component
 // records and states are also kept in the global frame record frg.  Returns
 // c_t (valid in every thread); s.w, s.xo, s.Po hold the mixture weights and
@@ -697,7 +697,7 @@ template <int D, int REGS>
 __global__ void __maxnreg__(REGS) mix_forward_kernel(MixArgs A) {
   extern __shared__ __align__(16) float msm[];
   Smem s;
-  float* scr = carve(s, msm, D);                 // per-warp component scratch follows
+  float* scr = carve(s, msm, D);                 // per-group component scratch follows
   constexpr int d = D;
   const int J = A.M.J;
   const int tid = threadIdx.x, TB = blockDim.x;
@@ -1192,8 +1192,12 @@ static int mix_occ(MixKernel kern, int tpb, size_t smem, int* occ) {
 // shared-memory sizes, STAGE choice and the persistent grid
 static int mix_grid(mkf_mixkf* h) {
   const int d = h->d, K = h->K;
-  // the reverse sweep stages one joint record in a warp's forward scratch
-  if (rec_size(d) > fwd_scratch_floats(d)) { set_error("mkf_mixkf: record larger than the warp scratch"); return MKF_ERR_ARG; }
+  // the reverse sweep stages one joint record and the rebuilt entering
+  // covariance in a group's forward scratch
+  if (rec_Pin(d) + d * d > fwd_scratch_floats(d)) {
+    set_error("mkf_mixkf: record larger than the group scratch");
+    return MKF_ERR_ARG;
+  }
   const WorkLayout WL = work_layout(d);
   const size_t base = mix_smem_bytes(d);
   const int SRf = fwd_scratch_floats(d);
